@@ -1,0 +1,341 @@
+"""Benchmark: env-steps/s of the multi-environment soft-tissue step at 4096 environments.
+
+Workload (one "step"): every environment of a 4096-env batch drawn from a pool of
+mixed-size ellipsoids (tet counts log-uniform in [500, 20000]) takes one RL step --
+instrument displacement (0.5 mm random walk), 8 substeps x 10 Jacobi iterations of
+Neo-Hookean + volume + distance constraints with grasp and instrument contact, BVH refit,
+and a 128x128 (2x2 supersampled) depth + colour ray-cast per environment.
+
+  value  -- env-steps/s with inputs resident in HBM (CUDA events on the stream)
+  e2e    -- the same through the public API with host buffers: each step copies the
+            actions (N x 4 float32 from pinned memory) to the device and reads back the
+            per-env result (effector position + contact count, N x 4 float32)
+  plain  -- the reference-shaped drop-in (one launch per reference kernel) on the same GPU
+
+`--impl reference` times the reference algorithm's CPU implementation (the C++
+restatement, all host threads) on a bounded sample of the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "ff-srl_gb300"))
+
+METRIC = "env-steps/s at 4096 envs"
+NUM_ENVS = 4096
+RES = 128
+POOL = 64
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ffsrl", choices=["ffsrl", "reference"])
+    ap.add_argument("--envs", type=int, default=NUM_ENVS)
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    return rank, world, local
+
+
+def config(envs, n):
+    return {"workload": f"{envs} mixed-size ellipsoid envs (tets log-uniform 500-20000), 8 substeps x 10 iterations, "
+                        f"Neo-Hookean+volume+distance+grasp+contact, BVH refit, {RES}x{RES} depth+colour ray-cast",
+            "envs_per_gpu": envs, "pool_meshes": POOL, "substeps": 8, "iterations": 10, "resolution": RES,
+            "parallelism": f"env-shard x{n}", "l2": "working set (GBs) exceeds the 129 MB L2; no flush needed"}
+
+
+class Clocks:
+    """Samples nvidia-smi SM clocks and throttle reasons while active."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[0]) for r in self.rows if len(r) >= 7 and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) >= 7 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) >= 7 for i in range(4) if r[3 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(sm)}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            for k in ("hbm_gbs", "hbm_GBs", "hbm"):
+                if k in d:
+                    return float(d[k]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def algorithmic_bytes(model, substeps=8, iterations=10, nh=True):
+    """Per-step compulsory bytes of the constraint solve, summed over envs:
+    B_iter = V*32 + E*12 + T*(20 [+36 NH]) + F*12; B_sub = I*B_iter + V*48; B = S*B_sub."""
+    V, E, T, F = model.numVertices, model.numEdges, model.numTetrahedrons, model.numTriangles
+    b_iter = V * 32 + E * 12 + T * (20 + (36 if nh else 0)) + F * 12
+    return substeps * (iterations * b_iter + V * 48)
+
+
+def build_workload(device, envs, seed):
+    import torch
+    from ffsrl import SimBVH, SimIntegratorDO, WarpRaycastRendererDO, scenarios as sc
+    meshes, pool = sc.mixed_meshes(envs, pool_size=POOL, seed=seed)
+    m, _ = sc.liver_model(device, envs, meshes=meshes)
+    bvh = SimBVH(device, m)
+    ap = sc.fov_aperture(60.0)
+    r = WarpRaycastRendererDO(device, m, resolution=RES, mode="headless", verticalAperture=ap,
+                              horizontalAperture=ap, lightPos=(0.3, 1.0, 0.5), lightIntensity=0.8)
+    pos, rot = sc.env_cameras(meshes, seed=seed + 1)
+    r.setCameras(pos, rot)
+    m.graspNearest(torch.ones(envs, dtype=torch.int32, device=device), radius=0.3)
+    return m, meshes, bvh, r
+
+
+def cpu_sample(meshes, threads, n_env=16, seed=0):
+    """Oracle (C++ restatement) env-steps/s on a bounded sample of the workload."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    from ffsrl import scenarios as sc
+    m, _ = sc.liver_model("cpu", n_env, meshes=meshes[:n_env])
+    o = oracle.OracleSim(m)
+    t0 = time.perf_counter()
+    o.step(1, threads=threads)
+    dt = time.perf_counter() - t0
+    return n_env / dt, dt
+
+
+def reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from ffsrl import scenarios as sc
+    threads = os.cpu_count() or 1
+    meshes, _ = sc.mixed_meshes(args.envs, pool_size=POOL, seed=0)
+    sample = 32
+    for _ in range(args.warmup):
+        cpu_sample(meshes, threads, n_env=sample)
+    vals = []
+    for k in range(args.steps):
+        v, dt = cpu_sample(meshes[k * sample % (len(meshes) - sample):], threads, n_env=sample)
+        vals.append(v)
+    v = float(np.mean(vals))
+    line = {"metric": METRIC, "value": v, "unit": "env-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * sample / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": config(args.envs, world) | {"sample": f"{sample} envs x 1 step per timed step"},
+            "cpu_baseline": {"value": v, "unit": "env-steps/s", "cores": threads, "kind": "port",
+                             "sample": f"{sample} envs of the same pool, 1 step (8x10 solve only, no render)"},
+            "e2e": {"value": v, "unit": "env-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+    torch.cuda.set_device(local)
+    device = f"cuda:{local}"
+    envs = args.envs
+    m, meshes, bvh, r = build_workload(device, envs, seed=rank)
+    from ffsrl import SimIntegratorDO, scenarios as sc, _lib as L
+    integ = SimIntegratorDO(device)
+    plan = integ.plan(m)
+    n_cls = plan.info()["num_classes"]
+    K, W = args.steps, max(args.warmup, 3)
+    walk = torch.as_tensor(sc.random_walk_steps(envs, K + W, seed=rank + 100), device=device)
+    stream = torch.cuda.current_stream()
+
+    def step(k):
+        m.moveTool(walk[k])
+        integ.stepModel(m, 1)
+        bvh.refitBVH()
+        r.renderNew(bvh, m)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    for k in range(W):
+        step(k)
+    barrier()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(K + 1)]
+    with Clocks(local) as clk:
+        evs[0].record(stream)
+        for k in range(K):
+            step(W + k)
+            evs[k + 1].record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    per = [evs[k].elapsed_time(evs[k + 1]) for k in range(K)]
+    total_ms = evs[0].elapsed_time(evs[K])
+    if world > 1:
+        t = torch.tensor([total_ms], device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    r.checkErrors()
+    status = integ.envStatus(m)
+    value = envs * world * K / (total_ms / 1000.0)
+
+    # dominant kernel: the batched step alone
+    ks = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    kreps = max(3, K // 2)
+    integ.plan(m).step(1)
+    torch.cuda.synchronize()
+    ks[0].record(stream)
+    for _ in range(kreps):
+        plan.step(1)
+    ks[1].record(stream)
+    torch.cuda.synchronize()
+    step_kernel_ms = ks[0].elapsed_time(ks[1]) / kreps
+    alg = algorithmic_bytes(m)
+    peak, peak_kind = peaks()
+    achieved = alg / (step_kernel_ms / 1000.0) / 1e9
+    prof = ROOT / "profiles" / "batched_step_traffic.json"
+    traffic = None
+    if prof.exists():
+        try:
+            d = json.loads(prof.read_text())
+            traffic = d["dram_bytes_per_env_step"] * envs
+        except Exception:
+            traffic = None
+
+    # end to end through the public API with host buffers
+    act_h = torch.empty((envs, 4), dtype=torch.float32, pin_memory=True)
+    res_h = torch.empty((envs, 4), dtype=torch.float32, pin_memory=True)
+    act_d = torch.empty((envs, 4), dtype=torch.float32, device=device)
+    res_d = torch.empty((envs, 4), dtype=torch.float32, device=device)
+    walk_h = walk.cpu()
+
+    def e2e_step(k):
+        act_h[:, :3] = walk_h[k % len(walk_h)]
+        act_h[:, 3] = 1.0
+        act_d.copy_(act_h, non_blocking=True)
+        m.moveTool(act_d[:, :3].contiguous())
+        integ.stepModel(m, 1)
+        bvh.refitBVH()
+        r.renderNew(bvh, m)
+        res_d[:, :3] = m.laparoscopeTip[3::4]
+        res_d[:, 3] = m.laparoscopeInCollision.float()
+        res_h.copy_(res_d, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+
+    for k in range(W):
+        e2e_step(k)
+    barrier()
+    t0 = time.perf_counter()
+    for k in range(K):
+        e2e_step(k)
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    e2e = envs * world * K / e2e_s
+
+    plain = None
+    if not args.no_plain:
+        pint = SimIntegratorDO(device, batched=False)
+        pint.stepModel(m, 1)
+        torch.cuda.synchronize()
+        pe = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        pk = 2
+        pe[0].record(stream)
+        for k in range(pk):
+            m.moveTool(walk[k])
+            pint.stepModel(m, 1)
+            bvh.refitBVH(fused=False)
+            r.fused = False
+            r.renderNew(bvh, m)
+            r.fused = True
+        pe[1].record(stream)
+        torch.cuda.synchronize()
+        plain_ms = pe[0].elapsed_time(pe[1]) / pk
+        plain = {"value": envs / (plain_ms / 1000.0), "unit": "env-steps/s", "ms_per_step": plain_ms,
+                 "speedup_batched_vs_plain": value / world / (envs / (plain_ms / 1000.0))}
+
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu:
+            threads = os.cpu_count() or 1
+            v, dt = cpu_sample(meshes, threads, n_env=32)
+            cpu = {"value": v, "unit": "env-steps/s", "cores": threads, "kind": "port",
+                   "sample": "32 envs of the same pool, 1 step (8x10 solve only, no render), oracle restatement"}
+        launches = K * (n_cls + 4)
+        line = {"metric": METRIC, "value": value, "unit": "env-steps/s", "n_gpus": world, "steps": K,
+                "warmup": W, "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded meshes and random-walk actions)",
+                "config": config(envs, world),
+                "latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99)),
+                               "what": "full-batch step latency (all envs), per timed step"},
+                "e2e": {"value": e2e, "unit": "env-steps/s", "h2d_bytes_per_step": envs * 16,
+                        "d2h_bytes_per_step": envs * 16},
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                             "kernel": "k_batched (batched step, all size classes)", "kernel_ms": step_kernel_ms},
+                "cpu_baseline": cpu, "plain": plain, "gpu_launches": launches,
+                "clocks": clk.summary(), "env_status_nonzero": int((status != 0).sum())}
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

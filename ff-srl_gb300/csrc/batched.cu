@@ -1,0 +1,1012 @@
+// batched.cu -- env-resident batched step.
+//
+// One thread block owns one environment at a time and runs every substep and
+// iteration of the step for it without leaving the SM: the env's predicted positions
+// (with the inverse mass in .w) and its per-vertex correction accumulators live in
+// shared memory, the read-only constraint tables stream from L2/HBM in coalesced
+// structure-of-arrays records with 16-bit env-local vertex ids.  Blocks are persistent
+// and take environments from a largest-first work list through an atomic counter, so
+// meshes of uneven size share the GPU in one launch per size class.
+//
+// Semantics are SimIntegratorDO.stepModel's (FF_SRL/FF_SRL/integrator.py:1640-1741),
+// Jacobi iteration unchanged: all constraint projections of an iteration read the same
+// positions, their corrections are summed per vertex and divided by the number of
+// contributing constraints (applyConstraints, integrator.py:946-960), then the grasp
+// (dragConstraintsDO) and the instrument contact (collideLaparoscopeDO).
+//
+// Accumulation is deterministic: in float32 runs each correction component is rounded
+// once to a 64-bit fixed-point integer (scale 2^40, resolution 9.1e-13 m, range
+// +-8.4e6 m) and summed with integer atomics, which are associative, so the result does
+// not depend on thread order and an environment gives the same bits alone or in any
+// batch.  The float64 build of the same kernel (used for the precision report) sums in
+// double.
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <vector>
+#include <algorithm>
+#include <numeric>
+#include <cstring>
+#include <string>
+#include "ffsrl_internal.h"
+
+namespace ffsrl {
+namespace {
+
+#define BEPS 2.220446049250313e-16
+
+template <class R> struct t3 { R x, y, z; };
+template <class R> __device__ __forceinline__ t3<R> T3(R x, R y, R z) { t3<R> r; r.x = x; r.y = y; r.z = z; return r; }
+template <class R> __device__ __forceinline__ t3<R> operator+(t3<R> a, t3<R> b) { return T3<R>(a.x + b.x, a.y + b.y, a.z + b.z); }
+template <class R> __device__ __forceinline__ t3<R> operator-(t3<R> a, t3<R> b) { return T3<R>(a.x - b.x, a.y - b.y, a.z - b.z); }
+template <class R> __device__ __forceinline__ t3<R> operator-(t3<R> a) { return T3<R>(-a.x, -a.y, -a.z); }
+template <class R> __device__ __forceinline__ t3<R> operator*(t3<R> a, R s) { return T3<R>(a.x * s, a.y * s, a.z * s); }
+template <class R> __device__ __forceinline__ t3<R> operator*(R s, t3<R> a) { return T3<R>(s * a.x, s * a.y, s * a.z); }
+template <class R> __device__ __forceinline__ t3<R> operator/(t3<R> a, R s) { return T3<R>(a.x / s, a.y / s, a.z / s); }
+template <class R> __device__ __forceinline__ R dot(t3<R> a, t3<R> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <class R> __device__ __forceinline__ t3<R> cross(t3<R> a, t3<R> b) {
+    return T3<R>(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+template <class R> __device__ __forceinline__ R length(t3<R> a) { return sqrt(dot(a, a)); }
+template <class R> __device__ __forceinline__ t3<R> normalize(t3<R> a) {
+    R l = length(a);
+    if (l > R(0)) return a / l;
+    return T3<R>(0, 0, 0);
+}
+template <class R> __device__ __forceinline__ R rmin(R a, R b) { return a < b ? a : b; }
+template <class R> __device__ __forceinline__ R rmax(R a, R b) { return a > b ? a : b; }
+
+// per-precision storage: predicted position + inverse mass, accumulator word
+template <class R> struct Store;
+template <> struct Store<float> {
+    typedef float4 P;
+    typedef unsigned long long A;
+    __device__ static t3<float> pos(const P& p) { return T3<float>(p.x, p.y, p.z); }
+    __device__ static P make(t3<float> v, float w) { return make_float4(v.x, v.y, v.z, w); }
+    __device__ static void add(A* a, float v) {
+        atomicAdd(a, (unsigned long long)__float2ll_rn(v * 1099511627776.0f));
+    }
+    __device__ static float get(A a) { return __ll2float_rn((long long)a) * 9.094947017729282e-13f; }
+};
+struct __align__(32) dpos { double x, y, z, w; };
+template <> struct Store<double> {
+    typedef dpos P;
+    typedef double A;
+    __device__ static t3<double> pos(const P& p) { return T3<double>(p.x, p.y, p.z); }
+    __device__ static P make(t3<double> v, double w) { P r; r.x = v.x; r.y = v.y; r.z = v.z; r.w = w; return r; }
+    __device__ static void add(A* a, double v) { atomicAdd(a, v); }
+    __device__ static double get(A a) { return a; }
+};
+
+struct EnvRec { int v0, nv, t0, nt, e0, ne, f0, nf; };
+
+// adds a correction vector to vertex i's accumulator; a non-finite component (which
+// the fixed-point form cannot carry) raises `bad` so the env is reported non-finite
+template <class R> __device__ __forceinline__ void add3(typename Store<R>::A* acc, int i, t3<R> d, bool& bad) {
+    Store<R>::add(acc + 3 * i, d.x);
+    Store<R>::add(acc + 3 * i + 1, d.y);
+    Store<R>::add(acc + 3 * i + 2, d.z);
+    bad |= !(isfinite(d.x) && isfinite(d.y) && isfinite(d.z));
+}
+
+template <class R> struct Dev {
+    const EnvRec* env;
+    const uint2* tet_idx;      // 4 x u16 local ids
+    const float2* tet_va;      // (|V0|, active)
+    const float4* dmA;         // Dm^-1 row-major entries 0..3
+    const float4* dmB;         // entries 4..7
+    const float* dmC;          // entry 8
+    const float* tet_vs;       // signed rest volume (XPBD)
+    const unsigned* edge_idx;  // 2 x u16 local ids
+    const float2* edge_la;     // (L0, active)
+    const uint2* tri_idx;      // (a | b<<16, c | hole<<16)
+    R* vertex; R* velocity; R* predicted;
+    const float* inv_mass; const float* drag;
+    const float* lap_base; const float* lap_tip; const float* lap_radius;
+    int* in_collision;
+    float* tet_lambda; float* edge_lambda;
+    int* env_status;
+    unsigned flags;
+    int substeps, iterations;
+    float dt, gx, gy, gz, damping, ground;
+    float ks_distance, ks_volume, ks_contact, ks_drag;
+    float vol_c, dev_c, a_dist, a_vol;
+};
+
+template <class R> __device__ __forceinline__ t3<R> ldgen3(const R* p, long long i) { return T3<R>(p[3 * i], p[3 * i + 1], p[3 * i + 2]); }
+template <class R> __device__ __forceinline__ void stg3(R* p, long long i, t3<R> v) { p[3 * i] = v.x; p[3 * i + 1] = v.y; p[3 * i + 2] = v.z; }
+__device__ __forceinline__ t3<float> ldf3(const float* __restrict__ p, long long i) {
+    return T3<float>(__ldg(p + 3 * i), __ldg(p + 3 * i + 1), __ldg(p + 3 * i + 2));
+}
+template <class R> __device__ __forceinline__ t3<R> prom(t3<float> a) { return T3<R>(R(a.x), R(a.y), R(a.z)); }
+
+template <class R> __device__ __forceinline__ t3<R> closest_on_edge(t3<R> p, t3<R> a, t3<R> b) {
+    t3<R> d = b - a;
+    R t;
+    if (length(d) < R(BEPS)) {
+        t = R(0.5);
+    } else {
+        R ld = length(d);
+        R d2 = ld * ld;
+        t = dot(d, p - a) / d2;
+        if (t < R(0)) t = R(0);
+        else if (t > R(1)) t = R(1);
+    }
+    return a + d * t;
+}
+
+template <class R> __device__ __forceinline__ t3<R> closest_bary(t3<R> a, t3<R> b, t3<R> c, t3<R> p) {
+    t3<R> ab = b - a, ac = c - a, ap = p - a;
+    R d1 = dot(ab, ap), d2 = dot(ac, ap);
+    if (d1 <= R(0) && d2 <= R(0)) return T3<R>(1, 0, 0);
+    t3<R> bp = p - b;
+    R d3 = dot(ab, bp), d4 = dot(ac, bp);
+    if (d3 >= R(0) && d4 <= d3) return T3<R>(0, 1, 0);
+    R vc = d1 * d4 - d3 * d2;
+    R v = d1 / (d1 - d3);
+    if (vc <= R(0) && d1 >= R(0) && d3 <= R(0)) return T3<R>(R(1) - v, v, 0);
+    t3<R> cp = p - c;
+    R d5 = dot(ab, cp), d6 = dot(ac, cp);
+    if (d6 >= R(0) && d5 <= d6) return T3<R>(0, 0, 1);
+    R vb = d5 * d2 - d1 * d6;
+    R w = d2 / (d2 - d6);
+    if (vb <= R(0) && d2 >= R(0) && d6 <= R(0)) return T3<R>(R(1) - w, 0, w);
+    R va = d3 * d6 - d5 * d4;
+    w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+    if (va <= R(0) && (d4 - d3) >= R(0) && (d5 - d6) >= R(0)) return T3<R>(0, w, R(1) - w);
+    R denom = R(1) / (va + vb + vc);
+    v = vb * denom;
+    w = vc * denom;
+    return T3<R>(R(1) - v - w, v, w);
+}
+
+// checkSdfCapsuleCollision (integrator.py:1302-1355)
+template <class R> __device__ __forceinline__ bool capsule_response(t3<R> tip, t3<R> base, R radius, t3<R> n,
+                                                                    t3<R> centre, t3<R> pA, t3<R> pB, t3<R> pC, R ks,
+                                                                    t3<R>& rA, t3<R>& rB, t3<R>& rC) {
+    t3<R> cn = normalize(tip - base);
+    t3<R> off = cn * radius;
+    t3<R> posA = base + off;
+    t3<R> posB = tip - off;
+    R denom = dot(n, cn);
+    if (fabs(denom) < R(BEPS)) return false;
+    R t = dot(n, centre - base) / denom;
+    t3<R> lp = base + cn * t;
+    t3<R> ref = closest_bary(pA, pB, pC, lp);
+    t3<R> sc = closest_on_edge(ref, posA, posB);
+    t3<R> bary = closest_bary(pA, pB, pC, sc);
+    t3<R> contact = pA * bary.x + pB * bary.y + pC * bary.z;
+    t3<R> sv = sc - contact;
+    R dist = length(sv);
+    R pen = radius / length(sv) - R(1);
+    t3<R> pv = T3<R>(pen * sv.x, pen * sv.y, pen * sv.z);
+    R plen = length(pv);
+    t3<R> pn = normalize(pv);
+    R sq = bary.x * bary.x + bary.y * bary.y + bary.z * bary.z;
+    if (sq < R(BEPS)) return false;
+    t3<R> resp = pn * (plen / sq) * ks;
+    if (dist > radius) return false;
+    rA = resp * bary.x; rB = resp * bary.y; rC = resp * bary.z;
+    return true;
+}
+
+template <class R> struct ToolShared {
+    t3<R> base[3], tip[3];
+    R radius[3];
+    t3<R> blo[3], bhi[3];  // conservative contact boxes per capsule
+    t3<R> drag_tip;
+};
+
+// MODE 0: positions and accumulators in shared memory.  MODE 1: positions in shared
+// memory, accumulators in the block's global scratch.  MODE 2: both in global scratch.
+template <class R, int BLOCK, int MODE>
+__global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __restrict__ work, int nwork,
+                                                   int* counter, int nsteps, unsigned char* scratch,
+                                                   long long scratch_stride, int max_nv) {
+    typedef Store<R> S;
+    typedef typename S::P P;
+    typedef typename S::A A;
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int s_work;
+    __shared__ int s_incol;
+    __shared__ int s_bad;
+    __shared__ int s_any_contact;
+    __shared__ int s_any_drag;
+    __shared__ ToolShared<R> tool;
+
+    unsigned char* gbase = scratch + (long long)blockIdx.x * scratch_stride;
+    const int tid = threadIdx.x;
+    const R dt = R(D.dt);
+    const unsigned fl = D.flags;
+
+    for (;;) {
+        if (tid == 0) s_work = atomicAdd(counter, 1);
+        __syncthreads();
+        const int w = s_work;
+        if (w >= nwork) return;
+        const int env = work[w];
+        const EnvRec E = D.env[env];
+        const int nv = E.nv, nt = E.nt, ne = E.ne, nf = E.nf;
+
+        P* xp;
+        A* acc;
+        int* cnt;
+        unsigned* dbits;
+        if (MODE == 0) {
+            xp = reinterpret_cast<P*>(smem);
+            acc = reinterpret_cast<A*>(smem + sizeof(P) * (size_t)max_nv);
+            cnt = reinterpret_cast<int*>(smem + (sizeof(P) + 3 * sizeof(A)) * (size_t)max_nv);
+            dbits = reinterpret_cast<unsigned*>(smem + (sizeof(P) + 3 * sizeof(A) + sizeof(int)) * (size_t)max_nv);
+        } else if (MODE == 1) {
+            xp = reinterpret_cast<P*>(smem);
+            dbits = reinterpret_cast<unsigned*>(smem + sizeof(P) * (size_t)max_nv);
+            acc = reinterpret_cast<A*>(gbase);
+            cnt = reinterpret_cast<int*>(gbase + 3 * sizeof(A) * (size_t)max_nv);
+        } else {
+            dbits = reinterpret_cast<unsigned*>(smem);
+            xp = reinterpret_cast<P*>(gbase);
+            acc = reinterpret_cast<A*>(gbase + sizeof(P) * (size_t)max_nv);
+            cnt = reinterpret_cast<int*>(gbase + (sizeof(P) + 3 * sizeof(A)) * (size_t)max_nv);
+        }
+
+        if (tid == 0) { s_incol = 0; s_bad = 0; s_any_drag = 0; }
+        bool bad = false;
+        if (tid < 3) {
+            long long k = 4ll * env + tid;
+            t3<R> b = prom<R>(ldf3(D.lap_base, k)), t = prom<R>(ldf3(D.lap_tip, k));
+            R r = R(D.lap_radius[k]);
+            tool.base[tid] = b; tool.tip[tid] = t; tool.radius[tid] = r;
+            t3<R> cn = normalize(t - b);
+            t3<R> off = cn * r;
+            t3<R> pa = b + off, pb = t - off;
+            R mag = rmax(rmax(rmax(fabs(pa.x), fabs(pa.y)), rmax(fabs(pa.z), fabs(pb.x))), rmax(fabs(pb.y), fabs(pb.z)));
+            R m = r + R(1e-4) * (R(1) + mag);
+            tool.blo[tid] = T3<R>(rmin(pa.x, pb.x) - m, rmin(pa.y, pb.y) - m, rmin(pa.z, pb.z) - m);
+            tool.bhi[tid] = T3<R>(rmax(pa.x, pb.x) + m, rmax(pa.y, pb.y) + m, rmax(pa.z, pb.z) + m);
+            if (tid == 2) tool.drag_tip = t;
+        }
+        for (int i = tid; i < nv; i += BLOCK) {
+            acc[3 * i] = A(0); acc[3 * i + 1] = A(0); acc[3 * i + 2] = A(0);
+            cnt[i] = 0;
+        }
+        // grasp mask of this env, one bit per vertex
+        if (fl & FFSRL_DRAG) {
+            const int lane = tid & 31;
+            for (int b0 = tid & ~31; b0 < nv; b0 += BLOCK) {
+                int i = b0 + lane;
+                bool on = i < nv && __ldg(D.drag + E.v0 + i) != 0.0f;
+                unsigned word = __ballot_sync(0xffffffffu, on);
+                if (lane == 0) {
+                    dbits[b0 >> 5] = word;
+                    if (word) s_any_drag = 1;
+                }
+            }
+        }
+        // inverse masses ride in .w for the whole step
+        for (int i = tid; i < nv; i += BLOCK) {
+            t3<R> x = ldgen3(D.vertex, E.v0 + i);
+            xp[i] = S::make(x, R(__ldg(D.inv_mass + E.v0 + i)));
+        }
+        __syncthreads();
+
+        for (int step = 0; step < nsteps; ++step) {
+            for (int sub = 0; sub < D.substeps; ++sub) {
+                // gravity (integrator.py:40-63)
+                for (int i = tid; i < nv; i += BLOCK) {
+                    t3<R> x = ldgen3(D.vertex, E.v0 + i), v = ldgen3(D.velocity, E.v0 + i);
+                    R inv = xp[i].w;
+                    R damp = R(1) - R(D.damping);
+                    v = v + T3<R>(R(D.gx), R(D.gy), R(D.gz)) * inv * dt * damp;
+                    if (inv < R(BEPS)) v = T3<R>(0, 0, 0);
+                    xp[i] = S::make(x + v * dt, inv);
+                }
+                if (fl & FFSRL_VOLUME_XPBD)
+                    for (int t = tid; t < nt; t += BLOCK) D.tet_lambda[E.t0 + t] = 0.0f;
+                if (fl & FFSRL_DISTANCE_XPBD)
+                    for (int e = tid; e < ne; e += BLOCK) D.edge_lambda[E.e0 + e] = 0.0f;
+                __syncthreads();
+
+                for (int it = 0; it < D.iterations; ++it) {
+                    // ---- tet constraints: volume, XPBD volume, Neo-Hookean ----
+                    if (fl & (FFSRL_VOLUME | FFSRL_VOLUME_XPBD | FFSRL_NEOHOOKEAN)) {
+                        for (int t = tid; t < nt; t += BLOCK) {
+                            const long long gt = (long long)E.t0 + t;
+                            const uint2 ix = __ldg(D.tet_idx + gt);
+                            const int ia = ix.x & 0xffff, ib = ix.x >> 16, ic = ix.y & 0xffff, id = ix.y >> 16;
+                            const P PA = xp[ia], PB = xp[ib], PC = xp[ic], PD = xp[id];
+                            const t3<R> pa = S::pos(PA), pb = S::pos(PB), pc = S::pos(PC), pd = S::pos(PD);
+                            const R mA = PA.w, mB = PB.w, mC = PC.w, mD = PD.w;
+                            const t3<R> p1 = pb - pa, p2 = pc - pa, p3 = pd - pa;
+                            t3<R> dA = T3<R>(0, 0, 0), dB = dA, dC = dA, dD = dA;
+                            int k = 0;
+                            const float2 va = __ldg(D.tet_va + gt);
+                            if (fl & (FFSRL_VOLUME | FFSRL_VOLUME_XPBD)) {
+                                // volumeConstraints (integrator.py:444-504) / XPBD (:507-576)
+                                const R active = R(va.y);
+                                if (active == R(1)) {
+                                    t3<R> q2 = cross(p3, p1), q1 = cross(p2, p3), q3 = cross(p1, p2);
+                                    t3<R> q0 = -q1 - q2 - q3;
+                                    R w = mA * dot(q0, q0) + mB * dot(q1, q1) + mC * dot(q2, q2) + mD * dot(q3, q3);
+                                    if (!(fabs(w) < R(BEPS))) {
+                                        R s6 = dot(cross(p1, p2), p3);
+                                        if (fl & FFSRL_VOLUME) {
+                                            R C = R(va.x) - fabs(s6) / R(6);
+                                            R dl = -R(D.ks_volume) * active * C / w;
+                                            dA = q0 * dl * mA; dB = q1 * dl * mB; dC = q2 * dl * mC; dD = q3 * dl * mD;
+                                            ++k;
+                                        }
+                                        if (fl & FFSRL_VOLUME_XPBD) {
+                                            R alpha = R(D.a_vol);
+                                            R lam = R(D.tet_lambda[gt]);
+                                            R C = s6 / R(6) - R(__ldg(D.tet_vs + gt));
+                                            R dl = -(C + alpha * lam) / (w + alpha);
+                                            D.tet_lambda[gt] = float(lam + dl);
+                                            dA = dA + q0 * dl * mA; dB = dB + q1 * dl * mB;
+                                            dC = dC + q2 * dl * mC; dD = dD + q3 * dl * mD;
+                                            ++k;
+                                        }
+                                    }
+                                }
+                            }
+                            if (fl & FFSRL_NEOHOOKEAN) {
+                                // neoHookeanConstraints (integrator.py:578-698)
+                                const float4 a4 = __ldg(D.dmA + gt), b4 = __ldg(D.dmB + gt);
+                                const R d00 = R(a4.x), d01 = R(a4.y), d02 = R(a4.z), d10 = R(a4.w);
+                                const R d11 = R(b4.x), d12 = R(b4.y), d20 = R(b4.z), d21 = R(b4.w);
+                                const R d22 = R(__ldg(D.dmC + gt));
+                                const R rv = R(va.x);
+                                t3<R> f0 = p1 * d00 + p2 * d10 + p3 * d20;
+                                t3<R> f1 = p1 * d01 + p2 * d11 + p3 * d21;
+                                t3<R> f2 = p1 * d02 + p2 * d12 + p3 * d22;
+                                t3<R> c0 = cross(f1, f2), c1 = cross(f2, f0), c2 = cross(f0, f1);
+                                t3<R> g1 = c0 * d00 + c1 * d01 + c2 * d02;
+                                t3<R> g2 = c0 * d10 + c1 * d11 + c2 * d12;
+                                t3<R> g3 = c0 * d20 + c1 * d21 + c2 * d22;
+                                t3<R> g0 = -g1 - g2 - g3;
+                                R detF = dot(f0, c0);
+                                R invVol = R(1) / R(D.vol_c), invDev = R(1) / R(D.dev_c);
+                                R C = detF - R(1) - invDev / invVol;
+                                R w = R(0), l;
+                                l = length(g0); w += l * l * mA;
+                                l = length(g1); w += l * l * mB;
+                                l = length(g2); w += l * l * mC;
+                                l = length(g3); w += l * l * mD;
+                                if (!(w < R(BEPS))) {
+                                    R alpha = R(D.vol_c) / dt / dt / rv;
+                                    R dl = -C / (w + alpha);
+                                    t3<R> hA = g0 * dl * mA, hB = g1 * dl * mB, hC = g2 * dl * mC, hD = g3 * dl * mD;
+                                    R l0 = length(f0), l1 = length(f1), l2 = length(f2);
+                                    R rs = sqrt(l0 * l0 + l1 * l1 + l2 * l2);
+                                    R rsi = R(1) / rs;
+                                    g1 = (f0 * d00 + f1 * d01 + f2 * d02) * rsi;
+                                    g2 = (f0 * d10 + f1 * d11 + f2 * d12) * rsi;
+                                    g3 = (f0 * d20 + f1 * d21 + f2 * d22) * rsi;
+                                    g0 = -g1 - g2 - g3;
+                                    w = R(0);
+                                    l = length(g0); w += l * l * mA;
+                                    l = length(g1); w += l * l * mB;
+                                    l = length(g2); w += l * l * mC;
+                                    l = length(g3); w += l * l * mD;
+                                    if (!(w < R(BEPS))) {
+                                        alpha = R(D.dev_c) / dt / dt / rv;
+                                        dl = -rs / (w + alpha);
+                                        hA = hA + g0 * dl * mA; hB = hB + g1 * dl * mB;
+                                        hC = hC + g2 * dl * mC; hD = hD + g3 * dl * mD;
+                                        dA = dA + hA; dB = dB + hB; dC = dC + hC; dD = dD + hD;
+                                        ++k;
+                                    }
+                                }
+                            }
+                            if (k) {
+                                add3<R>(acc, ia, dA, bad); add3<R>(acc, ib, dB, bad);
+                                add3<R>(acc, ic, dC, bad); add3<R>(acc, id, dD, bad);
+                                atomicAdd(cnt + ia, k); atomicAdd(cnt + ib, k); atomicAdd(cnt + ic, k); atomicAdd(cnt + id, k);
+                            }
+                        }
+                    }
+                    // ---- edge constraints: distance (integrator.py:65-109), XPBD (:191-240) ----
+                    if (fl & (FFSRL_DISTANCE | FFSRL_DISTANCE_XPBD)) {
+                        for (int e = tid; e < ne; e += BLOCK) {
+                            const long long ge = (long long)E.e0 + e;
+                            const unsigned ix = __ldg(D.edge_idx + ge);
+                            const int ia = ix & 0xffff, ib = ix >> 16;
+                            const float2 la = __ldg(D.edge_la + ge);
+                            const R active = R(la.y), L0 = R(la.x);
+                            if (active == R(0) || L0 < R(BEPS)) continue;
+                            const P PA = xp[ia], PB = xp[ib];
+                            t3<R> dir = S::pos(PB) - S::pos(PA);
+                            R len = length(dir);
+                            if (len < R(BEPS)) continue;
+                            R mA = PA.w, mB = PB.w;
+                            R w = mA + mB;
+                            if (w < R(BEPS)) continue;
+                            R C = len - L0;
+                            t3<R> dA = T3<R>(0, 0, 0), dB = dA;
+                            int k = 0;
+                            if (fl & FFSRL_DISTANCE) {
+                                t3<R> d = -C * (dir / len) * R(D.ks_distance) * active / w;
+                                dA = -(d * mA); dB = d * mB;
+                                ++k;
+                            }
+                            if (fl & FFSRL_DISTANCE_XPBD) {
+                                R alpha = R(D.a_dist);
+                                R lam = R(D.edge_lambda[ge]);
+                                R dl = -(C + alpha * lam) / (w + alpha);
+                                D.edge_lambda[ge] = float(lam + dl);
+                                t3<R> d = dl * normalize(dir);
+                                dA = dA - d * mA; dB = dB + d * mB;
+                                ++k;
+                            }
+                            add3<R>(acc, ia, dA, bad); add3<R>(acc, ib, dB, bad);
+                            atomicAdd(cnt + ia, k); atomicAdd(cnt + ib, k);
+                        }
+                    }
+                    __syncthreads();
+                    // ---- applyConstraints + dragConstraintsDO ----
+                    for (int i = tid; i < nv; i += BLOCK) {
+                        int c = cnt[i];
+                        P q = xp[i];
+                        t3<R> x = S::pos(q);
+                        if (c > 0) {
+                            R N = R(c);
+                            x = x + T3<R>(S::get(acc[3 * i]) / N, S::get(acc[3 * i + 1]) / N, S::get(acc[3 * i + 2]) / N);
+                            acc[3 * i] = A(0); acc[3 * i + 1] = A(0); acc[3 * i + 2] = A(0);
+                            cnt[i] = 0;
+                        }
+                        if ((fl & FFSRL_DRAG) && s_any_drag && ((dbits[i >> 5] >> (i & 31)) & 1u)) {
+                            R dr = R(__ldg(D.drag + E.v0 + i));
+                            t3<R> dir = x - tool.drag_tip;
+                            R len = length(dir);
+                            if (!(len < R(BEPS))) x = x - len * normalize(dir) * dr * R(D.ks_drag) / R(2);
+                        }
+                        xp[i] = S::make(x, q.w);
+                    }
+                    __syncthreads();
+                    // ---- collideLaparoscopeDO (integrator.py:981-1050), positions as of phase start ----
+                    if ((fl & FFSRL_COLLIDE) && nf > 0) {
+                        if (tid == 0) s_any_contact = 0;
+                        __syncthreads();
+                        const R ks = R(D.ks_contact);
+                        for (int f = tid; f < nf; f += BLOCK) {
+                            const uint2 tr = __ldg(D.tri_idx + (long long)E.f0 + f);
+                            if ((tr.y >> 16) == 1u) continue;
+                            const int a = tr.x & 0xffff, b = tr.x >> 16, c = tr.y & 0xffff;
+                            const P PA = xp[a], PB = xp[b], PC = xp[c];
+                            const t3<R> pA = S::pos(PA), pB = S::pos(PB), pC = S::pos(PC);
+                            const t3<R> lo = T3<R>(rmin(pA.x, rmin(pB.x, pC.x)), rmin(pA.y, rmin(pB.y, pC.y)), rmin(pA.z, rmin(pB.z, pC.z)));
+                            const t3<R> hi = T3<R>(rmax(pA.x, rmax(pB.x, pC.x)), rmax(pA.y, rmax(pB.y, pC.y)), rmax(pA.z, rmax(pB.z, pC.z)));
+                            unsigned near = 0;
+                            for (int i = 0; i < 3; ++i) {
+                                bool apart = lo.x > tool.bhi[i].x || lo.y > tool.bhi[i].y || lo.z > tool.bhi[i].z ||
+                                             hi.x < tool.blo[i].x || hi.y < tool.blo[i].y || hi.z < tool.blo[i].z;
+                                if (!apart) near |= 1u << i;
+                            }
+                            if (!near) continue;
+                            t3<R> centre = (pA + pB + pC) * R(0.3333f);
+                            t3<R> n = normalize(cross(pB - pA, pC - pA));
+                            t3<R> tA = T3<R>(0, 0, 0), tB = tA, tC = tA;
+                            R tl = R(0);
+                            for (int i = 0; i < 3; ++i) {
+                                if (!((near >> i) & 1u)) continue;
+                                t3<R> rA = T3<R>(0, 0, 0), rB = rA, rC = rA;
+                                capsule_response(tool.tip[i], tool.base[i], tool.radius[i], n, centre, pA, pB, pC, ks, rA, rB, rC);
+                                tA = tA + rA; tB = tB + rB; tC = tC + rC;
+                                tl = tl + length(rA) + length(rB) + length(rC);
+                            }
+                            if (tl > R(0)) atomicAdd(&s_incol, 1);
+                            if (!(tl > R(0)) && !isnan(tl)) continue;  // every response is zero
+                            s_any_contact = 1;
+                            if (PA.w > R(0)) add3<R>(acc, a, tA, bad);
+                            if (PB.w > R(0)) add3<R>(acc, b, tB, bad);
+                            if (PC.w > R(0)) add3<R>(acc, c, tC, bad);
+                        }
+                        __syncthreads();
+                        if (s_any_contact) {
+                            for (int i = tid; i < nv; i += BLOCK) {
+                                P q = xp[i];
+                                t3<R> d = T3<R>(S::get(acc[3 * i]), S::get(acc[3 * i + 1]), S::get(acc[3 * i + 2]));
+                                xp[i] = S::make(S::pos(q) - d, q.w);
+                                acc[3 * i] = A(0); acc[3 * i + 1] = A(0); acc[3 * i + 2] = A(0);
+                            }
+                            __syncthreads();
+                        }
+                    }
+                }
+                // ---- bounds (integrator.py:12-21) + PBDStep (:23-38) ----
+                for (int i = tid; i < nv; i += BLOCK) {
+                    P q = xp[i];
+                    t3<R> p = S::pos(q);
+                    if (p.y < R(D.ground)) p.y = R(D.ground);
+                    t3<R> x = ldgen3(D.vertex, E.v0 + i);
+                    t3<R> v = (p - x) * (R(1) / dt);
+                    stg3(D.vertex, E.v0 + i, p);
+                    stg3(D.velocity, E.v0 + i, v);
+                    xp[i] = S::make(p, q.w);
+                    bad |= !(isfinite(p.x) && isfinite(p.y) && isfinite(p.z));
+                }
+                __syncthreads();
+            }
+        }
+        for (int i = tid; i < nv; i += BLOCK) stg3(D.predicted, E.v0 + i, S::pos(xp[i]));
+        if (bad) s_bad = 1;
+        __syncthreads();
+        if (tid == 0) {
+            if (s_incol) atomicAdd(D.in_collision + env, s_incol);
+            D.env_status[env] = s_bad ? FFSRL_ERR_NONFINITE : FFSRL_OK;
+        }
+        __syncthreads();
+    }
+}
+
+template <class R> size_t smem_bytes(int mode, int max_nv) {
+    size_t P = sizeof(typename Store<R>::P), A = sizeof(typename Store<R>::A);
+    size_t bits = 4 * (size_t)((max_nv + 31) / 32 + 1);
+    if (mode == 0) return (P + 3 * A + 4) * (size_t)max_nv + bits;
+    if (mode == 1) return P * (size_t)max_nv + bits;
+    return bits;
+}
+template <class R> size_t scratch_bytes(int mode, int max_nv) {
+    size_t P = sizeof(typename Store<R>::P), A = sizeof(typename Store<R>::A);
+    if (mode == 0) return 0;
+    if (mode == 1) return (3 * A + 4) * (size_t)max_nv;
+    return (P + 3 * A + 4) * (size_t)max_nv;
+}
+
+typedef void (*kern_f)(const Dev<float>, const int*, int, int*, int, unsigned char*, long long, int);
+typedef void (*kern_d)(const Dev<double>, const int*, int, int*, int, unsigned char*, long long, int);
+
+kern_f pick_f(int block, int mode) {
+#define PK(B, M) if (block == B && mode == M) return k_batched<float, B, M>;
+    PK(128, 0) PK(256, 0) PK(512, 0) PK(1024, 0)
+    PK(256, 1) PK(512, 1) PK(1024, 1)
+    PK(256, 2) PK(512, 2)
+#undef PK
+    return nullptr;
+}
+kern_d pick_d(int block, int mode) {
+    if (block == 256 && mode == 0) return k_batched<double, 256, 0>;
+    if (block == 256 && mode == 2) return k_batched<double, 256, 2>;
+    return nullptr;
+}
+
+}  // namespace
+}  // namespace ffsrl
+
+using namespace ffsrl;
+
+struct ffsrl_batch {
+    int num_envs = 0;
+    int precision = 32;
+    int sm_count = 0, max_smem = 0;
+    ffsrl_params params{};
+    ffsrl_model dm{};  // device pointers of the model
+    // device tables
+    EnvRec* d_env = nullptr;
+    uint2* d_tet_idx = nullptr; float2* d_tet_va = nullptr;
+    float4* d_dmA = nullptr; float4* d_dmB = nullptr; float* d_dmC = nullptr; float* d_tet_vs = nullptr;
+    unsigned* d_edge_idx = nullptr; float2* d_edge_la = nullptr; uint2* d_tri_idx = nullptr;
+    int* d_work = nullptr; int* d_counters = nullptr; int* d_status = nullptr;
+    unsigned char* d_scratch = nullptr;
+    double* d_state64 = nullptr;  // x, v, xp in double for precision 64
+    int64_t device_bytes = 0;
+    // classes
+    struct Class {
+        int mode, block, max_nv, grid;
+        size_t smem, scratch_stride, scratch_offset;
+        int work_offset, work_count;
+        cudaStream_t stream;
+        cudaEvent_t done;
+    };
+    std::vector<Class> classes;
+    std::vector<int> env_class;
+    std::vector<int> work_host;  // per class, largest first
+    std::vector<int64_t> env_cost;
+    cudaEvent_t fork = nullptr;
+    int* h_work_pinned = nullptr;
+    int* d_work_sub = nullptr;
+};
+
+namespace {
+
+template <class T> int32_t dalloc(ffsrl_batch* b, T** p, size_t n) {
+    if (n == 0) { *p = nullptr; return FFSRL_OK; }
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+    if (e != cudaSuccess) return cuda_fail(e, "ffsrl_batch: cudaMalloc");
+    b->device_bytes += (int64_t)(n * sizeof(T));
+    return FFSRL_OK;
+}
+template <class T> int32_t upload(T* d, const std::vector<T>& h) {
+    if (h.empty()) return FFSRL_OK;
+    cudaError_t e = cudaMemcpy(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "ffsrl_batch: upload");
+    return FFSRL_OK;
+}
+
+void free_batch(ffsrl_batch* b) {
+    if (!b) return;
+    cudaFree(b->d_env); cudaFree(b->d_tet_idx); cudaFree(b->d_tet_va); cudaFree(b->d_dmA); cudaFree(b->d_dmB);
+    cudaFree(b->d_dmC); cudaFree(b->d_tet_vs); cudaFree(b->d_edge_idx); cudaFree(b->d_edge_la); cudaFree(b->d_tri_idx);
+    cudaFree(b->d_work); cudaFree(b->d_counters); cudaFree(b->d_status); cudaFree(b->d_scratch);
+    cudaFree(b->d_state64); cudaFree(b->d_work_sub);
+    if (b->h_work_pinned) cudaFreeHost(b->h_work_pinned);
+    for (auto& c : b->classes) {
+        if (c.stream) cudaStreamDestroy(c.stream);
+        if (c.done) cudaEventDestroy(c.done);
+    }
+    if (b->fork) cudaEventDestroy(b->fork);
+    delete b;
+}
+
+int default_block(int max_nv, int mode) {
+    if (mode == 2) return 256;
+    if (max_nv <= 256) return 128;
+    if (max_nv <= 1024) return 256;
+    if (max_nv <= 2560) return 512;
+    return 1024;
+}
+
+template <class R> int32_t launch_class(ffsrl_batch* b, const ffsrl_batch::Class& c, const int* work, int nwork,
+                                        int slot, int nsteps, cudaStream_t s);
+
+Dev<float> make_dev_f(ffsrl_batch* b) {
+    Dev<float> D;
+    const ffsrl_params& p = b->params;
+    D.env = b->d_env; D.tet_idx = b->d_tet_idx; D.tet_va = b->d_tet_va; D.dmA = b->d_dmA; D.dmB = b->d_dmB;
+    D.dmC = b->d_dmC; D.tet_vs = b->d_tet_vs; D.edge_idx = b->d_edge_idx; D.edge_la = b->d_edge_la;
+    D.tri_idx = b->d_tri_idx;
+    D.vertex = b->dm.vertex; D.velocity = b->dm.velocity; D.predicted = b->dm.predicted_vertex;
+    D.inv_mass = b->dm.inverse_mass; D.drag = b->dm.active_drag_constraint;
+    D.lap_base = b->dm.laparoscope_base; D.lap_tip = b->dm.laparoscope_tip; D.lap_radius = b->dm.laparoscope_radius;
+    D.in_collision = b->dm.laparoscope_in_collision;
+    D.tet_lambda = b->dm.tetrahedron_lambda; D.edge_lambda = b->dm.edge_lambda;
+    D.env_status = b->d_status;
+    D.flags = p.flags; D.substeps = p.substeps; D.iterations = p.iterations;
+    D.dt = p.dt; D.gx = p.gravity[0]; D.gy = p.gravity[1]; D.gz = p.gravity[2];
+    D.damping = p.velocity_dampening; D.ground = p.ground_level;
+    D.ks_distance = p.ks_distance; D.ks_volume = p.ks_volume; D.ks_contact = p.ks_contact; D.ks_drag = p.ks_drag;
+    D.vol_c = p.volume_compliance; D.dev_c = p.deviatoric_compliance;
+    D.a_dist = (float)((double)p.distance_compliance / ((double)p.dt * (double)p.dt));
+    D.a_vol = (float)((double)p.volume_compliance_xpbd / ((double)p.dt * (double)p.dt));
+    return D;
+}
+
+template <> int32_t launch_class<float>(ffsrl_batch* b, const ffsrl_batch::Class& c, const int* work, int nwork,
+                                        int slot, int nsteps, cudaStream_t s) {
+    kern_f k = pick_f(c.block, c.mode);
+    if (!k) return fail(FFSRL_ERR_UNSUPPORTED, "ffsrl_batch: no kernel for block/mode");
+    Dev<float> D = make_dev_f(b);
+    int grid = std::min(c.grid, nwork);
+    if (grid <= 0) return FFSRL_OK;
+    k<<<grid, c.block, c.smem, s>>>(D, work, nwork, b->d_counters + slot, nsteps, b->d_scratch + c.scratch_offset,
+                                    (long long)c.scratch_stride, c.max_nv);
+    FFSRL_LAUNCH_CHECK("ffsrl_batch: step kernel");
+    return FFSRL_OK;
+}
+
+template <> int32_t launch_class<double>(ffsrl_batch* b, const ffsrl_batch::Class& c, const int* work, int nwork,
+                                         int slot, int nsteps, cudaStream_t s) {
+    kern_d k = pick_d(c.block, c.mode);
+    if (!k) return fail(FFSRL_ERR_UNSUPPORTED, "ffsrl_batch: no float64 kernel for block/mode");
+    Dev<float> F = make_dev_f(b);
+    Dev<double> D;
+    // same tables and parameters; state in the plan's double arrays
+    D.env = F.env; D.tet_idx = F.tet_idx; D.tet_va = F.tet_va; D.dmA = F.dmA; D.dmB = F.dmB; D.dmC = F.dmC;
+    D.tet_vs = F.tet_vs; D.edge_idx = F.edge_idx; D.edge_la = F.edge_la; D.tri_idx = F.tri_idx;
+    int64_t V = b->dm.num_vertices;
+    D.vertex = b->d_state64; D.velocity = b->d_state64 + 3 * V; D.predicted = b->d_state64 + 6 * V;
+    D.inv_mass = F.inv_mass; D.drag = F.drag; D.lap_base = F.lap_base; D.lap_tip = F.lap_tip;
+    D.lap_radius = F.lap_radius; D.in_collision = F.in_collision; D.tet_lambda = F.tet_lambda;
+    D.edge_lambda = F.edge_lambda; D.env_status = F.env_status; D.flags = F.flags; D.substeps = F.substeps;
+    D.iterations = F.iterations; D.dt = F.dt; D.gx = F.gx; D.gy = F.gy; D.gz = F.gz; D.damping = F.damping;
+    D.ground = F.ground; D.ks_distance = F.ks_distance; D.ks_volume = F.ks_volume; D.ks_contact = F.ks_contact;
+    D.ks_drag = F.ks_drag; D.vol_c = F.vol_c; D.dev_c = F.dev_c; D.a_dist = F.a_dist; D.a_vol = F.a_vol;
+    int grid = std::min(c.grid, nwork);
+    if (grid <= 0) return FFSRL_OK;
+    k<<<grid, c.block, c.smem, s>>>(D, work, nwork, b->d_counters + slot, nsteps, b->d_scratch + c.scratch_offset,
+                                    (long long)c.scratch_stride, c.max_nv);
+    FFSRL_LAUNCH_CHECK("ffsrl_batch: float64 step kernel");
+    return FFSRL_OK;
+}
+
+int32_t run(ffsrl_batch* b, const std::vector<int>& counts, const int* d_work_base,
+            const std::vector<int>& offsets, int nsteps, cudaStream_t s) {
+    FFSRL_CUDA_TRY(cudaMemsetAsync(b->d_counters, 0, sizeof(int) * b->classes.size(), s));
+    FFSRL_CUDA_TRY(cudaEventRecord(b->fork, s));
+    for (size_t ci = 0; ci < b->classes.size(); ++ci) {
+        auto& c = b->classes[ci];
+        FFSRL_CUDA_TRY(cudaStreamWaitEvent(c.stream, b->fork, 0));
+        if (counts[ci] > 0) {
+            int32_t st = b->precision == 64
+                             ? launch_class<double>(b, c, d_work_base + offsets[ci], counts[ci], (int)ci, nsteps, c.stream)
+                             : launch_class<float>(b, c, d_work_base + offsets[ci], counts[ci], (int)ci, nsteps, c.stream);
+            if (st) return st;
+        }
+        FFSRL_CUDA_TRY(cudaEventRecord(c.done, c.stream));
+        FFSRL_CUDA_TRY(cudaStreamWaitEvent(s, c.done, 0));
+    }
+    return FFSRL_OK;
+}
+
+}  // namespace
+
+extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* dmod, const ffsrl_params* p,
+                                      const ffsrl_batch_options* opts, ffsrl_batch** out) {
+    if (!hm || !dmod || !p || !out) return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_create: null argument");
+    *out = nullptr;
+    const int N = hm->num_envs;
+    if (N <= 0 || !hm->env_vertex_start || !hm->env_tet_start || !hm->env_edge_start || !hm->env_tri_start)
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_create: host env ranges required");
+    if ((p->flags & FFSRL_CONNECTORS) && hm->num_connectors > 0)
+        return fail(FFSRL_ERR_UNSUPPORTED, "ffsrl_batch_create: connectors couple environments; use ffsrl_step_model");
+    int precision = 32;
+    int block_override = 0;
+    if (opts) {
+        block_override = opts->block_threads;
+        if (opts->reserved[0] == 64) precision = 64;
+    }
+    ffsrl_batch* b = new ffsrl_batch();
+    b->num_envs = N;
+    b->params = *p;
+    b->dm = *dmod;
+    b->precision = precision;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&b->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (b->sm_count <= 0 || b->max_smem <= 0) { free_batch(b); return fail(FFSRL_ERR_CUDA, "ffsrl_batch_create: no device"); }
+    // the kernels' static shared memory (block-wide scalars and the instrument) comes off
+    // the per-block opt-in limit; budget dynamic shared memory below that
+    size_t static_smem = 0;
+    {
+        const void* probes[] = {(const void*)pick_f(1024, 0), (const void*)pick_f(512, 1), (const void*)pick_d(256, 0)};
+        for (const void* k : probes) {
+            cudaFuncAttributes fa;
+            if (cudaFuncGetAttributes(&fa, k) == cudaSuccess) static_smem = std::max(static_smem, fa.sharedSizeBytes);
+        }
+    }
+    const size_t dyn_budget = (size_t)b->max_smem > static_smem + 64 ? (size_t)b->max_smem - static_smem - 64 : 0;
+
+    const int64_t V = hm->num_vertices, T = hm->num_tetrahedrons, E = hm->num_edges, F = hm->num_triangles;
+    std::vector<EnvRec> env(N);
+    std::vector<uint2> tet_idx(T);
+    std::vector<float2> tet_va(T);
+    std::vector<float4> dmA, dmB;
+    std::vector<float> dmC, tet_vs;
+    const bool nh = (p->flags & FFSRL_NEOHOOKEAN) != 0;
+    const bool xv = (p->flags & FFSRL_VOLUME_XPBD) != 0;
+    if (nh && !hm->tetrahedron_dm_inv) { free_batch(b); return fail(FFSRL_ERR_INVALID_ARGUMENT, "Neo-Hookean needs tetrahedron_dm_inv"); }
+    if (xv && (!hm->xpbd_rest_volume || !dmod->tetrahedron_lambda)) { free_batch(b); return fail(FFSRL_ERR_INVALID_ARGUMENT, "XPBD volume needs xpbd_rest_volume and lambdas"); }
+    if ((p->flags & FFSRL_DISTANCE_XPBD) && !dmod->edge_lambda) { free_batch(b); return fail(FFSRL_ERR_INVALID_ARGUMENT, "XPBD distance needs edge_lambda"); }
+    if (nh) { dmA.resize(T); dmB.resize(T); dmC.resize(T); }
+    if (xv) tet_vs.resize(T);
+    std::vector<unsigned> edge_idx(E);
+    std::vector<float2> edge_la(E);
+    std::vector<uint2> tri_idx(F);
+    for (int e = 0; e < N; ++e) {
+        EnvRec r;
+        r.v0 = hm->env_vertex_start[e]; r.nv = hm->env_vertex_start[e + 1] - r.v0;
+        r.t0 = hm->env_tet_start[e]; r.nt = hm->env_tet_start[e + 1] - r.t0;
+        r.e0 = hm->env_edge_start[e]; r.ne = hm->env_edge_start[e + 1] - r.e0;
+        r.f0 = hm->env_tri_start[e]; r.nf = hm->env_tri_start[e + 1] - r.f0;
+        if (r.nv < 0 || r.nt < 0 || r.ne < 0 || r.nf < 0 || r.nv > 65535) {
+            free_batch(b);
+            return fail(FFSRL_ERR_UNSUPPORTED, "ffsrl_batch_create: env " + std::to_string(e) +
+                                                   " has a negative range or more than 65535 vertices");
+        }
+        env[e] = r;
+        auto local = [&](int g, int& outv) -> bool {
+            int l = g - r.v0;
+            if (l < 0 || l >= r.nv) return false;
+            outv = l;
+            return true;
+        };
+        for (int t = r.t0; t < r.t0 + r.nt; ++t) {
+            int l[4];
+            for (int k = 0; k < 4; ++k)
+                if (!local(hm->tetrahedron[4ll * t + k], l[k])) {
+                    free_batch(b);
+                    return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_create: tet " + std::to_string(t) + " leaves its env");
+                }
+            tet_idx[t] = make_uint2((unsigned)l[0] | ((unsigned)l[1] << 16), (unsigned)l[2] | ((unsigned)l[3] << 16));
+            tet_va[t] = make_float2(hm->tetrahedron_rest_volume ? hm->tetrahedron_rest_volume[t] : 0.0f,
+                                    hm->active_tetrahedron ? hm->active_tetrahedron[t] : 1.0f);
+            if (nh) {
+                const float* d = hm->tetrahedron_dm_inv + 9ll * t;
+                dmA[t] = make_float4(d[0], d[1], d[2], d[3]);
+                dmB[t] = make_float4(d[4], d[5], d[6], d[7]);
+                dmC[t] = d[8];
+            }
+            if (xv) tet_vs[t] = hm->xpbd_rest_volume[t];
+        }
+        for (int k = r.e0; k < r.e0 + r.ne; ++k) {
+            int a, c;
+            if (!local(hm->edge[2ll * k], a) || !local(hm->edge[2ll * k + 1], c)) {
+                free_batch(b);
+                return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_create: edge " + std::to_string(k) + " leaves its env");
+            }
+            edge_idx[k] = (unsigned)a | ((unsigned)c << 16);
+            edge_la[k] = make_float2(hm->edge_rest_length[k], hm->active_edge ? hm->active_edge[k] : 1.0f);
+        }
+        for (int f = r.f0; f < r.f0 + r.nf; ++f) {
+            int a, c, d;
+            if (!local(hm->triangle[3ll * f], a) || !local(hm->triangle[3ll * f + 1], c) ||
+                !local(hm->triangle[3ll * f + 2], d)) {
+                free_batch(b);
+                return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_create: triangle " + std::to_string(f) + " leaves its env");
+            }
+            unsigned h = (hm->hole && hm->hole[f] == 1) ? 1u : 0u;
+            tri_idx[f] = make_uint2((unsigned)a | ((unsigned)c << 16), (unsigned)d | (h << 16));
+        }
+    }
+
+    // size classes: mode by fit, then by vertex-count band
+    const int bands[] = {192, 384, 768, 1536, 3072, 65536};
+    b->env_class.assign(N, -1);
+    std::vector<std::vector<int>> members;
+    std::vector<int> keys;  // mode*16 + band
+    auto mode_for = [&](int nv) {
+        if (precision == 64) return smem_bytes<double>(0, nv) <= dyn_budget ? 0 : 2;
+        if (smem_bytes<float>(0, nv) <= dyn_budget) return 0;
+        if (smem_bytes<float>(1, nv) <= dyn_budget) return 1;
+        return 2;
+    };
+    for (int e = 0; e < N; ++e) {
+        int m = mode_for(env[e].nv);
+        int band = 0;
+        while (env[e].nv > bands[band]) ++band;
+        int key = m * 16 + (m == 0 ? band : 0);
+        auto it = std::find(keys.begin(), keys.end(), key);
+        int ci;
+        if (it == keys.end()) { keys.push_back(key); members.emplace_back(); ci = (int)keys.size() - 1; }
+        else ci = (int)(it - keys.begin());
+        members[ci].push_back(e);
+    }
+    // order classes by key for reproducible launch order
+    std::vector<int> order(keys.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::sort(order.begin(), order.end(), [&](int a, int c) { return keys[a] < keys[c]; });
+    size_t scratch_total = 0;
+    b->env_cost.resize(N);
+    for (int e = 0; e < N; ++e) b->env_cost[e] = 4ll * env[e].nt + env[e].ne + env[e].nf + env[e].nv;
+    for (int oi : order) {
+        auto& mem = members[oi];
+        std::sort(mem.begin(), mem.end(), [&](int a, int c) {
+            return b->env_cost[a] != b->env_cost[c] ? b->env_cost[a] > b->env_cost[c] : a < c;
+        });
+        ffsrl_batch::Class c{};
+        c.mode = keys[oi] / 16;
+        c.max_nv = 1;
+        for (int e : mem) c.max_nv = std::max(c.max_nv, env[e].nv);
+        c.block = block_override > 0 ? block_override : default_block(c.max_nv, c.mode);
+        if (precision == 64) c.block = 256;
+        if (c.mode == 1 && c.block < 256) c.block = 256;
+        if (c.mode == 2 && c.block > 512) c.block = 512;
+        c.smem = precision == 64 ? smem_bytes<double>(c.mode, c.max_nv) : smem_bytes<float>(c.mode, c.max_nv);
+        c.scratch_stride = precision == 64 ? scratch_bytes<double>(c.mode, c.max_nv) : scratch_bytes<float>(c.mode, c.max_nv);
+        c.scratch_stride = (c.scratch_stride + 255) & ~(size_t)255;
+        // resident blocks per SM, from the runtime's occupancy calculator
+        const void* kfn = precision == 64 ? (const void*)pick_d(c.block, c.mode) : (const void*)pick_f(c.block, c.mode);
+        if (!kfn) { free_batch(b); return fail(FFSRL_ERR_UNSUPPORTED, "ffsrl_batch_create: no kernel for block/mode"); }
+        if (c.smem > 48 * 1024) {
+            // several classes may share one instantiation: allow the device maximum
+            cudaError_t ea = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_budget);
+            if (ea != cudaSuccess) { free_batch(b); return cuda_fail(ea, "ffsrl_batch_create: shared memory attribute"); }
+        }
+        int per_sm = 0;
+        cudaError_t eo = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, c.block, c.smem);
+        if (eo != cudaSuccess || per_sm <= 0) {
+            free_batch(b);
+            return fail(FFSRL_ERR_UNSUPPORTED, "ffsrl_batch_create: class does not fit on an SM (block " +
+                                                   std::to_string(c.block) + ", shared " + std::to_string(c.smem) + ")");
+        }
+        c.grid = std::max(1, std::min((int)mem.size(), per_sm * b->sm_count));
+        c.scratch_offset = scratch_total;
+        scratch_total += c.scratch_stride * (size_t)c.grid;
+        c.work_offset = (int)b->work_host.size();
+        c.work_count = (int)mem.size();
+        for (int e : mem) { b->env_class[e] = (int)b->classes.size(); b->work_host.push_back(e); }
+        b->classes.push_back(c);
+    }
+
+    int32_t st = FFSRL_OK;
+    if ((st = dalloc(b, &b->d_env, N)) || (st = upload(b->d_env, env)) ||
+        (st = dalloc(b, &b->d_tet_idx, T)) || (st = upload(b->d_tet_idx, tet_idx)) ||
+        (st = dalloc(b, &b->d_tet_va, T)) || (st = upload(b->d_tet_va, tet_va)) ||
+        (st = dalloc(b, &b->d_dmA, dmA.size())) || (st = upload(b->d_dmA, dmA)) ||
+        (st = dalloc(b, &b->d_dmB, dmB.size())) || (st = upload(b->d_dmB, dmB)) ||
+        (st = dalloc(b, &b->d_dmC, dmC.size())) || (st = upload(b->d_dmC, dmC)) ||
+        (st = dalloc(b, &b->d_tet_vs, tet_vs.size())) || (st = upload(b->d_tet_vs, tet_vs)) ||
+        (st = dalloc(b, &b->d_edge_idx, E)) || (st = upload(b->d_edge_idx, edge_idx)) ||
+        (st = dalloc(b, &b->d_edge_la, E)) || (st = upload(b->d_edge_la, edge_la)) ||
+        (st = dalloc(b, &b->d_tri_idx, F)) || (st = upload(b->d_tri_idx, tri_idx)) ||
+        (st = dalloc(b, &b->d_work, (size_t)N)) || (st = upload(b->d_work, b->work_host)) ||
+        (st = dalloc(b, &b->d_work_sub, (size_t)N)) ||
+        (st = dalloc(b, &b->d_counters, b->classes.size() + 1)) || (st = dalloc(b, &b->d_status, (size_t)N)) ||
+        (st = dalloc(b, &b->d_scratch, scratch_total))) {
+        free_batch(b);
+        return st;
+    }
+    FFSRL_CUDA_TRY(cudaMemset(b->d_status, 0, sizeof(int) * N));
+    if (precision == 64) {
+        if ((st = dalloc(b, &b->d_state64, 9 * (size_t)V))) { free_batch(b); return st; }
+        // double state initialised from the model's float state
+        std::vector<float> hx(3 * V), hv(3 * V);
+        std::vector<double> h64(9 * V);
+        cudaMemcpy(hx.data(), dmod->vertex, 12 * V, cudaMemcpyDeviceToHost);
+        cudaMemcpy(hv.data(), dmod->velocity, 12 * V, cudaMemcpyDeviceToHost);
+        for (int64_t i = 0; i < 3 * V; ++i) { h64[i] = hx[i]; h64[3 * V + i] = hv[i]; h64[6 * V + i] = hx[i]; }
+        if ((st = upload(b->d_state64, h64))) { free_batch(b); return st; }
+    }
+    FFSRL_CUDA_TRY(cudaHostAlloc((void**)&b->h_work_pinned, sizeof(int) * N, cudaHostAllocDefault));
+    FFSRL_CUDA_TRY(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    for (auto& c : b->classes) {
+        FFSRL_CUDA_TRY(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+        FFSRL_CUDA_TRY(cudaEventCreateWithFlags(&c.done, cudaEventDisableTiming));
+    }
+    *out = b;
+    return FFSRL_OK;
+}
+
+extern "C" int32_t ffsrl_batch_destroy(ffsrl_batch* b) {
+    if (b) cudaDeviceSynchronize();
+    free_batch(b);
+    return FFSRL_OK;
+}
+
+extern "C" int32_t ffsrl_batch_step(ffsrl_batch* b, int32_t n_steps, void* stream) {
+    if (!b || n_steps < 0) return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_step");
+    if (n_steps == 0) return FFSRL_OK;
+    std::vector<int> counts, offsets;
+    for (auto& c : b->classes) { counts.push_back(c.work_count); offsets.push_back(c.work_offset); }
+    return run(b, counts, b->d_work, offsets, n_steps, (cudaStream_t)stream);
+}
+
+extern "C" int32_t ffsrl_batch_step_envs(ffsrl_batch* b, const int32_t* env_ids, int32_t n, int32_t n_steps,
+                                         void* stream) {
+    if (!b || n < 0 || n_steps < 0 || (n > 0 && !env_ids)) return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_step_envs");
+    if (n == 0 || n_steps == 0) return FFSRL_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    // the pinned staging buffer is reused: wait for the previous upload to finish reading it
+    FFSRL_CUDA_TRY(cudaStreamSynchronize(s));
+    std::vector<std::vector<int>> per(b->classes.size());
+    for (int i = 0; i < n; ++i) {
+        int e = env_ids[i];
+        if (e < 0 || e >= b->num_envs) return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_step_envs: env id out of range");
+        per[b->env_class[e]].push_back(e);
+    }
+    std::vector<int> counts, offsets;
+    int o = 0;
+    for (size_t ci = 0; ci < per.size(); ++ci) {
+        auto& v = per[ci];
+        std::sort(v.begin(), v.end(), [&](int a, int c) {
+            return b->env_cost[a] != b->env_cost[c] ? b->env_cost[a] > b->env_cost[c] : a < c;
+        });
+        offsets.push_back(o);
+        counts.push_back((int)v.size());
+        for (int e : v) b->h_work_pinned[o++] = e;
+    }
+    FFSRL_CUDA_TRY(cudaMemcpyAsync(b->d_work_sub, b->h_work_pinned, sizeof(int) * o, cudaMemcpyHostToDevice, s));
+    return run(b, counts, b->d_work_sub, offsets, n_steps, s);
+}
+
+extern "C" int32_t ffsrl_batch_info(const ffsrl_batch* b, int64_t* device_bytes, int32_t* num_classes,
+                                    int32_t* block_threads) {
+    if (!b) return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_info");
+    if (device_bytes) *device_bytes = b->device_bytes;
+    if (num_classes) *num_classes = (int32_t)b->classes.size();
+    if (block_threads)
+        for (size_t i = 0; i < b->classes.size(); ++i) block_threads[i] = b->classes[i].block;
+    return FFSRL_OK;
+}
+
+extern "C" int32_t ffsrl_batch_env_status(const ffsrl_batch* b, int32_t* host_status, int32_t num_envs) {
+    if (!b || !host_status || num_envs != b->num_envs) return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_env_status");
+    FFSRL_CUDA_TRY(cudaMemcpy(host_status, b->d_status, sizeof(int) * num_envs, cudaMemcpyDeviceToHost));
+    return FFSRL_OK;
+}
+
+// Copies the float64 plan's state (x, v, predicted; each [3V]) to host memory.
+extern "C" int32_t ffsrl_batch_state_f64(const ffsrl_batch* b, double* host_xvx) {
+    if (!b || !host_xvx || b->precision != 64) return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_state_f64: not a float64 plan");
+    FFSRL_CUDA_TRY(cudaMemcpy(host_xvx, b->d_state64, sizeof(double) * 9 * (size_t)b->dm.num_vertices, cudaMemcpyDeviceToHost));
+    return FFSRL_OK;
+}

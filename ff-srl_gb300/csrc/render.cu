@@ -1,0 +1,410 @@
+// render.cu -- BVH refit and ray-cast renderer (reference: FF_SRL/FF_SRL/bvh.py:30-104,
+// 419-454 and render.py:81-121, 276-498, 588-724, 975-1022).
+//
+// This unit is compiled with -fmad=false: every product and sum rounds as written, so
+// with IEEE division and square root the images and boxes equal the CPU restatement's
+// bit for bit whenever the summation order is the same (the fused paths).
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "ffsrl_internal.h"
+#include "vecmath.cuh"
+
+namespace ffsrl {
+namespace {
+
+constexpr int kStackCap = 64;  // traversal stack entries per ray (the reference uses 32)
+
+__device__ __forceinline__ int find_env(const int* __restrict__ node_offset, int n_env, int total, int tid) {
+    // env whose AABB range [node_offset[e], next) holds tid; node_offset ascending
+    int lo = 0, hi = n_env - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (node_offset[mid] <= tid) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void refit_node(const ffsrl_bvh& b, const float* __restrict__ pts,
+                                           const int* __restrict__ faces, int e, int n0, int t0, int base, int node) {
+    int left = b.left_node[n0 + node];
+    v3 lo, hi;
+    if (left < 0) {
+        lo = mk(1e6f, 1e6f, 1e6f);
+        hi = mk(-1e6f, -1e6f, -1e6f);
+        int first = b.first_tri_id[n0 + node];
+        int cnt = b.tri_count[n0 + node];
+        long long fofs = b.env_face_offset[e];
+        for (int k = 0; k < cnt; ++k) {
+            long long f = fofs + b.tri_id[t0 + first + k];
+            v3 pA = ld3(pts, faces[3 * f]), pB = ld3(pts, faces[3 * f + 1]), pC = ld3(pts, faces[3 * f + 2]);
+            lo = vmin(pA, vmin(pB, vmin(pC, lo)));
+            hi = vmax(pA, vmax(pB, vmax(pC, hi)));
+        }
+    } else {
+        v3 l0 = ld3(b.aabb_min, base + left), h0 = ld3(b.aabb_max, base + left);
+        v3 l1 = ld3(b.aabb_min, base + left + 1), h1 = ld3(b.aabb_max, base + left + 1);
+        lo = vmin(l0, l1);
+        hi = vmax(h0, h1);
+    }
+    st3(b.aabb_min, base + node, lo);
+    st3(b.aabb_max, base + node, hi);
+}
+
+// refitBVHLevel (bvh.py:30-104): every env node at `level`
+__global__ void k_refit_level(ffsrl_bvh b, const float* __restrict__ pts, const int* __restrict__ faces, int level) {
+    int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= b.total_env_nodes) return;
+    int e = find_env(b.env_node_offset, b.num_envs, b.total_env_nodes, tid);
+    int topo = b.env_topology[e];
+    int n0 = b.topo_node_offset[topo];
+    int node = tid - b.env_node_offset[e];
+    if (node >= b.topo_node_offset[topo + 1] - n0) return;
+    if (b.level[n0 + node] != level) return;
+    refit_node(b, pts, faces, e, n0, b.topo_tri_offset[topo], b.env_node_offset[e], node);
+}
+
+// One block per env: levels deepest first, nodes of a level in parallel.
+__global__ void k_refit_fused(ffsrl_bvh b, const float* __restrict__ pts, const int* __restrict__ faces) {
+    int e = blockIdx.x;
+    int topo = b.env_topology[e];
+    int n0 = b.topo_node_offset[topo], t0 = b.topo_tri_offset[topo];
+    int base = b.env_node_offset[e];
+    int lo = b.topo_level_offset[topo];
+    int groups = b.topo_max_level[topo] + 1;
+    for (int g = 0; g < groups; ++g) {
+        int s0 = b.level_start[lo + g], s1 = b.level_start[lo + g + 1];
+        for (int k = s0 + threadIdx.x; k < s1; k += blockDim.x) refit_node(b, pts, faces, e, n0, t0, base, b.level_node[k]);
+        __syncthreads();
+    }
+}
+
+__global__ void k_zero3(float* p, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) st3(p, i, mk(0.0f, 0.0f, 0.0f));
+}
+
+// vertex_normal_sum_kernel (render.py:81-105)
+__global__ void k_normal_sum(const float* __restrict__ pts, const int* __restrict__ faces, float* nsum, int nf) {
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    int i = faces[3 * f], j = faces[3 * f + 1], k = faces[3 * f + 2];
+    v3 a = ld3(pts, i), b = ld3(pts, j), c = ld3(pts, k);
+    v3 an = cross(b - a, c - a);
+    atomic_add3(nsum, i, an); atomic_add3(nsum, j, an); atomic_add3(nsum, k, an);
+}
+
+// normalize_kernel (render.py:113-121)
+__global__ void k_normalize(const float* __restrict__ nsum, float* __restrict__ nrm, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) st3(nrm, i, normalize(ld3(nsum, i)));
+}
+
+// Area-weighted normals gathered per point in ascending face order (deterministic; the
+// same order as a serial run of vertex_normal_sum_kernel), then normalised.
+__global__ void k_normal_gather(const float* __restrict__ pts, const int* __restrict__ faces,
+                                const int* __restrict__ start, const int* __restrict__ pf, float* __restrict__ nrm,
+                                int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    v3 s = mk(0.0f, 0.0f, 0.0f);
+    for (int k = start[i]; k < start[i + 1]; ++k) {
+        long long f = pf[k];
+        v3 a = ld3(pts, faces[3 * f]), b = ld3(pts, faces[3 * f + 1]), c = ld3(pts, faces[3 * f + 2]);
+        s = s + cross(b - a, c - a);
+    }
+    st3(nrm, i, normalize(s));
+}
+
+__device__ __forceinline__ v3 quat_rotate(float4 q, v3 x) {
+    v3 u = mk(q.x, q.y, q.z);
+    float c = 2.0f * q.w * q.w - 1.0f;
+    float d = 2.0f * (u.x * x.x + u.y * x.y + u.z * x.z);
+    return x * c + u * d + cross(u, x) * (q.w * 2.0f);
+}
+
+// intersectAABB (render.py:588-609)
+__device__ __forceinline__ bool slab(v3 ro, v3 rd, v3 lo, v3 hi, float& tnear) {
+    float t1 = (lo.x - ro.x) / rd.x, t2 = (hi.x - ro.x) / rd.x;
+    float t3 = (lo.y - ro.y) / rd.y, t4 = (hi.y - ro.y) / rd.y;
+    float t5 = (lo.z - ro.z) / rd.z, t6 = (hi.z - ro.z) / rd.z;
+    float tmin = fmax_ref(fmax_ref(fmin_ref(t1, t2), fmin_ref(t3, t4)), fmin_ref(t5, t6));
+    float tmax = fmin_ref(fmin_ref(fmax_ref(t1, t2), fmax_ref(t3, t4)), fmax_ref(t5, t6));
+    tnear = tmin;
+    return (tmax >= 0.0f) && (tmax >= tmin);
+}
+
+// MTTriRayIntersection (render.py:661-697)
+__device__ __forceinline__ float moller_trumbore(v3 a, v3 b, v3 c, v3 ro, v3 rd, v3& p) {
+    v3 ab = b - a, ac = c - a;
+    v3 pvec = cross(rd, ac);
+    float det = dot(ab, pvec);
+    if (fabsf(det) < 0.0001f) return -1.0f;
+    float invDet = 1.0f / det;
+    v3 tvec = ro - a;
+    float u = dot(tvec, pvec) * invDet;
+    if (u < 0.0f || u > 1.0f) return -1.0f;
+    v3 qvec = cross(tvec, ab);
+    float v = dot(rd, qvec) * invDet;
+    if (v < 0.0f || u + v > 1.0f) return -1.0f;
+    float t = dot(ac, qvec) * invDet;
+    p = ro + t * rd;
+    return t;
+}
+
+struct EnvView {
+    const int* left; const int* first; const int* count; const int* tri;
+    const float* amin; const float* amax;
+    long long fofs;
+    int nn;  // nodes in the topology
+};
+
+__device__ __forceinline__ EnvView env_view(const ffsrl_bvh& b, int e) {
+    int topo = b.env_topology[e];
+    EnvView v;
+    int n0 = b.topo_node_offset[topo];
+    v.left = b.left_node + n0; v.first = b.first_tri_id + n0; v.count = b.tri_count + n0;
+    v.tri = b.tri_id + b.topo_tri_offset[topo];
+    long long base = b.env_node_offset[e];
+    v.amin = b.aabb_min + 3 * base; v.amax = b.aabb_max + 3 * base;
+    v.fofs = b.env_face_offset[e];
+    v.nn = b.topo_node_offset[topo + 1] - n0;
+    return v;
+}
+
+// meshQueryRayManyEnvs (render.py:411-498): nearest hit with 0 < t < tMin, stack LIFO
+// with the right child popped first.  Returns the global face id or -1.
+__device__ int query(const EnvView& ev, const float* __restrict__ pts, const int* __restrict__ faces, v3 ro, v3 rd,
+                     float& t_hit, v3& p_hit, int* err) {
+    int stack[kStackCap];
+    int count = 1;
+    stack[0] = 0;
+    float tMin = 1e6f;
+    int hit_tri = -1;
+    int visits = 0;
+    while (count) {
+        int node = stack[--count];
+        if (++visits > ev.nn) {  // a valid tree visits each node at most once
+            atomicExch(err, FFSRL_ERR_STACK_OVERFLOW);
+            return -1;
+        }
+        float tn;
+        bool hit = slab(ro, rd, ld3(ev.amin, node), ld3(ev.amax, node), tn);
+        if (hit && tn < tMin) {
+            int left = ev.left[node];
+            if (left == -1) {
+                int first = ev.first[node];
+                int cnt = ev.count[node];
+                for (int k = 0; k < cnt; ++k) {
+                    long long f = ev.fofs + ev.tri[first + k];
+                    v3 A = ld3(pts, faces[3 * f]), B = ld3(pts, faces[3 * f + 1]), C = ld3(pts, faces[3 * f + 2]);
+                    v3 p;
+                    float t = moller_trumbore(A, B, C, ro, rd, p);
+                    if (t < tMin && t > 0.0f) {
+                        tMin = t;
+                        hit_tri = (int)f; t_hit = t; p_hit = p;
+                    }
+                }
+            } else {
+                if (left < 0 || left + 1 >= ev.nn) {
+                    atomicExch(err, FFSRL_ERR_INVALID_ARGUMENT);
+                    return -1;
+                }
+                if (count + 2 > kStackCap) {
+                    atomicExch(err, FFSRL_ERR_STACK_OVERFLOW);
+                    return -1;
+                }
+                stack[count] = left;
+                stack[count + 1] = left + 1;
+                count += 2;
+            }
+        }
+    }
+    if (tMin >= 1e6f) hit_tri = -1;
+    return hit_tri;
+}
+
+struct Shade { v3 color; float depth; };
+
+// shading of drawSimBVHKernelManyEnvs (render.py:334-409), modes 3 (vertex colour) and 4 (depth)
+__device__ __forceinline__ Shade trace(const ffsrl_render& r, const EnvView& ev, v3 ro, float4 q, int x, int y, int W,
+                                       int H) {
+    float sx = 2.0f * float(x) / float(W) - 1.0f;
+    float sy = 2.0f * float(y) / float(H) - 1.0f;
+    v3 rd = normalize(quat_rotate(q, mk(sx * r.camera_tan * r.camera_aspect, sy * r.camera_tan, -1.0f)));
+    float t = 0.0f;
+    v3 p = mk(0.0f, 0.0f, 0.0f);
+    int tri = query(ev, r.vis_point, r.vis_face, ro, rd, t, p, r.error_flag);
+    Shade s;
+    s.color = mk(0.0f, 0.0f, 0.0f);
+    s.depth = 0.0f;
+    if (tri > -1) {
+        int i = r.vis_face[3ll * tri], j = r.vis_face[3ll * tri + 1], k = r.vis_face[3ll * tri + 2];
+        v3 a = ld3(r.vis_point, i), b = ld3(r.vis_point, j), c = ld3(r.vis_point, k);
+        float area = length(cross(b - a, c - a));
+        float w = length(cross(b - a, p - a)) / area;
+        float v = length(cross(p - a, c - a)) / area;
+        float u = 1.0f - w - v;
+        v3 n = u * ld3(r.vertex_normal, i) + v * ld3(r.vertex_normal, j) + w * ld3(r.vertex_normal, k);
+        v3 vc = (ld3(r.vis_point_color, i) + ld3(r.vis_point_color, j) + ld3(r.vis_point_color, k)) / 3.0f;
+        float lam = 0.0f;
+        for (int l = 0; l < r.num_lights; ++l) {
+            float val = r.light_intensity[l] * dot(n, ld3(r.light_dir, l));
+            if (val < 0.0f) val = 0.0f;
+            lam = lam + val;
+        }
+        v3 col = lam * vc;
+        if (col.x > 1.0f) col.x = 1.0f;
+        if (col.y > 1.0f) col.y = 1.0f;
+        if (col.z > 1.0f) col.z = 1.0f;
+        s.color = col;
+        float d = t / 50.0f;
+        if (d > 1.0f) d = 1.0f;
+        s.depth = d;
+    }
+    return s;
+}
+
+// drawSimBVHKernelManyEnvs (render.py:276-409): one thread per ray, into scratch
+__global__ void k_draw(ffsrl_render r, ffsrl_bvh b) {
+    const int W = 2 * r.resolution, H = 2 * r.resolution;
+    long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (tid >= (long long)W * H * r.num_envs) return;
+    int e = (int)(tid / (W * H));
+    int et = (int)(tid % (W * H));
+    int x = et % W;
+    int y = H - et / W;
+    int cam = r.num_cameras > 1 ? e : 0;
+    v3 ro = ld3(r.camera_pos, cam);
+    float4 q = reinterpret_cast<const float4*>(r.camera_rot)[cam];
+    EnvView ev = env_view(b, e);
+    Shade s = trace(r, ev, ro, q, x, y, W, H);
+    st3(r.rays, tid, s.color);
+    r.ray_depth[tid] = s.depth;
+}
+
+// downsample_kernel (render.py:699-724), 2x2 rays per pixel
+__global__ void k_downsample(ffsrl_render r) {
+    const int R = r.resolution, W = 2 * R;
+    long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (tid >= (long long)R * R * r.num_envs) return;
+    long long px = tid % R, py = tid / R;
+    long long start = py * 2 * W + px * 2;
+    v3 c = mk(0.0f, 0.0f, 0.0f);
+    float d = 0.0f;
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j) {
+            v3 s = ld3(r.rays, start + i * W + j);
+            c = mk(c.x + s.x, c.y + s.y, c.z + s.z);
+            d = d + r.ray_depth[start + i * W + j];
+        }
+    float nsq = float(2 * 2);
+    if (r.color) st3(r.color, tid, mk(c.x / nsq, c.y / nsq, c.z / nsq));
+    if (r.depth) r.depth[tid] = d / nsq;
+}
+
+// One thread per output pixel: its 2x2 rays traced in the downsample order, averaged.
+// Blocks cover 8x8 pixel tiles of one env so neighbouring rays share BVH nodes in L1.
+__global__ void __launch_bounds__(64) k_pixel(ffsrl_render r, ffsrl_bvh b) {
+    const int R = r.resolution, W = 2 * R, H = 2 * R;
+    const int tiles_x = (R + 7) / 8;
+    const int tiles = tiles_x * ((R + 7) / 8);
+    int e = blockIdx.x / tiles;
+    int tile = blockIdx.x % tiles;
+    int px = (tile % tiles_x) * 8 + (threadIdx.x & 7);
+    int py = (tile / tiles_x) * 8 + (threadIdx.x >> 3);
+    if (e >= r.num_envs || px >= R || py >= R) return;
+    int cam = r.num_cameras > 1 ? e : 0;
+    v3 ro = ld3(r.camera_pos, cam);
+    float4 q = reinterpret_cast<const float4*>(r.camera_rot)[cam];
+    EnvView ev = env_view(b, e);
+    v3 c = mk(0.0f, 0.0f, 0.0f);
+    float d = 0.0f;
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j) {
+            int rx = 2 * px + j, ry = 2 * py + i;  // ray index (ry * W + rx) as in downsample_kernel
+            int et = ry * W + rx;
+            Shade s = trace(r, ev, ro, q, et % W, H - et / W, W, H);
+            c = mk(c.x + s.color.x, c.y + s.color.y, c.z + s.color.z);
+            d = d + s.depth;
+        }
+    float nsq = float(2 * 2);
+    long long o = (long long)e * R * R + (long long)py * R + px;
+    if (r.color) st3(r.color, o, mk(c.x / nsq, c.y / nsq, c.z / nsq));
+    if (r.depth) r.depth[o] = d / nsq;
+}
+
+int32_t check_bvh(const ffsrl_bvh* b) {
+    if (!b || b->num_envs <= 0 || !b->env_topology || !b->env_node_offset || !b->env_face_offset ||
+        !b->topo_node_offset || !b->topo_tri_offset || !b->topo_max_level || !b->left_node || !b->first_tri_id ||
+        !b->tri_count || !b->level || !b->tri_id || !b->aabb_min || !b->aabb_max || b->total_env_nodes <= 0)
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_bvh: missing arrays or empty");
+    return FFSRL_OK;
+}
+
+int32_t check_render(const ffsrl_render* r) {
+    if (!r || r->num_envs <= 0 || r->resolution <= 0 || !r->vis_point || !r->vis_face || !r->vis_point_color ||
+        !r->vertex_normal || !r->camera_pos || !r->camera_rot || r->num_cameras <= 0 ||
+        (r->num_lights > 0 && (!r->light_dir || !r->light_intensity)) || !r->error_flag)
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_render: missing arrays");
+    if (r->num_cameras != 1 && r->num_cameras != r->num_envs)
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_render: num_cameras must be 1 or num_envs");
+    if (((uintptr_t)r->camera_rot) & 15)
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_render: camera_rot must be 16-byte aligned");
+    return FFSRL_OK;
+}
+
+}  // namespace
+}  // namespace ffsrl
+
+using namespace ffsrl;
+
+extern "C" int32_t ffsrl_bvh_refit_levels(const ffsrl_bvh* b, const float* pts, const int32_t* faces, void* stream) {
+    if (int32_t st = check_bvh(b)) return st;
+    if (!pts || !faces) return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_bvh_refit_levels: null points/faces");
+    for (int L = b->max_level; L >= 0; --L)
+        k_refit_level<<<grid_for(b->total_env_nodes, 256), 256, 0, (cudaStream_t)stream>>>(*b, pts, faces, L);
+    FFSRL_LAUNCH_CHECK("ffsrl_bvh_refit_levels");
+    return FFSRL_OK;
+}
+
+extern "C" int32_t ffsrl_bvh_refit_fused(const ffsrl_bvh* b, const float* pts, const int32_t* faces, void* stream) {
+    if (int32_t st = check_bvh(b)) return st;
+    if (!pts || !faces || !b->level_node || !b->level_start || !b->topo_level_offset)
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_bvh_refit_fused: needs level grouping arrays");
+    k_refit_fused<<<b->num_envs, 256, 0, (cudaStream_t)stream>>>(*b, pts, faces);
+    FFSRL_LAUNCH_CHECK("ffsrl_bvh_refit_fused");
+    return FFSRL_OK;
+}
+
+extern "C" int32_t ffsrl_render_reference(const ffsrl_render* r, const ffsrl_bvh* b, void* stream) {
+    if (int32_t st = check_render(r)) return st;
+    if (int32_t st = check_bvh(b)) return st;
+    if (!r->normal_sum || !r->rays || !r->ray_depth)
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_render_reference: needs normal_sum, rays, ray_depth scratch");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int P = r->num_vis_points, Fv = r->num_vis_faces;
+    k_zero3<<<grid_for(P, 256), 256, 0, s>>>(r->normal_sum, P);
+    if (Fv > 0) k_normal_sum<<<grid_for(Fv, 256), 256, 0, s>>>(r->vis_point, r->vis_face, r->normal_sum, Fv);
+    k_normalize<<<grid_for(P, 256), 256, 0, s>>>(r->normal_sum, r->vertex_normal, P);
+    long long rays = 4ll * r->resolution * r->resolution * r->num_envs;
+    k_draw<<<grid_for(rays, 128), 128, 0, s>>>(*r, *b);
+    long long pix = (long long)r->resolution * r->resolution * r->num_envs;
+    k_downsample<<<grid_for(pix, 256), 256, 0, s>>>(*r);
+    FFSRL_LAUNCH_CHECK("ffsrl_render_reference");
+    return FFSRL_OK;
+}
+
+extern "C" int32_t ffsrl_render_fused(const ffsrl_render* r, const ffsrl_bvh* b, void* stream) {
+    if (int32_t st = check_render(r)) return st;
+    if (int32_t st = check_bvh(b)) return st;
+    if (!r->point_face_start || !r->point_face)
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_render_fused: needs the point->face CSR");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int P = r->num_vis_points;
+    k_normal_gather<<<grid_for(P, 256), 256, 0, s>>>(r->vis_point, r->vis_face, r->point_face_start, r->point_face,
+                                                     r->vertex_normal, P);
+    const int tiles = ((r->resolution + 7) / 8) * ((r->resolution + 7) / 8);
+    k_pixel<<<(unsigned)((long long)tiles * r->num_envs), 64, 0, s>>>(*r, *b);
+    FFSRL_LAUNCH_CHECK("ffsrl_render_fused");
+    return FFSRL_OK;
+}

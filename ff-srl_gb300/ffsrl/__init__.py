@@ -1,0 +1,15 @@
+"""ffsrl: GB300-native multi-environment soft-tissue step, BVH refit and ray-cast.
+
+Public classes keep the reference's names (``FF_SRL/FF_SRL/__init__.py:1-6``):
+``SimModelDO``, ``SimIntegratorDO``, ``SimBVH``, ``WarpRaycastRendererDO``.
+"""
+
+from . import meshgen
+from ._lib import FFSRLError
+from .model import SimModelDO
+from .integrator import SimIntegratorDO, BatchPlan
+from .bvh import SimBVH
+from .render import WarpRaycastRendererDO, quat_rpy, look_at_rotation
+
+__all__ = ["SimModelDO", "SimIntegratorDO", "BatchPlan", "SimBVH", "WarpRaycastRendererDO", "meshgen",
+           "FFSRLError", "quat_rpy", "look_at_rotation"]

@@ -1,0 +1,120 @@
+"""SimIntegratorDO: the multi-environment step (reference ``FF_SRL/FF_SRL/integrator.py:1634-1744``).
+
+``stepModel(simModel)`` advances every environment by one step of ``simSubsteps``
+substeps x ``simConstraints`` Jacobi iterations and then maps the simulated vertices
+onto the visual points (``transformSimMeshData``), as the reference does.
+
+Two GPU forms with the same semantics:
+
+* ``batched=True`` (default): the env-resident batched kernel -- one persistent launch per
+  mesh-size class, every substep and iteration of an environment on one SM, shared-memory
+  positions and deterministic fixed-point correction sums;
+* ``batched=False``: the reference-shaped form -- one kernel launch per reference kernel
+  in the reference's launch order, float atomics.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check, lib, ptr
+
+
+class BatchPlan:
+    """Owner of an ffsrl_batch handle (packed constraint tables, work lists, streams)."""
+
+    def __init__(self, model, block_threads: int = 0, precision: int = 32):
+        model.require_cuda()
+        hm, self._host_arrays = model.host_model()
+        self._dm = model.device_model()
+        self._params = model.params()
+        opts = _lib.BatchOptions()
+        opts.block_threads = int(block_threads)
+        opts.deterministic = 1
+        opts.reserved[0] = int(precision)
+        h = C.c_void_p()
+        check(lib().ffsrl_batch_create(C.byref(hm), C.byref(self._dm), C.byref(self._params), C.byref(opts),
+                                       C.byref(h)))
+        self.handle = h
+        self.model = model
+        self.precision = precision
+        self._host_arrays = None  # the plan has copied what it needs
+
+    def step(self, n_steps: int = 1, stream=None) -> None:
+        check(lib().ffsrl_batch_step(self.handle, int(n_steps), _lib.stream_handle(stream)))
+
+    def step_envs(self, env_ids, n_steps: int = 1, stream=None) -> None:
+        ids = np.ascontiguousarray(np.asarray(env_ids, dtype=np.int32))
+        check(lib().ffsrl_batch_step_envs(self.handle, ids.ctypes.data, int(ids.size), int(n_steps),
+                                          _lib.stream_handle(stream)))
+
+    def info(self) -> dict:
+        nbytes = C.c_int64()
+        ncls = C.c_int32()
+        check(lib().ffsrl_batch_info(self.handle, C.byref(nbytes), C.byref(ncls), None))
+        blocks = np.zeros(max(ncls.value, 1), dtype=np.int32)
+        check(lib().ffsrl_batch_info(self.handle, None, None, blocks.ctypes.data))
+        return {"device_bytes": int(nbytes.value), "num_classes": int(ncls.value),
+                "block_threads": blocks[:ncls.value].tolist()}
+
+    def env_status(self) -> np.ndarray:
+        out = np.zeros(self.model.numEnvs, dtype=np.int32)
+        check(lib().ffsrl_batch_env_status(self.handle, out.ctypes.data, self.model.numEnvs))
+        return out
+
+    def state_f64(self) -> dict:
+        V = self.model.numVertices
+        out = np.zeros(9 * V, dtype=np.float64)
+        check(lib().ffsrl_batch_state_f64(self.handle, out.ctypes.data))
+        return {"vertex": out[:3 * V].reshape(-1, 3), "velocity": out[3 * V:6 * V].reshape(-1, 3),
+                "predicted_vertex": out[6 * V:].reshape(-1, 3)}
+
+    def close(self) -> None:
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            lib().ffsrl_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class SimIntegratorDO:
+    """Reference-compatible integrator: ``SimIntegratorDO(device).stepModel(simModel)``."""
+
+    def __init__(self, device="cuda:0", batched: bool = True, blockThreads: int = 0) -> None:
+        self.device = device
+        self.batched = bool(batched)
+        self.blockThreads = int(blockThreads)
+        self._plans = {}
+
+    def plan(self, simModel) -> BatchPlan:
+        key = id(simModel)
+        p = self._plans.get(key)
+        if p is None or p.model is not simModel:
+            p = BatchPlan(simModel, self.blockThreads)
+            self._plans[key] = p
+        return p
+
+    def stepModel(self, simModel, steps: int = 1, stream=None) -> None:
+        simModel.require_cuda()
+        if self.batched:
+            self.plan(simModel).step(steps, stream)
+        else:
+            m = simModel.device_model()
+            prm = simModel.params()
+            s = _lib.stream_handle(stream)
+            for _ in range(int(steps)):
+                check(lib().ffsrl_step_model(C.byref(m), C.byref(prm), s))
+        simModel.transformSimMeshData(stream)
+        simModel.transformSimLaparoscopeMeshData()
+
+    def envStatus(self, simModel) -> np.ndarray:
+        """Per-env status of the last batched step (0 ok, 7 non-finite state)."""
+        return self.plan(simModel).env_status()

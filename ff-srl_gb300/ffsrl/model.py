@@ -1,0 +1,425 @@
+"""SimModelDO: the multi-environment state arrays (reference ``FF_SRL/FF_SRL/modelDO.py:772-1645``).
+
+Every quantity is one flat array over all environments, in the reference's layout
+(``modelDO.py:1141-1246``): vec3 arrays are float32 ``[n, 3]``, index arrays int32 holding
+global ids.  The arrays are torch tensors on the model's device, so RL code reads them
+without copies (the reference's ``wp.to_torch`` getters, ``modelDO.py:1483-1518``).
+
+The reference builds the arrays from a USD stage (``modelDO.py:774-1266``).  USD cannot be
+read here; ``stage`` is instead an array-based scene: one mesh dict (as produced by
+``ffsrl.meshgen``) replicated over ``numEnvs`` environments, as the reference does, or a
+list of ``numEnvs`` mesh dicts for environments with different meshes.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check, lib, ptr
+
+_MESH_KEYS = ("vertex", "inverse_mass", "tetrahedron", "tetrahedron_rest_volume", "edge", "edge_rest_length",
+              "triangle", "vis_face", "point_to_vertex", "vis_point_color")
+
+
+def _cat(parts, dtype):
+    if not parts:
+        return np.zeros(0, dtype=dtype)
+    return np.ascontiguousarray(np.concatenate(parts), dtype=dtype)
+
+
+class SimModelDO:
+    """Multi-environment soft-body model.
+
+    Keyword arguments and their defaults are the reference's (``modelDO.py:774-802``);
+    the instrument-kinematics ones (workspace boxes) are accepted and stored.  Added:
+
+    * ``constraints``: ffsrl flag set of constraint kernels run per iteration (default:
+      the reference DO step's volume, distance, drag, connectors and contact);
+    * ``distanceCompliance`` / ``volumeComplianceXPBD``: XPBD alphas for the compliant
+      variants (``integrator.py:191-240, 507-576``);
+    * ``toolRadius``: capsule radii of the synthetic instrument (rod, clamps).
+    """
+
+    def __init__(self, stage, numEnvs, device="cuda:0",
+                 simSubsteps=8, simFrameRate=60, simConstraintsSteps=1,
+                 environmentGravity=(0.0, -9.8, 0.0), environmentVelocityDampening=0.1, environmentGroundLevel=0.0,
+                 globalKsDistance=1.0, globalKsVolume=1.0, globalKsContact=1.0, globalKsDrag=1.0,
+                 globalVolumeCompliance=1.0, globalDeviatoricCompliance=1.0,
+                 globalBreakFactor=1.0, globalBreakThreshold=1.0, globalHeatLoss=1.0, globalHeatConduction=1.0,
+                 globalHeatTransfer=1.0, globalHeatLimit=1.0, globalHeatSphereRadius=1.0, globalHeatQuantum=1.0,
+                 globalLaparoscopeDragLookupRadius=0.15, globalConnectorMassWeightRatio=0.75, globalConnectorKs=0.125,
+                 globalConnectorRestLengthMul=0.02,
+                 workspaceLow=(-1e5, -1e5, -1e5), workspaceHigh=(1e5, 1e5, 1e5),
+                 startingBoxLow=(-1e5, -1e5, -1e5), startingBoxHigh=(1e5, 1e5, 1e5),
+                 constraints=None, distanceCompliance=0.0, volumeComplianceXPBD=0.0,
+                 toolRadius=(0.004, 0.002, 0.002)):
+        if hasattr(stage, "GetPrimAtPath"):
+            raise _lib.FFSRLError(_lib.ERR_UNSUPPORTED,
+                                  "USD stages are not supported; pass ffsrl.meshgen mesh dicts (array scene)")
+        meshes = stage if isinstance(stage, (list, tuple)) else [stage] * int(numEnvs)
+        if len(meshes) != int(numEnvs):
+            raise ValueError(f"got {len(meshes)} meshes for {numEnvs} environments")
+        self.device = torch.device(device)
+        self.numEnvs = int(numEnvs)
+        self.cartesianActions = 3
+        self.simSubsteps = int(simSubsteps)
+        self.simFrameRate = simFrameRate
+        self.simConstraints = int(simConstraintsSteps)
+        self.simDt = (1.0 / self.simFrameRate) / self.simSubsteps
+        self.gravity = tuple(float(g) for g in environmentGravity)
+        self.velocityDampening = float(environmentVelocityDampening)
+        self.groundLevel = float(environmentGroundLevel)
+        self.globalKsDistance = float(globalKsDistance)
+        self.globalDistanceCompliance = globalKsDistance / (self.simDt * self.simDt)
+        self.globalKsVolume = float(globalKsVolume)
+        self.globalVolumeCompliance = globalKsVolume / (self.simDt * self.simDt)
+        self.globalKsContact = float(globalKsContact)
+        self.globalKsDrag = float(globalKsDrag)
+        self.globalVolumeComplianceNeoHookean = float(globalVolumeCompliance)
+        self.gloabalDeviatoricComplianceNeoHookean = float(globalDeviatoricCompliance)
+        self.globalLaparoscopeDragLookupRadius = float(globalLaparoscopeDragLookupRadius)
+        self.globalBreakFactor, self.globalBreakThreshold = globalBreakFactor, globalBreakThreshold
+        self.globalHeatLoss, self.globalHeatConduction = globalHeatLoss, globalHeatConduction
+        self.globalHeatTransfer, self.globalHeatLimit = globalHeatTransfer, globalHeatLimit
+        self.globalHeatSphereRadius, self.globalHeatQuantum = globalHeatSphereRadius, globalHeatQuantum
+        self.globalConnectorMassWeightRatio = float(globalConnectorMassWeightRatio)
+        self.globalConnectorKs = float(globalConnectorKs)
+        self.globalConnectorRestLengthMul = float(globalConnectorRestLengthMul)
+        self.workspaceLow, self.workspaceHigh = tuple(workspaceLow), tuple(workspaceHigh)
+        self.startingBoxLow, self.startingBoxHigh = tuple(startingBoxLow), tuple(startingBoxHigh)
+        self.constraintFlags = _lib.REFERENCE_STEP if constraints is None else int(constraints)
+        self.distanceComplianceXPBD = float(distanceCompliance)
+        self.volumeComplianceXPBD = float(volumeComplianceXPBD)
+        self.reduce = False
+
+        # distinct meshes (topologies) and the env -> mesh map
+        uniq, self.envMesh = [], []
+        for m in meshes:
+            for k, u in enumerate(uniq):
+                if u is m:
+                    self.envMesh.append(k)
+                    break
+            else:
+                uniq.append(m)
+                self.envMesh.append(len(uniq) - 1)
+        self.meshes = uniq
+        self._concatenate(meshes, toolRadius)
+        self._upload()
+        self._batch = None
+
+    # ------------------------------------------------------------------ build
+    def _concatenate(self, meshes, toolRadius):
+        N = self.numEnvs
+        nv = np.array([len(m["vertex"]) for m in meshes], dtype=np.int64)
+        nt = np.array([len(m["tetrahedron"]) for m in meshes], dtype=np.int64)
+        ne = np.array([len(m["edge"]) for m in meshes], dtype=np.int64)
+        nf = np.array([len(m["triangle"]) for m in meshes], dtype=np.int64)
+        npnt = np.array([len(m["point_to_vertex"]) for m in meshes], dtype=np.int64)
+        nvf = np.array([len(m["vis_face"]) for m in meshes], dtype=np.int64)
+        z = np.zeros(1, dtype=np.int64)
+        if int(nv.sum()) >= 2**31 or 4 * int(nt.sum()) >= 2**31 or 3 * int(nf.sum()) >= 2**31:
+            raise ValueError("model exceeds int32 indexing")
+        self.envVertexStart = np.concatenate([z, np.cumsum(nv)]).astype(np.int32)
+        self.envTetStart = np.concatenate([z, np.cumsum(nt)]).astype(np.int32)
+        self.envEdgeStart = np.concatenate([z, np.cumsum(ne)]).astype(np.int32)
+        self.envTriStart = np.concatenate([z, np.cumsum(nf)]).astype(np.int32)
+        self.envVisPointStart = np.concatenate([z, np.cumsum(npnt)]).astype(np.int32)
+        self.envVisFaceStart = np.concatenate([z, np.cumsum(nvf)]).astype(np.int32)
+        vo, po = self.envVertexStart[:-1].astype(np.int64), self.envVisPointStart[:-1].astype(np.int64)
+        h = {}
+        h["vertex"] = _cat([m["vertex"] for m in meshes], np.float32).reshape(-1, 3)
+        h["inverseMass"] = _cat([m["inverse_mass"] for m in meshes], np.float32)
+        h["tetrahedron"] = _cat([m["tetrahedron"].reshape(-1) + vo[e] for e, m in enumerate(meshes)], np.int32)
+        h["tetrahedronRestVolume"] = _cat([m["tetrahedron_rest_volume"] for m in meshes], np.float32)
+        h["tetrahedronRestVolumeSigned"] = _cat(
+            [m.get("tetrahedron_rest_volume_signed", -m["tetrahedron_rest_volume"]) for m in meshes], np.float32)
+        h["tetrahedronDmInv"] = _cat([m["tetrahedron_dm_inv"].reshape(-1) for m in meshes], np.float32)
+        h["edge"] = _cat([m["edge"].reshape(-1) + vo[e] for e, m in enumerate(meshes)], np.int32)
+        h["edgeRestLength"] = _cat([m["edge_rest_length"] for m in meshes], np.float32)
+        h["triangle"] = _cat([m["triangle"].reshape(-1) + vo[e] for e, m in enumerate(meshes)], np.int32)
+        h["triToEnv"] = np.repeat(np.arange(N, dtype=np.int32), nf)
+        h["vertexToEnv"] = np.repeat(np.arange(N, dtype=np.int32), nv)
+        h["allVisFace"] = _cat([m["vis_face"].reshape(-1) + po[e] for e, m in enumerate(meshes)], np.int32)
+        h["allVisPointColor"] = _cat([m["vis_point_color"] for m in meshes], np.float32).reshape(-1, 3)
+        ptv = []
+        for e, m in enumerate(meshes):
+            pv = m["point_to_vertex"].astype(np.int64).copy()
+            pv[:, 0] += po[e]
+            pv[:, 1] += vo[e]
+            ptv.append(pv.reshape(-1))
+        h["pointToVertex"] = _cat(ptv, np.int32)
+        # grasp candidates: the surface (visual) vertices of each env
+        self.graspCandStart = self.envVisPointStart.copy()
+        h["graspCand"] = h["pointToVertex"][1::2].copy()
+        self.host = h
+
+        self.numVertices = int(self.envVertexStart[-1])
+        self.numTetrahedrons = int(self.envTetStart[-1])
+        self.numEdges = int(self.envEdgeStart[-1])
+        self.numTriangles = int(self.envTriStart[-1])
+        self.numVisPoints = int(self.envVisPointStart[-1])
+        self.numAllVisPoints = self.numVisPoints
+        self.numVisFaces = int(self.envVisFaceStart[-1])
+        self.numAllVisFaces = self.numVisFaces
+        self.simConnectors = 0
+        # per-env sizes (the reference assumes identical envs; these hold env 0's)
+        self.environmentNumVertices = int(nv[0])
+        self.numEnvAllVertices = int(nv[0])
+        self.numEnvMeshesVisPoints = int(npnt[0])
+        self.numEnvMeshesVisFaces = int(nvf[0])
+        self.numEnvRigidsVisFaces = 0
+        self.numEnvLaparoscopeVisFaces = 0
+
+        # synthetic instrument: 3 capsules + drag point per env, parked far above
+        r = np.asarray(toolRadius, dtype=np.float32)
+        base = np.zeros((4 * N, 3), dtype=np.float32)
+        tip = np.zeros((4 * N, 3), dtype=np.float32)
+        tip[:, 1] = 10.0
+        base[:, 1] = 10.1
+        rad = np.tile(np.array([r[0], r[1], r[2], 0.0], dtype=np.float32), N)
+        self.toolHost = {"base": base, "tip": tip, "radius": rad}
+
+    def _upload(self):
+        d = self.device
+        h = self.host
+        f32 = dict(dtype=torch.float32, device=d)
+        i32 = dict(dtype=torch.int32, device=d)
+
+        def T(a, **kw):
+            return torch.as_tensor(np.ascontiguousarray(a), **kw).clone()
+
+        self.vertex = T(h["vertex"], **f32)
+        self.initialVertex = self.vertex.clone()
+        self.predictedVertex = torch.zeros_like(self.vertex)
+        self.velocity = torch.zeros_like(self.vertex)
+        self.initialVelocity = torch.zeros_like(self.vertex)
+        self.dP = torch.zeros_like(self.vertex)
+        self.collisionDP = torch.zeros_like(self.vertex)
+        self.constraintsNumber = torch.zeros(self.numVertices, **i32)
+        self.inverseMass = T(h["inverseMass"], **f32)
+        self.tetrahedron = T(h["tetrahedron"], **i32)
+        self.tetrahedronRestVolume = T(h["tetrahedronRestVolume"], **f32)
+        self.tetrahedronRestVolumeSigned = T(h["tetrahedronRestVolumeSigned"], **f32)
+        self.activeTetrahedron = torch.ones(self.numTetrahedrons, **f32)
+        self.tetrahedronDmInv = T(h["tetrahedronDmInv"], **f32)
+        self.tetrahedronLambda = torch.zeros(self.numTetrahedrons, **f32)
+        self.edge = T(h["edge"], **i32)
+        self.edgeRestLength = T(h["edgeRestLength"], **f32)
+        self.activeEdge = torch.ones(self.numEdges, **f32)
+        self.edgeLambda = torch.zeros(self.numEdges, **f32)
+        self.triangle = T(h["triangle"], **i32)
+        self.hole = torch.zeros(self.numTriangles, **i32)
+        self.triToEnv = T(h["triToEnv"], **i32)
+        self.vertexToEnv = T(h["vertexToEnv"], **i32)
+        self.activeDragConstraint = torch.zeros(self.numVertices, **f32)
+        ptv = h["pointToVertex"].reshape(-1, 2)
+        vis0 = np.zeros((self.numVisPoints, 3), dtype=np.float32)
+        vis0[ptv[:, 0]] = h["vertex"][ptv[:, 1]]
+        self.allVisPoint = T(vis0, **f32)
+        self.visPoint = self.allVisPoint
+        self.allVisFace = T(h["allVisFace"], **i32)
+        self.visFace = self.allVisFace
+        self.allVisPointColor = T(h["allVisPointColor"], **f32)
+        self.pointToVertex = T(h["pointToVertex"], **i32)
+        self.graspCand = T(h["graspCand"], **i32)
+        self.graspCandStartT = T(self.graspCandStart, **i32)
+        self.laparoscopeBase = T(self.toolHost["base"], **f32)
+        self.laparoscopeTip = T(self.toolHost["tip"], **f32)
+        self.laparoscopeRadius = T(self.toolHost["radius"], **f32)
+        self.laparoscopeInitialBase = self.laparoscopeBase.clone()
+        self.laparoscopeInitialTip = self.laparoscopeTip.clone()
+        self.laparoscopeInCollision = torch.zeros(self.numEnvs, **i32)
+        self.laparoscopeDragCutHeat = torch.zeros(3 * self.numEnvs, **i32)
+        self.laparoscopeDragCutHeatUpdate = torch.zeros(3 * self.numEnvs, **i32)
+        self.envStatus = torch.zeros(self.numEnvs, **i32)
+        self.envVertexStartT = T(self.envVertexStart, **i32)
+        self.envTetStartT = T(self.envTetStart, **i32)
+        self.envEdgeStartT = T(self.envEdgeStart, **i32)
+        self.envTriStartT = T(self.envTriStart, **i32)
+        self.connectorVertexId = torch.zeros(0, **i32)
+        self.connectorTriangleId = torch.zeros(0, **i32)
+        self.connectorTriBar = torch.zeros((0, 3), **f32)
+        self.connectorRestDist = torch.zeros(0, **f32)
+
+    # ------------------------------------------------------------ descriptors
+    def require_cuda(self) -> None:
+        """Every GPU entry point checks this: a host pointer given to a kernel would fault."""
+        if self.device.type != "cuda":
+            raise _lib.FFSRLError(_lib.ERR_INVALID_ARGUMENT,
+                                  f"model arrays live on {self.device}; GPU entry points need a CUDA device")
+
+    def params(self) -> _lib.Params:
+        p = _lib.Params()
+        p.substeps, p.iterations, p.flags = self.simSubsteps, self.simConstraints, self.constraintFlags
+        p.dt = self.simDt
+        p.gravity[:] = self.gravity
+        p.velocity_dampening, p.ground_level = self.velocityDampening, self.groundLevel
+        p.ks_distance, p.ks_volume = self.globalKsDistance, self.globalKsVolume
+        p.ks_contact, p.ks_drag = self.globalKsContact, self.globalKsDrag
+        p.volume_compliance = self.globalVolumeComplianceNeoHookean
+        p.deviatoric_compliance = self.gloabalDeviatoricComplianceNeoHookean
+        p.distance_compliance, p.volume_compliance_xpbd = self.distanceComplianceXPBD, self.volumeComplianceXPBD
+        p.connector_mass_weight_ratio = self.globalConnectorMassWeightRatio
+        p.connector_ks, p.connector_rest_length_mul = self.globalConnectorKs, self.globalConnectorRestLengthMul
+        return p
+
+    def _fill(self, m: _lib.Model, src: dict) -> _lib.Model:
+        m.num_vertices, m.num_tetrahedrons = self.numVertices, self.numTetrahedrons
+        m.num_edges, m.num_triangles = self.numEdges, self.numTriangles
+        m.num_connectors, m.num_envs = self.simConnectors, self.numEnvs
+        for k, v in src.items():
+            setattr(m, k, ptr(v))
+        return m
+
+    def device_model(self) -> _lib.Model:
+        self.require_cuda()
+        return self._fill(_lib.Model(), {
+            "vertex": self.vertex, "predicted_vertex": self.predictedVertex, "velocity": self.velocity,
+            "dp": self.dP, "constraints_number": self.constraintsNumber, "collision_dp": self.collisionDP,
+            "inverse_mass": self.inverseMass, "tetrahedron": self.tetrahedron,
+            "tetrahedron_rest_volume": self.tetrahedronRestVolume, "active_tetrahedron": self.activeTetrahedron,
+            "tetrahedron_dm_inv": self.tetrahedronDmInv, "tetrahedron_lambda": self.tetrahedronLambda,
+            "xpbd_rest_volume": self.tetrahedronRestVolumeSigned, "edge": self.edge,
+            "edge_rest_length": self.edgeRestLength, "active_edge": self.activeEdge, "edge_lambda": self.edgeLambda,
+            "triangle": self.triangle, "tri_to_env": self.triToEnv, "hole": self.hole,
+            "vertex_to_env": self.vertexToEnv, "active_drag_constraint": self.activeDragConstraint,
+            "laparoscope_base": self.laparoscopeBase, "laparoscope_tip": self.laparoscopeTip,
+            "laparoscope_radius": self.laparoscopeRadius, "laparoscope_in_collision": self.laparoscopeInCollision,
+            "connector_triangle_id": self.connectorTriangleId, "connector_tri_bar": self.connectorTriBar,
+            "connector_vertex_id": self.connectorVertexId, "connector_rest_dist": self.connectorRestDist,
+            "env_vertex_start": self.envVertexStartT, "env_tet_start": self.envTetStartT,
+            "env_edge_start": self.envEdgeStartT, "env_tri_start": self.envTriStartT,
+        })
+
+    def host_model(self) -> tuple[_lib.Model, dict]:
+        """Descriptor over host copies of the constant arrays (and the current state).
+
+        Returns the descriptor and the dict of numpy arrays it points into (keep it alive).
+        """
+        h = self.host
+        arrs = {
+            "vertex": self.vertex.detach().cpu().numpy().copy(),
+            "predicted_vertex": self.predictedVertex.detach().cpu().numpy().copy(),
+            "velocity": self.velocity.detach().cpu().numpy().copy(),
+            "inverse_mass": h["inverseMass"], "tetrahedron": h["tetrahedron"],
+            "tetrahedron_rest_volume": h["tetrahedronRestVolume"],
+            "active_tetrahedron": self.activeTetrahedron.cpu().numpy().copy(),
+            "tetrahedron_dm_inv": h["tetrahedronDmInv"], "xpbd_rest_volume": h["tetrahedronRestVolumeSigned"],
+            "edge": h["edge"], "edge_rest_length": h["edgeRestLength"],
+            "active_edge": self.activeEdge.cpu().numpy().copy(), "triangle": h["triangle"],
+            "tri_to_env": h["triToEnv"], "hole": self.hole.cpu().numpy().copy(), "vertex_to_env": h["vertexToEnv"],
+            "active_drag_constraint": self.activeDragConstraint.cpu().numpy().copy(),
+            "laparoscope_base": self.laparoscopeBase.cpu().numpy().copy(),
+            "laparoscope_tip": self.laparoscopeTip.cpu().numpy().copy(),
+            "laparoscope_radius": self.laparoscopeRadius.cpu().numpy().copy(),
+            "laparoscope_in_collision": self.laparoscopeInCollision.cpu().numpy().copy(),
+            "env_vertex_start": self.envVertexStart, "env_tet_start": self.envTetStart,
+            "env_edge_start": self.envEdgeStart, "env_tri_start": self.envTriStart,
+        }
+        return self._fill(_lib.Model(), arrs), arrs
+
+    # ----------------------------------------------------- reference methods
+    def transformSimMeshData(self, stream=None):
+        """remapAToB of the simulated vertices onto the visual points (modelDO.py:1441-1444)."""
+        self.require_cuda()
+        check(lib().ffsrl_remap(ptr(self.allVisPoint), ptr(self.vertex), ptr(self.pointToVertex),
+                                self.numVisPoints, _lib.stream_handle(stream)))
+
+    def transformSimLaparoscopeMeshData(self):
+        """The instrument's visual mesh is not part of this model (synthetic instrument)."""
+
+    def getVertexPositionsTensor(self, vertexId):
+        return self.vertex[vertexId]
+
+    def getVertexPositionsTensorMultiEnvs(self, vertexIds):
+        idx = torch.as_tensor(self.envVertexStart[:-1], device=self.device, dtype=torch.long) + \
+            torch.as_tensor(vertexIds, device=self.device, dtype=torch.long)
+        return self.vertex[idx]
+
+    def getLaparoscopePositionsTensor(self):
+        return self.laparoscopeTip[3::4]
+
+    def getLaparoscopeClampVertex(self, vertexId):
+        return self.activeDragConstraint[vertexId]
+
+    def getLaparoscopeInCollision(self):
+        return self.laparoscopeInCollision
+
+    def resetCollisionInfo(self):
+        """Zero the per-env contact counters in place (the reference reallocates the array,
+        ``modelDO.py:1520-1522``, which a captured graph would not see)."""
+        self.laparoscopeInCollision.zero_()
+
+    def forceLaparoscopeClampVertex(self, vertexId: int, envs, on: float = 1.0, animate: bool = True):
+        """forceClampsDragKernel (modelDO.py:281-289) for the envs where ``envs`` is nonzero.
+        The clamp animation of the instrument model is not part of this model."""
+        self.require_cuda()
+        env_ids = torch.nonzero(torch.as_tensor(envs, device=self.device)).to(torch.int32).flatten().contiguous()
+        check(lib().ffsrl_force_clamps_drag(ptr(self.activeDragConstraint), int(vertexId), ptr(env_ids),
+                                            int(env_ids.numel()), float(on), self.environmentNumVertices,
+                                            _lib.stream_handle()))
+
+    def updateClampsDrag(self, state, update, lookupRadius=None):
+        """updateClampsDragKernel (modelDO.py:247-279): state/update are int32 [3N] tensors."""
+        self.require_cuda()
+        r = self.globalLaparoscopeDragLookupRadius if lookupRadius is None else float(lookupRadius)
+        check(lib().ffsrl_update_clamps_drag(ptr(self.predictedVertex), ptr(self.vertexToEnv),
+                                             ptr(self.laparoscopeTip), ptr(self.activeDragConstraint), r,
+                                             ptr(state), ptr(update), self.numVertices, _lib.stream_handle()))
+
+    def graspNearest(self, clamp, radius=None, stream=None):
+        """Per env, grasp the surface vertex nearest the drag point within ``radius`` when
+        ``clamp[e]`` is nonzero, release the env's grasp when it is zero."""
+        self.require_cuda()
+        r = self.globalLaparoscopeDragLookupRadius if radius is None else float(radius)
+        clamp = torch.as_tensor(clamp, device=self.device, dtype=torch.int32).contiguous()
+        check(lib().ffsrl_grasp_nearest(ptr(self.vertex), ptr(self.graspCandStartT), ptr(self.graspCand),
+                                        ptr(self.laparoscopeTip), ptr(clamp), r, ptr(self.activeDragConstraint),
+                                        self.numEnvs, _lib.stream_handle(stream)))
+
+    def moveTool(self, disp, stream=None):
+        """Translate every env's instrument by ``disp`` [N, 3] (device tensor)."""
+        self.require_cuda()
+        disp = disp.contiguous()
+        check(lib().ffsrl_move_tool(ptr(self.laparoscopeBase), ptr(self.laparoscopeTip), ptr(disp), self.numEnvs,
+                                    _lib.stream_handle(stream)))
+
+    def setTool(self, base, tip, radius=None):
+        """Set the instrument's capsule ends [4N, 3] (and radii [4N])."""
+        self.laparoscopeBase.copy_(torch.as_tensor(base, dtype=torch.float32))
+        self.laparoscopeTip.copy_(torch.as_tensor(tip, dtype=torch.float32))
+        if radius is not None:
+            self.laparoscopeRadius.copy_(torch.as_tensor(radius, dtype=torch.float32))
+
+    def setEffectorInitialPosition(self):
+        self.laparoscopeInitialBase.copy_(self.laparoscopeBase)
+        self.laparoscopeInitialTip.copy_(self.laparoscopeTip)
+
+    def resetFixedModel(self, envNums):
+        """Restore the listed envs' vertices and instrument, zero their velocity,
+        predicted positions and grasp (modelDO.py:1589-1622)."""
+        for e in envNums:
+            v0, v1 = int(self.envVertexStart[e]), int(self.envVertexStart[e + 1])
+            self.vertex[v0:v1] = self.initialVertex[v0:v1]
+            self.predictedVertex[v0:v1] = 0.0
+            self.velocity[v0:v1] = 0.0
+            self.activeDragConstraint[v0:v1] = 0.0
+            self.laparoscopeBase[4 * e:4 * e + 4] = self.laparoscopeInitialBase[4 * e:4 * e + 4]
+            self.laparoscopeTip[4 * e:4 * e + 4] = self.laparoscopeInitialTip[4 * e:4 * e + 4]
+            self.laparoscopeDragCutHeat[3 * e:3 * e + 3] = 0
+            self.laparoscopeDragCutHeatUpdate[3 * e:3 * e + 3] = 0
+        self.transformSimMeshData()
+
+    def resetStochasticModel(self, *args, **kwargs):
+        """Restore every env (modelDO.py:1624-1645); the instrument returns to its initial pose."""
+        self.vertex.copy_(self.initialVertex)
+        self.laparoscopeBase.copy_(self.laparoscopeInitialBase)
+        self.laparoscopeTip.copy_(self.laparoscopeInitialTip)
+        self.laparoscopeDragCutHeat.zero_()
+        self.laparoscopeDragCutHeatUpdate.zero_()
+        self.transformSimMeshData()
+
+    def envSlice(self, e: int) -> slice:
+        return slice(int(self.envVertexStart[e]), int(self.envVertexStart[e + 1]))

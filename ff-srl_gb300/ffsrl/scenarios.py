@@ -1,0 +1,139 @@
+"""Synthetic workloads: the instrument stand-in and model builders for the benchmark
+configurations (beam, liver-like ellipsoid, mixed-size pools).  Units: cm, g, s.
+
+The reference drives its instrument (a dVRK laparoscope, 7 transforms per env,
+``FF_SRL/FF_SRL/modelDO.py:26-416``) from USD; here each env's instrument is three
+capsules plus a drag point around an effector point that the caller moves (a seeded
+random walk in the benchmarks).  Entry layout per env, as the reference's
+``laparoscopeBase/Tip/Radius`` arrays: 0 = rod, 1 = left clamp, 2 = right clamp (its tip
+is the point ``dragConstraintsDO`` pulls grasped vertices to), 3 = drag point (the point
+``updateClampsDragKernel`` measures from).
+"""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import _lib as L
+from . import meshgen as mg
+from .model import SimModelDO
+
+KPA = 1.0e4  # 1 kPa in barye (g / (cm s^2))
+NH_E, NH_NU = 3.0 * KPA, 0.45
+
+
+def lame(E: float, nu: float) -> tuple[float, float]:
+    mu = E / (2.0 * (1.0 + nu))
+    lam = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu))
+    return mu, lam
+
+
+def instrument_arrays(points, up=(0.0, 1.0, 0.0), radii=(0.3, 0.1, 0.1), rod=12.0, clamp=1.2):
+    """base/tip [4N,3] and radius [4N] of instruments whose effector sits at ``points``."""
+    p = np.asarray(points, dtype=np.float64).reshape(-1, 3)
+    u = np.asarray(up, dtype=np.float64)
+    u = u / np.linalg.norm(u)
+    side = np.cross(u, [0.0, 0.0, 1.0])
+    if np.linalg.norm(side) < 1e-6:
+        side = np.cross(u, [1.0, 0.0, 0.0])
+    side = side / np.linalg.norm(side) * 0.2
+    N = len(p)
+    base = np.zeros((N, 4, 3))
+    tip = np.zeros((N, 4, 3))
+    base[:, 0], tip[:, 0] = p + u * (clamp + rod), p + u * clamp
+    base[:, 1], tip[:, 1] = p + u * clamp - side, p - side
+    base[:, 2], tip[:, 2] = p + u * clamp + side, p
+    base[:, 3], tip[:, 3] = p, p
+    rad = np.tile(np.array([radii[0], radii[1], radii[2], 0.0]), N)
+    return base.reshape(-1, 3).astype(np.float32), tip.reshape(-1, 3).astype(np.float32), rad.astype(np.float32)
+
+
+def top_surface_point(mesh) -> np.ndarray:
+    """The highest surface vertex of a mesh (the default grasp site)."""
+    surf = mesh["point_to_vertex"][:, 1]
+    v = mesh["vertex"][surf]
+    return v[np.argmax(v[:, 1])].astype(np.float64)
+
+
+def place_instruments(model: SimModelDO, meshes: list, dip: float = 0.1) -> np.ndarray:
+    """Effector of env e just below mesh e's highest surface point; returns the points."""
+    pts = np.stack([top_surface_point(m) - np.array([0.0, dip, 0.0]) for m in meshes])
+    b, t, r = instrument_arrays(pts)
+    model.setTool(b, t, r)
+    model.toolHost = {"base": b, "tip": t, "radius": r}
+    model.setEffectorInitialPosition()
+    return pts
+
+
+def beam_model(device, num_envs=1, neo=False, xpbd=False, **kw) -> tuple[SimModelDO, list]:
+    """Config 0: 10x4x4 beam of 1 cm cubes, 275 vertices, 800 tets, x=0 face fixed,
+    1 g/cm^3, dt 1/60, 8 substeps x 10 iterations.  Plain form: the reference DO step with
+    kS = 1; the compliant form (xpbd=True) runs XPBD distance (alpha 1e-6) and volume
+    (alpha 0)."""
+    mesh = mg.beam()
+    flags = L.REFERENCE_STEP
+    if xpbd:
+        flags = (flags & ~(L.DISTANCE | L.VOLUME)) | L.DISTANCE_XPBD | L.VOLUME_XPBD
+    kw.setdefault("environmentGravity", mg.gravity_force(mesh))
+    m = SimModelDO(mesh, num_envs, device, simSubsteps=8, simFrameRate=60, simConstraintsSteps=10,
+                   environmentGroundLevel=-100.0, constraints=flags, distanceCompliance=1e-6,
+                   volumeComplianceXPBD=0.0, **kw)
+    return m, [mesh] * num_envs
+
+
+def liver_model(device, num_envs, meshes=None, E=NH_E, nu=NH_NU, substeps=8, iterations=10, grasp=True,
+                collide=True, **kw) -> tuple[SimModelDO, list]:
+    """Config 1 (meshes=None: the 12/8/6 cm ellipsoid in every env) or a given list
+    of meshes (configs 2/4): Neo-Hookean + volume + distance, grasp and contact."""
+    if meshes is None:
+        meshes = [mg.ellipsoid()] * num_envs
+    mu, lam = lame(E, nu)
+    flags = L.VOLUME | L.DISTANCE | L.NEOHOOKEAN | L.DRAG | (L.COLLIDE if collide else 0)
+    kw.setdefault("environmentGravity", mg.gravity_force(meshes[0]))
+    m = SimModelDO(meshes, num_envs, device, simSubsteps=substeps, simFrameRate=60, simConstraintsSteps=iterations,
+                   environmentGroundLevel=-100.0, constraints=flags, globalVolumeCompliance=1.0 / lam,
+                   globalDeviatoricCompliance=1.0 / mu, globalLaparoscopeDragLookupRadius=0.3, **kw)
+    place_instruments(m, meshes)
+    return m, meshes
+
+
+def mixed_meshes(num_envs: int, pool_size: int = 64, seed: int = 0, t_lo: int = 500, t_hi: int = 20000):
+    """Config 2 pool: ``pool_size`` ellipsoids with tet targets log-uniform in [t_lo, t_hi],
+    each env drawing one (seeded)."""
+    pool = mg.mixed_pool(pool_size, seed=seed, t_lo=t_lo, t_hi=t_hi)
+    rng = np.random.Generator(np.random.PCG64(seed + 17))
+    pick = rng.integers(0, pool_size, size=num_envs)
+    return [pool[k] for k in pick], pool
+
+
+def random_walk_steps(num_envs: int, num_steps: int, step: float = 0.05, seed: int = 0) -> np.ndarray:
+    """[num_steps, N, 3] effector displacements of length ``step`` in seeded random directions."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    d = rng.normal(size=(num_steps, num_envs, 3))
+    d /= np.linalg.norm(d, axis=2, keepdims=True)
+    return (d * step).astype(np.float32)
+
+
+def env_cameras(meshes, seed: int = 0, distance: float | None = None):
+    """Per-env pinhole poses looking at each mesh's centre from a seeded direction, at
+    ``distance`` (default: 2.5 times the mesh's bounding radius)."""
+    from .render import look_at_rotation
+    rng = np.random.Generator(np.random.PCG64(seed))
+    pos, rot = [], []
+    for m in meshes:
+        c = m["vertex"].mean(axis=0).astype(np.float64)
+        dist = distance if distance is not None else 2.5 * float(np.linalg.norm(m["vertex"] - c, axis=1).max())
+        az = rng.uniform(0, 2 * math.pi)
+        el = rng.uniform(0.3, 1.0)
+        d = np.array([math.cos(el) * math.sin(az), math.sin(el), math.cos(el) * math.cos(az)])
+        p = c + d * dist
+        pos.append(p)
+        rot.append(look_at_rotation(p, c))
+    return np.asarray(pos, dtype=np.float32), np.asarray(rot, dtype=np.float32)
+
+
+def fov_aperture(fov_deg: float = 60.0) -> float:
+    """vertical aperture giving the reference camera (focal 50) a vertical field of view."""
+    return 2.0 * 50.0 * math.tan(math.radians(fov_deg) / 2.0)

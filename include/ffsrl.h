@@ -1,0 +1,252 @@
+/*
+ * ffsrl.h -- C ABI of libffsrl_cuda.so, the GB300 (sm_103a) implementation of FF-SRL's
+ * multi-environment soft-tissue step, BVH refit and ray-cast renderer.
+ *
+ * Every entry point takes plain pointers and sizes.  Device arrays are owned by the
+ * caller (the Python layer hands it torch tensors' data_ptr()).  Streams are passed as
+ * `void*` holding a cudaStream_t (NULL = legacy default stream).  Calls return an
+ * ffsrl_status; ffsrl_last_error() gives a message for the calling thread's last error.
+ *
+ * Array layouts follow the reference's SimModelDO (FF_SRL/FF_SRL/modelDO.py:1141-1246):
+ * every array is the concatenation over environments, vec3 arrays are float32 AoS
+ * (x,y,z per element), index arrays are int32 holding GLOBAL indices.
+ */
+#ifndef FFSRL_H
+#define FFSRL_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FFSRL_ABI_VERSION 1
+
+typedef enum {
+    FFSRL_OK = 0,
+    FFSRL_ERR_INVALID_ARGUMENT = 1,
+    FFSRL_ERR_CUDA = 2,
+    FFSRL_ERR_OUT_OF_MEMORY = 3,
+    FFSRL_ERR_BUDGET = 4,          /* serving: admission would exceed the HBM budget */
+    FFSRL_ERR_TIMEOUT = 5,         /* a bounded wait gave up */
+    FFSRL_ERR_UNSUPPORTED = 6,
+    FFSRL_ERR_NONFINITE = 7,       /* NaN/Inf detected in an environment's state */
+    FFSRL_ERR_STACK_OVERFLOW = 8,  /* BVH traversal stack exhausted */
+    FFSRL_ERR_BUSY = 9,            /* serving: no free slot */
+    FFSRL_ERR_NOT_FOUND = 10
+} ffsrl_status;
+
+/* ---- constraint selection (ffsrl_params.flags) --------------------------------- */
+#define FFSRL_VOLUME         (1u << 0) /* volumeConstraints      integrator.py:444-504 */
+#define FFSRL_DISTANCE       (1u << 1) /* distanceConstraints    integrator.py:65-109  */
+#define FFSRL_NEOHOOKEAN     (1u << 2) /* neoHookeanConstraints  integrator.py:578-698 */
+#define FFSRL_DISTANCE_XPBD  (1u << 3) /* distanceConstraintsXPBD integrator.py:191-240 */
+#define FFSRL_VOLUME_XPBD    (1u << 4) /* volumeConstraintsXPBD  integrator.py:507-576 */
+#define FFSRL_DRAG           (1u << 5) /* dragConstraintsDO      integrator.py:412-442 */
+#define FFSRL_CONNECTORS     (1u << 6) /* triToPointDistanceConstraintsDO integrator.py:300-353 */
+#define FFSRL_COLLIDE        (1u << 7) /* collideLaparoscopeDO   integrator.py:981-1050 */
+/* the launch sequence of SimIntegratorDO.stepModel (integrator.py:1640-1741) */
+#define FFSRL_REFERENCE_STEP (FFSRL_VOLUME | FFSRL_DISTANCE | FFSRL_DRAG | FFSRL_CONNECTORS | FFSRL_COLLIDE)
+
+/* ---- model: the arrays of SimModelDO (modelDO.py:1141-1246) -------------------- */
+typedef struct {
+    int32_t num_vertices, num_tetrahedrons, num_edges, num_triangles, num_connectors, num_envs;
+
+    float* vertex;              /* [3V] */
+    float* predicted_vertex;    /* [3V] */
+    float* velocity;            /* [3V] */
+    float* dp;                  /* [3V] correction accumulator (reference: SimModelDO.dP) */
+    int32_t* constraints_number;/* [V]  (reference: SimModelDO.constraintsNumber) */
+    float* collision_dp;        /* [3V] collision response accumulator (see collide) */
+    const float* inverse_mass;  /* [V] */
+
+    const int32_t* tetrahedron;            /* [4T] */
+    const float* tetrahedron_rest_volume;  /* [T]  |V0| */
+    const float* active_tetrahedron;       /* [T] */
+    const float* tetrahedron_dm_inv;       /* [9T] row-major Dm^-1 (Neo-Hookean) */
+    float* tetrahedron_lambda;             /* [T]  XPBD volume multipliers */
+    const float* xpbd_rest_volume;         /* [T]  signed rest volume (XPBD volume) */
+
+    const int32_t* edge;                   /* [2E] */
+    const float* edge_rest_length;         /* [E] */
+    const float* active_edge;              /* [E] */
+    float* edge_lambda;                    /* [E]  XPBD distance multipliers */
+
+    const int32_t* triangle;               /* [3F] surface triangles (vertex ids) */
+    const int32_t* tri_to_env;             /* [F] */
+    const int32_t* hole;                   /* [F] */
+    const int32_t* vertex_to_env;          /* [V] */
+    const float* active_drag_constraint;   /* [V] */
+
+    /* instrument, 4 entries per env: 0..2 capsules (rod, left clamp, right clamp),
+       3 = drag point (modelDO.py:218-245) */
+    const float* laparoscope_base;         /* [3*4N] */
+    const float* laparoscope_tip;          /* [3*4N] */
+    const float* laparoscope_radius;       /* [4N] */
+    int32_t* laparoscope_in_collision;     /* [N] */
+
+    const int32_t* connector_triangle_id;  /* [3C] */
+    const float* connector_tri_bar;        /* [3C] */
+    const int32_t* connector_vertex_id;    /* [C] */
+    const float* connector_rest_dist;      /* [C] */
+
+    /* per-env ranges, [N+1] prefix arrays (optional for the reference-shaped step) */
+    const int32_t* env_vertex_start;
+    const int32_t* env_tet_start;
+    const int32_t* env_edge_start;
+    const int32_t* env_tri_start;
+} ffsrl_model;
+
+/* ---- solver parameters (SimModelDO.__init__ kwargs, modelDO.py:774-802) -------- */
+typedef struct {
+    int32_t substeps;            /* simSubsteps */
+    int32_t iterations;          /* simConstraints */
+    uint32_t flags;              /* FFSRL_* selection */
+    float dt;                    /* simDt = 1/fps/substeps, as float32 */
+    float gravity[3];
+    float velocity_dampening;
+    float ground_level;
+    float ks_distance, ks_volume, ks_contact, ks_drag;
+    float volume_compliance, deviatoric_compliance;   /* Neo-Hookean (1/lambda, 1/mu) */
+    float distance_compliance, volume_compliance_xpbd;/* XPBD alpha; alpha/dt^2 is formed in double */
+    float connector_mass_weight_ratio, connector_ks, connector_rest_length_mul;
+} ffsrl_params;
+
+/* ---- BVH (bvh.py:144-518), per-env AABBs over shared or per-env topologies ------ */
+typedef struct {
+    int32_t num_envs;
+    int32_t num_topologies;
+    const int32_t* env_topology;     /* [N] topology used by env e */
+    const int32_t* env_node_offset;  /* [N] first AABB slot of env e */
+    const int32_t* env_face_offset;  /* [N] global vis-face id of env e's local face 0 */
+    const int32_t* topo_node_offset; /* [M+1] node range of each topology */
+    const int32_t* topo_tri_offset;  /* [M+1] tri-map range of each topology */
+    const int32_t* topo_max_level;   /* [M] */
+    const int32_t* left_node;        /* [nodes] -1 = leaf; children leftNode, leftNode+1 (topology-local) */
+    const int32_t* first_tri_id;     /* [nodes] into the topology's tri map */
+    const int32_t* tri_count;        /* [nodes] */
+    const int32_t* level;            /* [nodes] */
+    const int32_t* tri_id;           /* [tris] local face ids (triMap) */
+    float* aabb_min;                 /* [3 * total_env_nodes] */
+    float* aabb_max;                 /* [3 * total_env_nodes] */
+    int32_t total_env_nodes;
+    int32_t total_topology_nodes;
+    int32_t max_level;               /* max over topologies */
+    /* optional, for the fused refit: each topology's node ids grouped by level, deepest
+       level first; group g of topology m is level_node[level_start[topo_level_offset[m] + g]
+       .. level_start[topo_level_offset[m] + g + 1]) holding level topo_max_level[m] - g */
+    const int32_t* level_node;       /* [total_topology_nodes] topology-local node ids */
+    const int32_t* level_start;      /* [sum_m (topo_max_level[m] + 2)] absolute offsets */
+    const int32_t* topo_level_offset;/* [M+1] */
+} ffsrl_bvh;
+
+/* ---- ray-cast renderer (render.py:826-1196) ------------------------------------ */
+typedef struct {
+    int32_t num_envs;
+    int32_t resolution;              /* R: output is R x R per env */
+    int32_t num_vis_points;
+    int32_t num_vis_faces;
+    const float* vis_point;          /* [3P] allVisPoint */
+    const int32_t* vis_face;         /* [3Fv] global point ids */
+    const float* vis_point_color;    /* [3P] */
+    float* normal_sum;               /* [3P] scratch */
+    float* vertex_normal;            /* [3P] */
+    const int32_t* point_face_start; /* [P+1] point -> incident faces, ascending face id */
+    const int32_t* point_face;
+    int32_t num_cameras;             /* 1 (shared, as the reference) or num_envs */
+    const float* camera_pos;         /* [3C] */
+    const float* camera_rot;         /* [4C] quaternion x,y,z,w */
+    float camera_tan;                /* vertical_aperture / (2 * 50) */
+    float camera_aspect;
+    int32_t num_lights;
+    const float* light_dir;          /* [3L] */
+    const float* light_intensity;    /* [L] */
+    float* color;                    /* [N*R*R*3] vertex-colour Lambert (mode 3) */
+    float* depth;                    /* [N*R*R]   t/50 (mode 4, one channel) */
+    float* rays;                     /* [N*(2R)^2*3] per-ray scratch, reference-shaped path only */
+    float* ray_depth;                /* [N*(2R)^2]   per-ray scratch, reference-shaped path only */
+    int32_t* error_flag;             /* [1] set to FFSRL_ERR_STACK_OVERFLOW by an overflowing ray */
+} ffsrl_render;
+
+/* ---- library ---------------------------------------------------------------- */
+int32_t ffsrl_abi_version(void);
+const char* ffsrl_last_error(void);
+/* bytes of dynamic shared memory the device allows per block (0 without a GPU) */
+int32_t ffsrl_device_info(int32_t* sm_count, int32_t* max_smem_per_block, int32_t* cc_major, int32_t* cc_minor);
+
+/* One SimIntegratorDO.stepModel (integrator.py:1640-1741): substeps x (gravity,
+   iterations x (constraints, applyConstraints, drag, connectors, collide), bounds,
+   PBDStep), one kernel launch per reference kernel, float atomics as the reference. */
+int32_t ffsrl_step_model(const ffsrl_model* model, const ffsrl_params* params, void* stream);
+
+/* remapAToBKernel (utils.py:32-42): dst[map[2i]] = src[map[2i+1]] for i < count */
+int32_t ffsrl_remap(float* dst, const float* src, const int32_t* map, int32_t count, void* stream);
+
+/* updateClampsDragKernel (modelDO.py:247-279): for every vertex of an env whose drag
+   update flag is set, drag = (state==1 && |x - tip[4e+3]| < radius) ? 1 : 0 */
+int32_t ffsrl_update_clamps_drag(const float* positions, const int32_t* vertex_to_env, const float* laparoscope_tip,
+                                 float* drag, float lookup_radius, const int32_t* state, const int32_t* update,
+                                 int32_t num_vertices, void* stream);
+/* forceClampsDragKernel (modelDO.py:281-289): drag[env_id[i]*verts_per_env + vertex_id] = on */
+int32_t ffsrl_force_clamps_drag(float* drag, int32_t vertex_id, const int32_t* env_id, int32_t num, float on,
+                                int32_t verts_per_env, void* stream);
+/* Grasp the nearest vertex of each env's candidate list (surface vertices) within
+   `radius` of tip[4e+3]: drag=1 for it when clamp[e] != 0, every candidate of the env
+   set to 0 when clamp[e] == 0.  cand_start is an [N+1] prefix array. */
+int32_t ffsrl_grasp_nearest(const float* positions, const int32_t* cand_start, const int32_t* cand,
+                            const float* laparoscope_tip, const int32_t* clamp, float radius, float* drag,
+                            int32_t num_envs, void* stream);
+/* Rigidly translate each env's instrument (4 bases + 4 tips) by disp[3e..3e+2]. */
+int32_t ffsrl_move_tool(float* laparoscope_base, float* laparoscope_tip, const float* disp, int32_t num_envs,
+                        void* stream);
+
+/* ---- BVH ---------------------------------------------------------------------- */
+/* Host build for one mesh: binned SAH (bvh.py:281-518).  Output capacity 2*F nodes;
+   returns the node count in *num_nodes and the deepest level in *max_level.
+   aabb_min/max receive the build-time float bounds. */
+int32_t ffsrl_bvh_build_host(const float* points, const int32_t* faces, int32_t num_points, int32_t num_faces,
+                             int32_t bins, int32_t* left_node, int32_t* first_tri_id, int32_t* tri_count,
+                             int32_t* level, int32_t* tri_id, float* aabb_min, float* aabb_max,
+                             int32_t* num_nodes, int32_t* max_level);
+/* refitBVHLoop (bvh.py:419-440): one launch of refitBVHLevel per level, deepest first. */
+int32_t ffsrl_bvh_refit_levels(const ffsrl_bvh* bvh, const float* vis_point, const int32_t* vis_face, void* stream);
+/* Same result in one launch: one block per env walks its tree bottom-up. */
+int32_t ffsrl_bvh_refit_fused(const ffsrl_bvh* bvh, const float* vis_point, const int32_t* vis_face, void* stream);
+
+/* ---- renderer ------------------------------------------------------------------- */
+/* renderFunctionNew (render.py:975-1022): zero, vertex_normal_sum (atomics), normalize,
+   drawSimBVHKernelManyEnvs over (2R)^2 rays per env, downsample_kernel. */
+int32_t ffsrl_render_reference(const ffsrl_render* r, const ffsrl_bvh* bvh, void* stream);
+/* Same images: normals by CSR gather in face order, one thread per output pixel
+   tracing its 2x2 rays with a register stack, downsample fused. */
+int32_t ffsrl_render_fused(const ffsrl_render* r, const ffsrl_bvh* bvh, void* stream);
+
+/* ---- batched step ------------------------------------------------------------------ */
+typedef struct ffsrl_batch ffsrl_batch;
+typedef struct {
+    int32_t block_threads;   /* 0 = autotuned */
+    int32_t use_clusters;    /* reserved */
+    int32_t deterministic;   /* 1 = fixed-point accumulation (default) */
+    int32_t reserved[5];
+} ffsrl_batch_options;
+
+/* Build the env-resident batch plan from HOST copies of the model arrays (host_model
+   pointers are host memory; sizes and env ranges must be set).  device_model holds the
+   device pointers of the same arrays; the plan keeps those for state (vertex, velocity,
+   predicted_vertex, drag, instrument) and uploads its own packed constraint tables. */
+int32_t ffsrl_batch_create(const ffsrl_model* host_model, const ffsrl_model* device_model,
+                           const ffsrl_params* params, const ffsrl_batch_options* opts, ffsrl_batch** out);
+int32_t ffsrl_batch_destroy(ffsrl_batch* b);
+/* n_steps full steps of every env; same semantics as n_steps ffsrl_step_model calls. */
+int32_t ffsrl_batch_step(ffsrl_batch* b, int32_t n_steps, void* stream);
+/* Step only the listed envs (device array of env ids, count n). */
+int32_t ffsrl_batch_step_envs(ffsrl_batch* b, const int32_t* env_ids, int32_t n, int32_t n_steps, void* stream);
+/* bytes of device memory the plan holds; per-env shared-memory class */
+int32_t ffsrl_batch_info(const ffsrl_batch* b, int64_t* device_bytes, int32_t* num_classes, int32_t* block_threads);
+/* per-env status after a step: 0 ok, FFSRL_ERR_NONFINITE if the env's state went non-finite */
+int32_t ffsrl_batch_env_status(const ffsrl_batch* b, int32_t* host_status, int32_t num_envs);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FFSRL_H */

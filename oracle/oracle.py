@@ -1,0 +1,184 @@
+"""TEST INFRASTRUCTURE ONLY: Python harness of the CPU oracle (ffsrl_oracle.cpp).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this module,
+as the checker or the timed CPU baseline.  It restates the reference's kernels
+(FF_SRL/FF_SRL/integrator.py, bvh.py, render.py, utils.py) serially in launch and
+thread order.  Parity is unpinned: the reference (warp-lang 0.10.1, pxr) cannot run
+here and ships no golden vectors; the restatement is pinned by analytic known-answer
+tests (tests/test_oracle_kat.py) instead.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "ffsrl_oracle.cpp"
+SO = HERE / "_build" / "libffsrl_oracle.so"
+ROOT = HERE.parent
+sys.path.insert(0, str(ROOT / "ff-srl_gb300"))
+from ffsrl import _lib as L  # noqa: E402  (struct layouts of include/ffsrl.h)
+
+
+def build(force: bool = False) -> Path:
+    SO.parent.mkdir(parents=True, exist_ok=True)
+    hdr = ROOT / "include" / "ffsrl.h"
+    if force or not SO.exists() or SO.stat().st_mtime < max(SRC.stat().st_mtime, hdr.stat().st_mtime):
+        cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp",
+               "-ffp-contract=off", "-fno-fast-math", "-o", str(SO), str(SRC)]
+        subprocess.run(cmd, check=True)
+    return SO
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(str(SO))
+        P = C.c_void_p
+        _lib.oracle_step_f32.argtypes = [C.POINTER(L.Model), C.POINTER(L.Params), C.c_int, C.c_int]
+        _lib.oracle_step_f64.argtypes = [C.POINTER(L.Model), C.POINTER(L.Params), C.c_int, C.c_int, P, P, P]
+        _lib.oracle_remap.argtypes = [P, P, P, C.c_int32]
+        _lib.oracle_refit.argtypes = [C.POINTER(L.Bvh), P, P]
+        _lib.oracle_render.argtypes = [C.POINTER(L.Render), C.POINTER(L.Bvh), C.c_int]
+        for f in ("oracle_step_f32", "oracle_step_f64", "oracle_render"):
+            getattr(_lib, f).restype = C.c_int
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+class OracleSim:
+    """Host copy of a SimModelDO's arrays stepped by the oracle."""
+
+    def __init__(self, model, state=None):
+        h = model.host
+        V = model.numVertices
+        self.model = model
+        self.params = model.params()
+        src = state or {}
+        self.a = {
+            "vertex": np.array(src.get("vertex", h["vertex"]), dtype=np.float32).reshape(-1, 3).copy(),
+            "predicted_vertex": np.array(src.get("predicted_vertex", np.zeros((V, 3))), dtype=np.float32).reshape(-1, 3).copy(),
+            "velocity": np.array(src.get("velocity", np.zeros((V, 3))), dtype=np.float32).reshape(-1, 3).copy(),
+            "dp": np.zeros((V, 3), dtype=np.float32),
+            "constraints_number": np.zeros(V, dtype=np.int32),
+            "inverse_mass": h["inverseMass"],
+            "tetrahedron": h["tetrahedron"],
+            "tetrahedron_rest_volume": h["tetrahedronRestVolume"],
+            "active_tetrahedron": np.array(src.get("active_tetrahedron", np.ones(model.numTetrahedrons)), dtype=np.float32),
+            "tetrahedron_dm_inv": h["tetrahedronDmInv"],
+            "tetrahedron_lambda": np.zeros(max(model.numTetrahedrons, 1), dtype=np.float32),
+            "xpbd_rest_volume": h["tetrahedronRestVolumeSigned"],
+            "edge": h["edge"], "edge_rest_length": h["edgeRestLength"],
+            "active_edge": np.array(src.get("active_edge", np.ones(model.numEdges)), dtype=np.float32),
+            "edge_lambda": np.zeros(max(model.numEdges, 1), dtype=np.float32),
+            "triangle": h["triangle"], "tri_to_env": h["triToEnv"],
+            "hole": np.array(src.get("hole", np.zeros(model.numTriangles)), dtype=np.int32),
+            "vertex_to_env": h["vertexToEnv"],
+            "active_drag_constraint": np.array(src.get("active_drag_constraint", np.zeros(V)), dtype=np.float32),
+            "laparoscope_base": np.array(src.get("laparoscope_base", model.toolHost["base"]), dtype=np.float32).copy(),
+            "laparoscope_tip": np.array(src.get("laparoscope_tip", model.toolHost["tip"]), dtype=np.float32).copy(),
+            "laparoscope_radius": np.array(src.get("laparoscope_radius", model.toolHost["radius"]), dtype=np.float32).copy(),
+            "laparoscope_in_collision": np.zeros(model.numEnvs, dtype=np.int32),
+            "env_vertex_start": model.envVertexStart, "env_tet_start": model.envTetStart,
+            "env_edge_start": model.envEdgeStart, "env_tri_start": model.envTriStart,
+        }
+        self.a = {k: np.ascontiguousarray(v) for k, v in self.a.items()}
+        m = L.Model()
+        m.num_vertices, m.num_tetrahedrons, m.num_edges = V, model.numTetrahedrons, model.numEdges
+        m.num_triangles, m.num_connectors, m.num_envs = model.numTriangles, 0, model.numEnvs
+        for k, v in self.a.items():
+            setattr(m, k, _p(v))
+        self.desc = m
+
+    def step(self, n: int = 1, threads: int = 1) -> None:
+        rc = lib().oracle_step_f32(C.byref(self.desc), C.byref(self.params), int(n), int(threads))
+        if rc:
+            raise RuntimeError(f"oracle step failed: {rc}")
+
+    def step_f64(self, n: int, x64: np.ndarray, xp64: np.ndarray, v64: np.ndarray, threads: int = 1) -> None:
+        rc = lib().oracle_step_f64(C.byref(self.desc), C.byref(self.params), int(n), int(threads),
+                                   x64.ctypes.data, xp64.ctypes.data, v64.ctypes.data)
+        if rc:
+            raise RuntimeError(f"oracle f64 step failed: {rc}")
+
+    def vis_points(self) -> np.ndarray:
+        m = self.model
+        out = np.zeros((m.numVisPoints, 3), dtype=np.float32)
+        ptv = np.ascontiguousarray(m.host["pointToVertex"])
+        lib().oracle_remap(out.ctypes.data, self.a["vertex"].ctypes.data, ptv.ctypes.data, m.numVisPoints)
+        return out
+
+
+def bvh_desc(bvh, arrays: dict) -> L.Bvh:
+    """Host ffsrl_bvh over numpy copies of a SimBVH's arrays (filled into ``arrays``)."""
+    names = {"env_topology": bvh.envTopology, "env_node_offset": bvh.envNodeOffset,
+             "env_face_offset": bvh.envFaceOffset, "topo_node_offset": bvh.topoNodeOffset,
+             "topo_tri_offset": bvh.topoTriOffset, "topo_max_level": bvh.topoMaxLevel, "left_node": bvh.leftNode,
+             "first_tri_id": bvh.firstTriId, "tri_count": bvh.triCount, "level": bvh.level, "tri_id": bvh.triId,
+             "aabb_min": bvh.aabbMin, "aabb_max": bvh.aabbMax}
+    for k, t in names.items():
+        arrays[k] = np.ascontiguousarray(t.detach().cpu().numpy())
+    d = L.Bvh()
+    d.num_envs, d.num_topologies = bvh.desc.num_envs, bvh.desc.num_topologies
+    for k, v in arrays.items():
+        setattr(d, k, _p(v))
+    d.total_env_nodes, d.total_topology_nodes, d.max_level = (bvh.desc.total_env_nodes, bvh.desc.total_topology_nodes,
+                                                              bvh.desc.max_level)
+    return d
+
+
+def refit(bvh, vis_points: np.ndarray, vis_face: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    arrays = {}
+    d = bvh_desc(bvh, arrays)
+    vp = np.ascontiguousarray(vis_points, dtype=np.float32)
+    vf = np.ascontiguousarray(vis_face, dtype=np.int32)
+    lib().oracle_refit(C.byref(d), vp.ctypes.data, vf.ctypes.data)
+    return arrays["aabb_min"], arrays["aabb_max"]
+
+
+def render(renderer, bvh, vis_points: np.ndarray, aabb: tuple | None = None, stack_cap: int = 64):
+    """Oracle images (colour [N,R,R,3], depth [N,R,R]) for a WarpRaycastRendererDO's settings."""
+    m = renderer.simModel
+    arrays = {}
+    d = bvh_desc(bvh, arrays)
+    if aabb is not None:
+        arrays["aabb_min"][:] = aabb[0]
+        arrays["aabb_max"][:] = aabb[1]
+    N, R = renderer.numEnvs, renderer.width
+    a = {
+        "vis_point": np.ascontiguousarray(vis_points, dtype=np.float32),
+        "vis_face": np.ascontiguousarray(m.host["allVisFace"], dtype=np.int32),
+        "vis_point_color": np.ascontiguousarray(m.host["allVisPointColor"], dtype=np.float32),
+        "vertex_normal": np.zeros((m.numAllVisPoints, 3), dtype=np.float32),
+        "camera_pos": np.ascontiguousarray(renderer.cameraPosT.cpu().numpy()),
+        "camera_rot": np.ascontiguousarray(renderer.cameraRotT.cpu().numpy()),
+        "light_dir": np.ascontiguousarray(renderer.lightDir.cpu().numpy()),
+        "light_intensity": np.ascontiguousarray(renderer.lightIntensity.cpu().numpy()),
+        "color": np.zeros((N * R * R, 3), dtype=np.float32),
+        "depth": np.zeros(N * R * R, dtype=np.float32),
+    }
+    r = L.Render()
+    r.num_envs, r.resolution = N, R
+    r.num_vis_points, r.num_vis_faces = m.numAllVisPoints, m.numAllVisFaces
+    for k, v in a.items():
+        setattr(r, k, _p(v))
+    r.num_cameras = a["camera_pos"].shape[0]
+    r.camera_tan, r.camera_aspect = renderer.camera_tan, renderer.camera_aspect
+    r.num_lights = a["light_dir"].shape[0]
+    rc = lib().oracle_render(C.byref(r), C.byref(d), int(stack_cap))
+    if rc:
+        raise RuntimeError(f"oracle render failed: {rc}")
+    return a["color"].reshape(N, R, R, 3), a["depth"].reshape(N, R, R), a["vertex_normal"]

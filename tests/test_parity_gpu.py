@@ -1,0 +1,202 @@
+"""GPU parity: every CUDA path against the CPU oracle on the same seeded inputs.
+
+Tolerances: vertex positions within 1e-4 of the position scale (max |x|) after the
+stated number of steps; BVH boxes and fused-render images bit-exact; reference-shaped
+render (float atomics in its normal sum) within 1e-5 colour, depth bit-exact.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from ffsrl import SimBVH, SimIntegratorDO, WarpRaycastRendererDO, _lib as L, meshgen as mg, scenarios as sc
+
+pytestmark = pytest.mark.gpu
+POS_TOL = 1e-4
+
+
+def rel_err(a, b, what=""):
+    e = float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
+    print(f"[parity] {what} max|dx|/max|x| = {e:.3e}")
+    return e
+
+
+def oracle_for(model):
+    st = {"vertex": model.vertex.cpu().numpy(), "velocity": model.velocity.cpu().numpy(),
+          "laparoscope_base": model.laparoscopeBase.cpu().numpy(), "laparoscope_tip": model.laparoscopeTip.cpu().numpy(),
+          "laparoscope_radius": model.laparoscopeRadius.cpu().numpy(),
+          "active_drag_constraint": model.activeDragConstraint.cpu().numpy()}
+    return oracle.OracleSim(model, st)
+
+
+def run_pair(model, steps, batched):
+    o = oracle_for(model)
+    integ = SimIntegratorDO("cuda:0", batched=batched)
+    integ.stepModel(model, steps)
+    torch.cuda.synchronize()
+    o.step(steps)
+    return model.vertex.cpu().numpy(), o
+
+
+@pytest.mark.parametrize("batched", [False, True])
+def test_beam_config0_100_steps(gpu, oracle_lib, batched):
+    m, _ = sc.beam_model("cuda:0")
+    x, o = run_pair(m, 100, batched)
+    assert np.isfinite(x).all()
+    assert rel_err(x, o.a["vertex"], f"beam 100 steps batched={batched}") < POS_TOL
+    assert rel_err(m.velocity.cpu().numpy(), o.a["velocity"], "beam velocity") < 1e-2  # velocities are position differences / dt
+    # the beam moved: the check is not trivially satisfied
+    assert np.abs(o.a["vertex"] - m.initialVertex.cpu().numpy()).max() > 1e-3
+
+
+@pytest.mark.parametrize("batched", [False, True])
+def test_beam_xpbd_variant(gpu, oracle_lib, batched):
+    m, _ = sc.beam_model("cuda:0", xpbd=True)
+    x, o = run_pair(m, 100, batched)
+    assert rel_err(x, o.a["vertex"], f"beam xpbd 100 steps batched={batched}") < POS_TOL
+
+
+@pytest.mark.parametrize("batched", [False, True])
+def test_neohookean_grasp_contact(gpu, oracle_lib, batched):
+    mesh = mg.ellipsoid_for_tets(1500, seed=2)
+    m, meshes = sc.liver_model("cuda:0", 2, meshes=[mesh, mesh])
+    m.graspNearest(torch.ones(2, dtype=torch.int32, device="cuda:0"), radius=0.3)
+    torch.cuda.synchronize()
+    assert int((m.activeDragConstraint != 0).sum()) == 2
+    disp = torch.tensor([[0.05, 0.05, 0.0], [-0.05, 0.05, 0.0]], device="cuda:0")
+    o = oracle_for(m)
+    integ = SimIntegratorDO("cuda:0", batched=batched)
+    for k in range(10):
+        m.moveTool(disp)
+        o.a["laparoscope_base"] += disp.cpu().numpy().repeat(4, axis=0)
+        o.a["laparoscope_tip"] += disp.cpu().numpy().repeat(4, axis=0)
+        integ.stepModel(m, 1)
+        o.step(1)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(m.laparoscopeTip.cpu().numpy(), o.a["laparoscope_tip"], atol=1e-6)
+    assert rel_err(m.vertex.cpu().numpy(), o.a["vertex"], f"NH+grasp+contact batched={batched}") < POS_TOL
+    print("[parity] contacts", m.laparoscopeInCollision.cpu().numpy().tolist())
+    assert m.laparoscopeInCollision.cpu().numpy().tolist() == o.a["laparoscope_in_collision"].tolist()
+
+
+def test_mixed_pool_batched(gpu, oracle_lib):
+    pool = [mg.ellipsoid_for_tets(t, seed=i) for i, t in enumerate([300, 1200, 4000])]
+    meshes = [pool[i % 3] for i in range(7)]
+    m, _ = sc.liver_model("cuda:0", 7, meshes=meshes)
+    x, o = run_pair(m, 5, batched=True)
+    assert rel_err(x, o.a["vertex"], "mixed pool") < POS_TOL
+
+
+def test_batched_is_deterministic_and_independent_of_batch(gpu):
+    pool = [mg.ellipsoid_for_tets(t, seed=i) for i, t in enumerate([400, 2500])]
+    meshes = [pool[i % 2] for i in range(6)]
+    m1, _ = sc.liver_model("cuda:0", 6, meshes=meshes)
+    m2, _ = sc.liver_model("cuda:0", 6, meshes=meshes)
+    i1, i2 = SimIntegratorDO("cuda:0"), SimIntegratorDO("cuda:0")
+    i1.stepModel(m1, 3)
+    # m2: env 3 alone, then the rest, then env 3 again with the others
+    p2 = i2.plan(m2)
+    p2.step_envs([3], 2)
+    p2.step_envs([0, 1, 2, 4, 5], 3)
+    p2.step_envs([3], 1)
+    torch.cuda.synchronize()
+    assert torch.equal(m1.vertex, m2.vertex)
+    assert torch.equal(m1.velocity, m2.velocity)
+    assert (i1.envStatus(m1) == 0).all()
+
+
+def test_nonfinite_env_is_reported(gpu):
+    mesh = mg.ellipsoid_for_tets(600, seed=1)
+    m, _ = sc.liver_model("cuda:0", 3, meshes=[mesh] * 3)
+    sl = m.envSlice(1)
+    m.vertex[sl.start + 5, 0] = float("nan")
+    integ = SimIntegratorDO("cuda:0")
+    integ.stepModel(m, 1)
+    st = integ.envStatus(m)
+    assert st.tolist() == [0, L.ERR_NONFINITE, 0]
+    assert torch.isfinite(m.vertex[m.envSlice(0)]).all()
+
+
+def _render_setup(n_env=3, R=24, per_env_cameras=True):
+    mesh = mg.ellipsoid_for_tets(2000, seed=7)
+    m, meshes = sc.liver_model("cuda:0", n_env, meshes=[mesh] * n_env)
+    bvh = SimBVH("cuda:0", m)
+    r = WarpRaycastRendererDO("cuda:0", m, resolution=R, mode="headless", verticalAperture=sc.fov_aperture(60.0),
+                              horizontalAperture=sc.fov_aperture(60.0), lightPos=(0.3, 1.0, 0.5), lightIntensity=0.8)
+    if per_env_cameras:
+        pos, rot = sc.env_cameras(meshes, seed=3)
+        r.setCameras(pos, rot)
+    return m, bvh, r
+
+
+@pytest.mark.parametrize("fused", [False, True])
+def test_refit_bit_exact(gpu, oracle_lib, fused):
+    m, bvh, _ = _render_setup()
+    SimIntegratorDO("cuda:0").stepModel(m, 3)
+    bvh.refitBVH(fused=fused)
+    torch.cuda.synchronize()
+    lo, hi = oracle.refit(bvh, m.allVisPoint.cpu().numpy(), m.host["allVisFace"])
+    assert np.array_equal(bvh.aabbMin.cpu().numpy(), lo)
+    assert np.array_equal(bvh.aabbMax.cpu().numpy(), hi)
+
+
+@pytest.mark.parametrize("fused", [True, False])
+def test_render_vs_oracle(gpu, oracle_lib, fused):
+    m, bvh, r = _render_setup()
+    r.fused = fused
+    SimIntegratorDO("cuda:0").stepModel(m, 2)
+    bvh.refitBVH()
+    img = r.renderNew(bvh, m)
+    torch.cuda.synchronize()
+    r.checkErrors()
+    col, dep, _ = oracle.render(r, bvh, m.allVisPoint.cpu().numpy(),
+                                aabb=(bvh.aabbMin.cpu().numpy(), bvh.aabbMax.cpu().numpy()))
+    g_col, g_dep = img.cpu().numpy(), r.depthImages().cpu().numpy()
+    print(f"[parity] render fused={fused} hit fraction {(dep > 0).mean():.3f}")
+    assert (dep > 0).mean() > 0.05  # the mesh is in view
+    if fused:
+        assert np.array_equal(g_dep, dep)
+        assert np.array_equal(g_col, col)
+    else:
+        assert np.array_equal(g_dep, dep)
+        assert np.abs(g_col - col).max() < 1e-5
+
+
+def test_grasp_nearest_matches_numpy(gpu):
+    mesh = mg.ellipsoid_for_tets(1000, seed=3)
+    m, meshes = sc.liver_model("cuda:0", 4, meshes=[mesh] * 4)
+    clamp = torch.tensor([1, 0, 1, 1], dtype=torch.int32, device="cuda:0")
+    tip = m.laparoscopeTip.cpu().numpy().reshape(4, 4, 3)[:, 3]
+    tip[3] += 100.0  # env 3: nothing within reach
+    t = m.laparoscopeTip.cpu().numpy()
+    t[4 * 3 + 3] = tip[3]
+    m.laparoscopeTip.copy_(torch.as_tensor(t))
+    m.graspNearest(clamp, radius=0.3)
+    got = m.activeDragConstraint.cpu().numpy()
+    x = m.vertex.cpu().numpy()
+    for e in range(4):
+        c0, c1 = m.graspCandStart[e], m.graspCandStart[e + 1]
+        cand = m.host["graspCand"][c0:c1]
+        d = np.linalg.norm(x[cand] - tip[e], axis=1)
+        want = np.zeros(m.numVertices, dtype=np.float32)
+        if clamp[e] and d.min() < 0.3:
+            want[cand[np.argmin(d)]] = 1.0
+        sl = m.envSlice(e)
+        np.testing.assert_array_equal(got[sl], want[sl])
+
+
+def test_plain_clamp_kernels(gpu):
+    mesh = mg.ellipsoid_for_tets(600, seed=1)
+    m, _ = sc.liver_model("cuda:0", 2, meshes=[mesh] * 2)
+    m.predictedVertex.copy_(m.vertex)
+    state = torch.tensor([1, 0, 0, 1, 0, 0], dtype=torch.int32, device="cuda:0")
+    update = torch.tensor([1, 0, 0, 0, 0, 0], dtype=torch.int32, device="cuda:0")
+    m.updateClampsDrag(state, update, lookupRadius=1.0)
+    x = m.vertex.cpu().numpy()
+    tip = m.laparoscopeTip.cpu().numpy()
+    d0 = np.linalg.norm(x[m.envSlice(0)] - tip[3], axis=1)
+    np.testing.assert_array_equal(m.activeDragConstraint.cpu().numpy()[m.envSlice(0)], (d0 < 1.0).astype(np.float32))
+    assert float(m.activeDragConstraint[m.envSlice(1)].abs().sum()) == 0.0
+    m.forceLaparoscopeClampVertex(7, torch.tensor([0, 1], device="cuda:0"), on=1.0)
+    assert float(m.activeDragConstraint[m.envVertexStart[1] + 7]) == 1.0
