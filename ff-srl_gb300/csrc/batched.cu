@@ -15,11 +15,17 @@
 // (dragConstraintsDO) and the instrument contact (collideLaparoscopeDO).
 //
 // Accumulation is deterministic: in float32 runs each correction component is rounded
-// once to a 64-bit fixed-point integer (scale 2^40, resolution 9.1e-13 m, range
-// +-8.4e6 m) and summed with integer atomics, which are associative, so the result does
-// not depend on thread order and an environment gives the same bits alone or in any
-// batch.  The float64 build of the same kernel (used for the precision report) sums in
-// double.
+// once to a 32-bit fixed-point integer and summed with native shared-memory integer
+// atomics, which are associative, so the sum does not depend on thread order and an
+// environment gives the same bits alone or in any batch.  The scale 2^k is chosen per
+// model so that one unit is about a quarter of a float ulp of the largest coordinate
+// (the position update itself rounds to an ulp); a contribution too large for the
+// per-vertex sum to stay in range flags the environment as diverged.  The number of contributions per vertex
+// is precomputed when the plan is built (a constraint only skips at run time on
+// degenerate geometry, which then decrements it), so no count atomics are needed.
+// Constraint records are ordered by a greedy vertex colouring within each environment so
+// that the 32 lanes of a warp update distinct vertices.  The float64 build of the same
+// kernel (used for the precision report) sums in double.
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <vector>
@@ -27,6 +33,7 @@
 #include <numeric>
 #include <cstring>
 #include <string>
+#include <cmath>
 #include "ffsrl_internal.h"
 
 namespace ffsrl {
@@ -57,15 +64,21 @@ template <class R> __device__ __forceinline__ R rmax(R a, R b) { return a > b ? 
 
 // per-precision storage: predicted position + inverse mass, accumulator word
 template <class R> struct Store;
+struct Fixed { float scale, inv, bound; };
+
 template <> struct Store<float> {
     typedef float4 P;
-    typedef unsigned long long A;
+    typedef unsigned int A;
     __device__ static t3<float> pos(const P& p) { return T3<float>(p.x, p.y, p.z); }
     __device__ static P make(t3<float> v, float w) { return make_float4(v.x, v.y, v.z, w); }
-    __device__ static void add(A* a, float v) {
-        atomicAdd(a, (unsigned long long)__float2ll_rn(v * 1099511627776.0f));
+    // false when the scaled value is outside the per-contribution bound (or not finite)
+    __device__ static bool add(A* a, float v, const Fixed& fx) {
+        float q = v * fx.scale;
+        if (!(fabsf(q) < fx.bound)) return false;
+        atomicAdd(a, (unsigned)__float2int_rn(q));
+        return true;
     }
-    __device__ static float get(A a) { return __ll2float_rn((long long)a) * 9.094947017729282e-13f; }
+    __device__ static float get(A a, const Fixed& fx) { return __int2float_rn((int)a) * fx.inv; }
 };
 struct __align__(32) dpos { double x, y, z, w; };
 template <> struct Store<double> {
@@ -73,19 +86,20 @@ template <> struct Store<double> {
     typedef double A;
     __device__ static t3<double> pos(const P& p) { return T3<double>(p.x, p.y, p.z); }
     __device__ static P make(t3<double> v, double w) { P r; r.x = v.x; r.y = v.y; r.z = v.z; r.w = w; return r; }
-    __device__ static void add(A* a, double v) { atomicAdd(a, v); }
-    __device__ static double get(A a) { return a; }
+    __device__ static bool add(A* a, double v, const Fixed&) { atomicAdd(a, v); return isfinite(v); }
+    __device__ static double get(A a, const Fixed&) { return a; }
 };
 
 struct EnvRec { int v0, nv, t0, nt, e0, ne, f0, nf; };
 
-// adds a correction vector to vertex i's accumulator; a non-finite component (which
-// the fixed-point form cannot carry) raises `bad` so the env is reported non-finite
-template <class R> __device__ __forceinline__ void add3(typename Store<R>::A* acc, int i, t3<R> d, bool& bad) {
-    Store<R>::add(acc + 3 * i, d.x);
-    Store<R>::add(acc + 3 * i + 1, d.y);
-    Store<R>::add(acc + 3 * i + 2, d.z);
-    bad |= !(isfinite(d.x) && isfinite(d.y) && isfinite(d.z));
+// adds a correction vector to vertex i's accumulator; a component the fixed-point form
+// cannot carry (non-finite or out of range) raises `bad` so the env is reported diverged
+template <class R> __device__ __forceinline__ void add3(typename Store<R>::A* acc, int i, t3<R> d, bool& bad,
+                                                        const Fixed& fx) {
+    bool ok = Store<R>::add(acc + 3 * i, d.x, fx);
+    ok &= Store<R>::add(acc + 3 * i + 1, d.y, fx);
+    ok &= Store<R>::add(acc + 3 * i + 2, d.z, fx);
+    bad |= !ok;
 }
 
 template <class R> struct Dev {
@@ -105,6 +119,10 @@ template <class R> struct Dev {
     int* in_collision;
     float* tet_lambda; float* edge_lambda;
     int* env_status;
+    const int* cnt0;           // per-vertex static contribution count (global vertex index)
+    const int* tet_orig;       // model tet id of each (colour-ordered) record, for XPBD lambdas
+    const int* edge_orig;      // model edge id of each record
+    Fixed fx;
     unsigned flags;
     int substeps, iterations;
     float dt, gx, gy, gz, damping, ground;
@@ -211,12 +229,14 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
     __shared__ int s_bad;
     __shared__ int s_any_contact;
     __shared__ int s_any_drag;
+    __shared__ int s_dyn_it;  // iteration in which a constraint skipped on degenerate geometry
     __shared__ ToolShared<R> tool;
 
     unsigned char* gbase = scratch + (long long)blockIdx.x * scratch_stride;
     const int tid = threadIdx.x;
     const R dt = R(D.dt);
     const unsigned fl = D.flags;
+    const Fixed fx = D.fx;
 
     for (;;) {
         if (tid == 0) s_work = atomicAdd(counter, 1);
@@ -248,7 +268,7 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
             cnt = reinterpret_cast<int*>(gbase + (sizeof(P) + 3 * sizeof(A)) * (size_t)max_nv);
         }
 
-        if (tid == 0) { s_incol = 0; s_bad = 0; s_any_drag = 0; }
+        if (tid == 0) { s_incol = 0; s_bad = 0; s_any_drag = 0; s_dyn_it = -1; }
         bool bad = false;
         if (tid < 3) {
             long long k = 4ll * env + tid;
@@ -266,7 +286,7 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
         }
         for (int i = tid; i < nv; i += BLOCK) {
             acc[3 * i] = A(0); acc[3 * i + 1] = A(0); acc[3 * i + 2] = A(0);
-            cnt[i] = 0;
+            cnt[i] = __ldg(D.cnt0 + E.v0 + i);
         }
         // grasp mask of this env, one bit per vertex
         if (fl & FFSRL_DRAG) {
@@ -317,8 +337,10 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                             const R mA = PA.w, mB = PB.w, mC = PC.w, mD = PD.w;
                             const t3<R> p1 = pb - pa, p2 = pc - pa, p3 = pd - pa;
                             t3<R> dA = T3<R>(0, 0, 0), dB = dA, dC = dA, dD = dA;
-                            int k = 0;
+                            int k = 0;     // constraints that contributed
+                            int skip = 0;  // statically counted constraints that skipped on degenerate geometry
                             const float2 va = __ldg(D.tet_va + gt);
+                            const bool anym = mA != R(0) || mB != R(0) || mC != R(0) || mD != R(0);
                             if (fl & (FFSRL_VOLUME | FFSRL_VOLUME_XPBD)) {
                                 // volumeConstraints (integrator.py:444-504) / XPBD (:507-576)
                                 const R active = R(va.y);
@@ -326,7 +348,9 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                                     t3<R> q2 = cross(p3, p1), q1 = cross(p2, p3), q3 = cross(p1, p2);
                                     t3<R> q0 = -q1 - q2 - q3;
                                     R w = mA * dot(q0, q0) + mB * dot(q1, q1) + mC * dot(q2, q2) + mD * dot(q3, q3);
-                                    if (!(fabs(w) < R(BEPS))) {
+                                    if (fabs(w) < R(BEPS)) {
+                                        if (anym) skip += ((fl & FFSRL_VOLUME) ? 1 : 0) + ((fl & FFSRL_VOLUME_XPBD) ? 1 : 0);
+                                    } else {
                                         R s6 = dot(cross(p1, p2), p3);
                                         if (fl & FFSRL_VOLUME) {
                                             R C = R(va.x) - fabs(s6) / R(6);
@@ -336,10 +360,11 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                                         }
                                         if (fl & FFSRL_VOLUME_XPBD) {
                                             R alpha = R(D.a_vol);
-                                            R lam = R(D.tet_lambda[gt]);
+                                            const int ot = __ldg(D.tet_orig + gt);
+                                            R lam = R(D.tet_lambda[ot]);
                                             R C = s6 / R(6) - R(__ldg(D.tet_vs + gt));
                                             R dl = -(C + alpha * lam) / (w + alpha);
-                                            D.tet_lambda[gt] = float(lam + dl);
+                                            D.tet_lambda[ot] = float(lam + dl);
                                             dA = dA + q0 * dl * mA; dB = dB + q1 * dl * mB;
                                             dC = dC + q2 * dl * mC; dD = dD + q3 * dl * mD;
                                             ++k;
@@ -370,7 +395,9 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                                 l = length(g1); w += l * l * mB;
                                 l = length(g2); w += l * l * mC;
                                 l = length(g3); w += l * l * mD;
-                                if (!(w < R(BEPS))) {
+                                if (w < R(BEPS)) {
+                                    if (anym) ++skip;
+                                } else {
                                     R alpha = R(D.vol_c) / dt / dt / rv;
                                     R dl = -C / (w + alpha);
                                     t3<R> hA = g0 * dl * mA, hB = g1 * dl * mB, hC = g2 * dl * mC, hD = g3 * dl * mD;
@@ -386,7 +413,9 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                                     l = length(g1); w += l * l * mB;
                                     l = length(g2); w += l * l * mC;
                                     l = length(g3); w += l * l * mD;
-                                    if (!(w < R(BEPS))) {
+                                    if (w < R(BEPS)) {
+                                        if (anym) ++skip;
+                                    } else {
                                         alpha = R(D.dev_c) / dt / dt / rv;
                                         dl = -rs / (w + alpha);
                                         hA = hA + g0 * dl * mA; hB = hB + g1 * dl * mB;
@@ -397,9 +426,13 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                                 }
                             }
                             if (k) {
-                                add3<R>(acc, ia, dA, bad); add3<R>(acc, ib, dB, bad);
-                                add3<R>(acc, ic, dC, bad); add3<R>(acc, id, dD, bad);
-                                atomicAdd(cnt + ia, k); atomicAdd(cnt + ib, k); atomicAdd(cnt + ic, k); atomicAdd(cnt + id, k);
+                                add3<R>(acc, ia, dA, bad, fx); add3<R>(acc, ib, dB, bad, fx);
+                                add3<R>(acc, ic, dC, bad, fx); add3<R>(acc, id, dD, bad, fx);
+                            }
+                            if (skip) {
+                                atomicSub(cnt + ia, skip); atomicSub(cnt + ib, skip);
+                                atomicSub(cnt + ic, skip); atomicSub(cnt + id, skip);
+                                s_dyn_it = it;
                             }
                         }
                     }
@@ -413,12 +446,17 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                             const R active = R(la.y), L0 = R(la.x);
                             if (active == R(0) || L0 < R(BEPS)) continue;
                             const P PA = xp[ia], PB = xp[ib];
-                            t3<R> dir = S::pos(PB) - S::pos(PA);
-                            R len = length(dir);
-                            if (len < R(BEPS)) continue;
                             R mA = PA.w, mB = PB.w;
                             R w = mA + mB;
-                            if (w < R(BEPS)) continue;
+                            if (w < R(BEPS)) continue;  // never counted
+                            t3<R> dir = S::pos(PB) - S::pos(PA);
+                            R len = length(dir);
+                            if (len < R(BEPS)) {
+                                const int skip = ((fl & FFSRL_DISTANCE) ? 1 : 0) + ((fl & FFSRL_DISTANCE_XPBD) ? 1 : 0);
+                                atomicSub(cnt + ia, skip); atomicSub(cnt + ib, skip);
+                                s_dyn_it = it;
+                                continue;
+                            }
                             R C = len - L0;
                             t3<R> dA = T3<R>(0, 0, 0), dB = dA;
                             int k = 0;
@@ -429,29 +467,31 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                             }
                             if (fl & FFSRL_DISTANCE_XPBD) {
                                 R alpha = R(D.a_dist);
-                                R lam = R(D.edge_lambda[ge]);
+                                const int oe = __ldg(D.edge_orig + ge);
+                                R lam = R(D.edge_lambda[oe]);
                                 R dl = -(C + alpha * lam) / (w + alpha);
-                                D.edge_lambda[ge] = float(lam + dl);
+                                D.edge_lambda[oe] = float(lam + dl);
                                 t3<R> d = dl * normalize(dir);
                                 dA = dA - d * mA; dB = dB + d * mB;
                                 ++k;
                             }
-                            add3<R>(acc, ia, dA, bad); add3<R>(acc, ib, dB, bad);
-                            atomicAdd(cnt + ia, k); atomicAdd(cnt + ib, k);
+                            add3<R>(acc, ia, dA, bad, fx); add3<R>(acc, ib, dB, bad, fx);
                         }
                     }
                     __syncthreads();
                     // ---- applyConstraints + dragConstraintsDO ----
+                    const bool restore = s_dyn_it == it;
                     for (int i = tid; i < nv; i += BLOCK) {
                         int c = cnt[i];
                         P q = xp[i];
                         t3<R> x = S::pos(q);
                         if (c > 0) {
                             R N = R(c);
-                            x = x + T3<R>(S::get(acc[3 * i]) / N, S::get(acc[3 * i + 1]) / N, S::get(acc[3 * i + 2]) / N);
+                            x = x + T3<R>(S::get(acc[3 * i], fx) / N, S::get(acc[3 * i + 1], fx) / N,
+                                          S::get(acc[3 * i + 2], fx) / N);
                             acc[3 * i] = A(0); acc[3 * i + 1] = A(0); acc[3 * i + 2] = A(0);
-                            cnt[i] = 0;
                         }
+                        if (restore) cnt[i] = __ldg(D.cnt0 + E.v0 + i);
                         if ((fl & FFSRL_DRAG) && s_any_drag && ((dbits[i >> 5] >> (i & 31)) & 1u)) {
                             R dr = R(__ldg(D.drag + E.v0 + i));
                             t3<R> dir = x - tool.drag_tip;
@@ -495,15 +535,15 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                             if (tl > R(0)) atomicAdd(&s_incol, 1);
                             if (!(tl > R(0)) && !isnan(tl)) continue;  // every response is zero
                             s_any_contact = 1;
-                            if (PA.w > R(0)) add3<R>(acc, a, tA, bad);
-                            if (PB.w > R(0)) add3<R>(acc, b, tB, bad);
-                            if (PC.w > R(0)) add3<R>(acc, c, tC, bad);
+                            if (PA.w > R(0)) add3<R>(acc, a, tA, bad, fx);
+                            if (PB.w > R(0)) add3<R>(acc, b, tB, bad, fx);
+                            if (PC.w > R(0)) add3<R>(acc, c, tC, bad, fx);
                         }
                         __syncthreads();
                         if (s_any_contact) {
                             for (int i = tid; i < nv; i += BLOCK) {
                                 P q = xp[i];
-                                t3<R> d = T3<R>(S::get(acc[3 * i]), S::get(acc[3 * i + 1]), S::get(acc[3 * i + 2]));
+                                t3<R> d = T3<R>(S::get(acc[3 * i], fx), S::get(acc[3 * i + 1], fx), S::get(acc[3 * i + 2], fx));
                                 xp[i] = S::make(S::pos(q) - d, q.w);
                                 acc[3 * i] = A(0); acc[3 * i + 1] = A(0); acc[3 * i + 2] = A(0);
                             }
@@ -587,6 +627,10 @@ struct ffsrl_batch {
     int* d_work = nullptr; int* d_counters = nullptr; int* d_status = nullptr;
     unsigned char* d_scratch = nullptr;
     double* d_state64 = nullptr;  // x, v, xp in double for precision 64
+    int* d_cnt0 = nullptr;        // static per-vertex contribution counts
+    int* d_tet_orig = nullptr;    // record -> model tet id
+    int* d_edge_orig = nullptr;   // record -> model edge id
+    Fixed fx{1.0f, 1.0f, 1.0f};
     int64_t device_bytes = 0;
     // classes
     struct Class {
@@ -626,7 +670,8 @@ void free_batch(ffsrl_batch* b) {
     cudaFree(b->d_env); cudaFree(b->d_tet_idx); cudaFree(b->d_tet_va); cudaFree(b->d_dmA); cudaFree(b->d_dmB);
     cudaFree(b->d_dmC); cudaFree(b->d_tet_vs); cudaFree(b->d_edge_idx); cudaFree(b->d_edge_la); cudaFree(b->d_tri_idx);
     cudaFree(b->d_work); cudaFree(b->d_counters); cudaFree(b->d_status); cudaFree(b->d_scratch);
-    cudaFree(b->d_state64); cudaFree(b->d_work_sub);
+    cudaFree(b->d_state64); cudaFree(b->d_work_sub); cudaFree(b->d_cnt0); cudaFree(b->d_tet_orig);
+    cudaFree(b->d_edge_orig);
     if (b->h_work_pinned) cudaFreeHost(b->h_work_pinned);
     for (auto& c : b->classes) {
         if (c.stream) cudaStreamDestroy(c.stream);
@@ -659,6 +704,7 @@ Dev<float> make_dev_f(ffsrl_batch* b) {
     D.in_collision = b->dm.laparoscope_in_collision;
     D.tet_lambda = b->dm.tetrahedron_lambda; D.edge_lambda = b->dm.edge_lambda;
     D.env_status = b->d_status;
+    D.cnt0 = b->d_cnt0; D.tet_orig = b->d_tet_orig; D.edge_orig = b->d_edge_orig; D.fx = b->fx;
     D.flags = p.flags; D.substeps = p.substeps; D.iterations = p.iterations;
     D.dt = p.dt; D.gx = p.gravity[0]; D.gy = p.gravity[1]; D.gz = p.gravity[2];
     D.damping = p.velocity_dampening; D.ground = p.ground_level;
@@ -696,6 +742,7 @@ template <> int32_t launch_class<double>(ffsrl_batch* b, const ffsrl_batch::Clas
     D.inv_mass = F.inv_mass; D.drag = F.drag; D.lap_base = F.lap_base; D.lap_tip = F.lap_tip;
     D.lap_radius = F.lap_radius; D.in_collision = F.in_collision; D.tet_lambda = F.tet_lambda;
     D.edge_lambda = F.edge_lambda; D.env_status = F.env_status; D.flags = F.flags; D.substeps = F.substeps;
+    D.cnt0 = F.cnt0; D.tet_orig = F.tet_orig; D.edge_orig = F.edge_orig; D.fx = F.fx;
     D.iterations = F.iterations; D.dt = F.dt; D.gx = F.gx; D.gy = F.gy; D.gz = F.gz; D.damping = F.damping;
     D.ground = F.ground; D.ks_distance = F.ks_distance; D.ks_volume = F.ks_volume; D.ks_contact = F.ks_contact;
     D.ks_drag = F.ks_drag; D.vol_c = F.vol_c; D.dev_c = F.dev_c; D.a_dist = F.a_dist; D.a_vol = F.a_vol;
@@ -838,6 +885,89 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
         }
     }
 
+    // ---- static contribution counts (the runtime skips only on degenerate geometry) ----
+    const float feps = (float)BEPS;
+    std::vector<int> cnt0(V, 0), tri_deg(V, 0);
+    const uint32_t fl = p->flags;
+    for (int64_t t = 0; t < T; ++t) {
+        const int32_t* q = hm->tetrahedron + 4 * t;
+        bool anym = false;
+        for (int k = 0; k < 4; ++k) anym |= hm->inverse_mass[q[k]] != 0.0f;
+        if (!anym) continue;
+        bool act = tet_va[t].y == 1.0f;
+        int k = ((fl & FFSRL_VOLUME) && act ? 1 : 0) + ((fl & FFSRL_VOLUME_XPBD) && act ? 1 : 0) +
+                ((fl & FFSRL_NEOHOOKEAN) ? 1 : 0);
+        for (int j = 0; j < 4; ++j) cnt0[q[j]] += k;
+    }
+    for (int64_t e = 0; e < E; ++e) {
+        const int32_t* q = hm->edge + 2 * e;
+        float w = hm->inverse_mass[q[0]] + hm->inverse_mass[q[1]];
+        if (edge_la[e].y == 0.0f || edge_la[e].x < feps || w < feps) continue;
+        int k = ((fl & FFSRL_DISTANCE) ? 1 : 0) + ((fl & FFSRL_DISTANCE_XPBD) ? 1 : 0);
+        cnt0[q[0]] += k; cnt0[q[1]] += k;
+    }
+    for (int64_t f = 0; f < F; ++f)
+        for (int k = 0; k < 3; ++k) tri_deg[hm->triangle[3 * f + k]] += 1;
+    int max_terms = 1;
+    for (int64_t v = 0; v < V; ++v) max_terms = std::max(max_terms, cnt0[v] + tri_deg[v]);
+
+    // ---- fixed-point scale: one unit ~ a quarter float ulp of the largest coordinate ----
+    {
+        double mx = 1e-30;
+        for (int64_t i = 0; i < 3 * V; ++i) mx = std::max(mx, (double)std::fabs(hm->vertex[i]));
+        int e2 = 0;
+        std::frexp(mx, &e2);  // mx < 2^e2
+        int k = 26 - e2;
+        b->fx.scale = std::ldexp(1.0f, k);
+        b->fx.inv = std::ldexp(1.0f, -k);
+        // each term below 2^31 / (terms + 1): the per-vertex sum cannot leave int32
+        b->fx.bound = std::ldexp(1.0f, 31) / (float)(max_terms + 1);
+    }
+
+    // ---- order each env's constraint records by a greedy vertex colouring ----
+    std::vector<int> tet_orig(T), edge_orig(E);
+    {
+        std::vector<uint64_t> used;
+        std::vector<int> col;
+        for (int e = 0; e < N; ++e) {
+            const EnvRec& r = env[e];
+            used.assign(r.nv, 0);
+            col.resize(std::max(r.nt, r.ne));
+            for (int t = 0; t < r.nt; ++t) {
+                uint2 ix = tet_idx[r.t0 + t];
+                int l[4] = {(int)(ix.x & 0xffff), (int)(ix.x >> 16), (int)(ix.y & 0xffff), (int)(ix.y >> 16)};
+                uint64_t m = used[l[0]] | used[l[1]] | used[l[2]] | used[l[3]];
+                int c = (~m) ? __builtin_ctzll(~m) : 63;
+                col[t] = c;
+                for (int k = 0; k < 4; ++k) used[l[k]] |= 1ull << c;
+            }
+            std::vector<int> ord(r.nt);
+            std::iota(ord.begin(), ord.end(), 0);
+            std::stable_sort(ord.begin(), ord.end(), [&](int a, int c2) { return col[a] < col[c2]; });
+            for (int j = 0; j < r.nt; ++j) tet_orig[r.t0 + j] = r.t0 + ord[j];
+            used.assign(r.nv, 0);
+            for (int k = 0; k < r.ne; ++k) {
+                unsigned ix = edge_idx[r.e0 + k];
+                int a = ix & 0xffff, c2 = ix >> 16;
+                uint64_t m = used[a] | used[c2];
+                int c = (~m) ? __builtin_ctzll(~m) : 63;
+                col[k] = c;
+                used[a] |= 1ull << c; used[c2] |= 1ull << c;
+            }
+            ord.resize(r.ne);
+            std::iota(ord.begin(), ord.end(), 0);
+            std::stable_sort(ord.begin(), ord.end(), [&](int a, int c2) { return col[a] < col[c2]; });
+            for (int j = 0; j < r.ne; ++j) edge_orig[r.e0 + j] = r.e0 + ord[j];
+        }
+        auto permute = [](auto& v, const std::vector<int>& orig) {
+            if (v.empty()) return;
+            auto c = v;
+            for (size_t i = 0; i < orig.size(); ++i) v[i] = c[orig[i]];
+        };
+        permute(tet_idx, tet_orig); permute(tet_va, tet_orig); permute(dmA, tet_orig); permute(dmB, tet_orig);
+        permute(dmC, tet_orig); permute(tet_vs, tet_orig); permute(edge_idx, edge_orig); permute(edge_la, edge_orig);
+    }
+
     // size classes: mode by fit, then by vertex-count band
     const int bands[] = {192, 384, 768, 1536, 3072, 65536};
     b->env_class.assign(N, -1);
@@ -908,7 +1038,10 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
     }
 
     int32_t st = FFSRL_OK;
-    if ((st = dalloc(b, &b->d_env, N)) || (st = upload(b->d_env, env)) ||
+    if ((st = dalloc(b, &b->d_cnt0, (size_t)V)) || (st = upload(b->d_cnt0, cnt0)) ||
+        (st = dalloc(b, &b->d_tet_orig, (size_t)T)) || (st = upload(b->d_tet_orig, tet_orig)) ||
+        (st = dalloc(b, &b->d_edge_orig, (size_t)E)) || (st = upload(b->d_edge_orig, edge_orig)) ||
+        (st = dalloc(b, &b->d_env, N)) || (st = upload(b->d_env, env)) ||
         (st = dalloc(b, &b->d_tet_idx, T)) || (st = upload(b->d_tet_idx, tet_idx)) ||
         (st = dalloc(b, &b->d_tet_va, T)) || (st = upload(b->d_tet_va, tet_va)) ||
         (st = dalloc(b, &b->d_dmA, dmA.size())) || (st = upload(b->d_dmA, dmA)) ||
