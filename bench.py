@@ -198,7 +198,7 @@ def main():
     envs = args.envs
     m, meshes, bvh, r = build_workload(device, envs, seed=rank)
     from ffsrl import SimIntegratorDO, scenarios as sc, _lib as L
-    integ = SimIntegratorDO(device)
+    integ = SimIntegratorDO(device, autotune=True)
     plan = integ.plan(m)
     n_cls = plan.info()["num_classes"]
     K, W = args.steps, max(args.warmup, 3)
@@ -330,7 +330,7 @@ def main():
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                              "kernel": "k_batched (batched step, all size classes)", "kernel_ms": step_kernel_ms},
-                "cpu_baseline": cpu, "plain": plain, "gpu_launches": launches,
+                "cpu_baseline": cpu, "plain": plain, "gpu_launches": launches, "autotune": integ.tuning,
                 "clocks": clk.summary(), "env_status_nonzero": int((status != 0).sum())}
         print(json.dumps(line))
     if world > 1:

@@ -237,6 +237,11 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
     const R dt = R(D.dt);
     const unsigned fl = D.flags;
     const Fixed fx = D.fx;
+    // Neo-Hookean constants, hoisted with the reference's association order:
+    // C offset invDev/invVol, and compliance/dT/dT (the per-tet /V0 stays per tet)
+    const R nh_off = (R(1) / R(D.dev_c)) / (R(1) / R(D.vol_c));
+    const R nh_uH = R(D.vol_c) / dt / dt;
+    const R nh_uD = R(D.dev_c) / dt / dt;
 
     for (;;) {
         if (tid == 0) s_work = atomicAdd(counter, 1);
@@ -388,8 +393,7 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                                 t3<R> g3 = c0 * d20 + c1 * d21 + c2 * d22;
                                 t3<R> g0 = -g1 - g2 - g3;
                                 R detF = dot(f0, c0);
-                                R invVol = R(1) / R(D.vol_c), invDev = R(1) / R(D.dev_c);
-                                R C = detF - R(1) - invDev / invVol;
+                                R C = detF - R(1) - nh_off;
                                 R w = R(0), l;
                                 l = length(g0); w += l * l * mA;
                                 l = length(g1); w += l * l * mB;
@@ -398,7 +402,7 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                                 if (w < R(BEPS)) {
                                     if (anym) ++skip;
                                 } else {
-                                    R alpha = R(D.vol_c) / dt / dt / rv;
+                                    R alpha = nh_uH / rv;
                                     R dl = -C / (w + alpha);
                                     t3<R> hA = g0 * dl * mA, hB = g1 * dl * mB, hC = g2 * dl * mC, hD = g3 * dl * mD;
                                     R l0 = length(f0), l1 = length(f1), l2 = length(f2);
@@ -416,7 +420,7 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                                     if (w < R(BEPS)) {
                                         if (anym) ++skip;
                                     } else {
-                                        alpha = R(D.dev_c) / dt / dt / rv;
+                                        alpha = nh_uD / rv;
                                         dl = -rs / (w + alpha);
                                         hA = hA + g0 * dl * mA; hB = hB + g1 * dl * mB;
                                         hC = hC + g2 * dl * mC; hD = hD + g3 * dl * mD;
@@ -632,9 +636,10 @@ struct ffsrl_batch {
     int* d_edge_orig = nullptr;   // record -> model edge id
     Fixed fx{1.0f, 1.0f, 1.0f};
     int64_t device_bytes = 0;
+    size_t dyn_budget = 0;
     // classes
     struct Class {
-        int mode, block, max_nv, grid;
+        int mode, block, max_nv, grid, members;
         size_t smem, scratch_stride, scratch_offset;
         int work_offset, work_count;
         cudaStream_t stream;
@@ -773,6 +778,30 @@ int32_t run(ffsrl_batch* b, const std::vector<int>& counts, const int* d_work_ba
     return FFSRL_OK;
 }
 
+// Block size of a class: the instantiation, its shared-memory allowance and the grid
+// from the runtime's occupancy calculator.
+int32_t configure_class(ffsrl_batch* b, ffsrl_batch::Class& c, int block, size_t dyn_budget) {
+    if (b->precision == 64) block = 256;
+    if (c.mode == 1 && block < 256) block = 256;
+    if (c.mode == 2 && block > 512) block = 512;
+    const void* kfn = b->precision == 64 ? (const void*)pick_d(block, c.mode) : (const void*)pick_f(block, c.mode);
+    if (!kfn) return fail(FFSRL_ERR_UNSUPPORTED, "ffsrl_batch: no kernel for block " + std::to_string(block) +
+                                                     " in mode " + std::to_string(c.mode));
+    if (c.smem > 48 * 1024) {
+        // several classes may share one instantiation: allow the whole budget
+        cudaError_t ea = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_budget);
+        if (ea != cudaSuccess) return cuda_fail(ea, "ffsrl_batch: shared memory attribute");
+    }
+    int per_sm = 0;
+    cudaError_t eo = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, block, c.smem);
+    if (eo != cudaSuccess || per_sm <= 0)
+        return fail(FFSRL_ERR_UNSUPPORTED, "ffsrl_batch: class does not fit on an SM (block " + std::to_string(block) +
+                                               ", shared " + std::to_string(c.smem) + ")");
+    c.block = block;
+    c.grid = std::max(1, std::min({c.members, per_sm * b->sm_count, c.scratch_stride ? 8 * b->sm_count : INT32_MAX}));
+    return FFSRL_OK;
+}
+
 }  // namespace
 
 extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* dmod, const ffsrl_params* p,
@@ -811,6 +840,7 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
         }
     }
     const size_t dyn_budget = (size_t)b->max_smem > static_smem + 64 ? (size_t)b->max_smem - static_smem - 64 : 0;
+    b->dyn_budget = dyn_budget;
 
     const int64_t V = hm->num_vertices, T = hm->num_tetrahedrons, E = hm->num_edges, F = hm->num_triangles;
     std::vector<EnvRec> env(N);
@@ -1006,31 +1036,15 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
         c.mode = keys[oi] / 16;
         c.max_nv = 1;
         for (int e : mem) c.max_nv = std::max(c.max_nv, env[e].nv);
-        c.block = block_override > 0 ? block_override : default_block(c.max_nv, c.mode);
-        if (precision == 64) c.block = 256;
-        if (c.mode == 1 && c.block < 256) c.block = 256;
-        if (c.mode == 2 && c.block > 512) c.block = 512;
         c.smem = precision == 64 ? smem_bytes<double>(c.mode, c.max_nv) : smem_bytes<float>(c.mode, c.max_nv);
         c.scratch_stride = precision == 64 ? scratch_bytes<double>(c.mode, c.max_nv) : scratch_bytes<float>(c.mode, c.max_nv);
         c.scratch_stride = (c.scratch_stride + 255) & ~(size_t)255;
-        // resident blocks per SM, from the runtime's occupancy calculator
-        const void* kfn = precision == 64 ? (const void*)pick_d(c.block, c.mode) : (const void*)pick_f(c.block, c.mode);
-        if (!kfn) { free_batch(b); return fail(FFSRL_ERR_UNSUPPORTED, "ffsrl_batch_create: no kernel for block/mode"); }
-        if (c.smem > 48 * 1024) {
-            // several classes may share one instantiation: allow the device maximum
-            cudaError_t ea = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_budget);
-            if (ea != cudaSuccess) { free_batch(b); return cuda_fail(ea, "ffsrl_batch_create: shared memory attribute"); }
-        }
-        int per_sm = 0;
-        cudaError_t eo = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, c.block, c.smem);
-        if (eo != cudaSuccess || per_sm <= 0) {
-            free_batch(b);
-            return fail(FFSRL_ERR_UNSUPPORTED, "ffsrl_batch_create: class does not fit on an SM (block " +
-                                                   std::to_string(c.block) + ", shared " + std::to_string(c.smem) + ")");
-        }
-        c.grid = std::max(1, std::min((int)mem.size(), per_sm * b->sm_count));
+        c.members = (int)mem.size();
+        int want = block_override > 0 ? block_override : default_block(c.max_nv, c.mode);
+        if (int32_t st = configure_class(b, c, want, dyn_budget)) { free_batch(b); return st; }
+        // scratch for the largest grid any block size can give (8 resident blocks per SM)
         c.scratch_offset = scratch_total;
-        scratch_total += c.scratch_stride * (size_t)c.grid;
+        if (c.scratch_stride) scratch_total += c.scratch_stride * (size_t)std::min(c.members, 8 * b->sm_count);
         c.work_offset = (int)b->work_host.size();
         c.work_count = (int)mem.size();
         for (int e : mem) { b->env_class[e] = (int)b->classes.size(); b->work_host.push_back(e); }
@@ -1141,5 +1155,33 @@ extern "C" int32_t ffsrl_batch_env_status(const ffsrl_batch* b, int32_t* host_st
 extern "C" int32_t ffsrl_batch_state_f64(const ffsrl_batch* b, double* host_xvx) {
     if (!b || !host_xvx || b->precision != 64) return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_state_f64: not a float64 plan");
     FFSRL_CUDA_TRY(cudaMemcpy(host_xvx, b->d_state64, sizeof(double) * 9 * (size_t)b->dm.num_vertices, cudaMemcpyDeviceToHost));
+    return FFSRL_OK;
+}
+
+extern "C" int32_t ffsrl_batch_class_info(const ffsrl_batch* b, int32_t cls, int32_t* max_nv, int32_t* mode,
+                                          int32_t* block, int32_t* num_envs) {
+    if (!b || cls < 0 || cls >= (int)b->classes.size()) return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_class_info");
+    const auto& c = b->classes[cls];
+    if (max_nv) *max_nv = c.max_nv;
+    if (mode) *mode = c.mode;
+    if (block) *block = c.block;
+    if (num_envs) *num_envs = c.work_count;
+    return FFSRL_OK;
+}
+
+extern "C" int32_t ffsrl_batch_class_envs(const ffsrl_batch* b, int32_t cls, int32_t* env_ids) {
+    if (!b || !env_ids || cls < 0 || cls >= (int)b->classes.size())
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_class_envs");
+    const auto& c = b->classes[cls];
+    for (int i = 0; i < c.work_count; ++i) env_ids[i] = b->work_host[c.work_offset + i];
+    return FFSRL_OK;
+}
+
+extern "C" int32_t ffsrl_batch_set_class_block(ffsrl_batch* b, int32_t cls, int32_t block) {
+    if (!b || cls < 0 || cls >= (int)b->classes.size()) return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_set_class_block");
+    FFSRL_CUDA_TRY(cudaDeviceSynchronize());
+    ffsrl_batch::Class c = b->classes[cls];
+    if (int32_t st = configure_class(b, c, block, b->dyn_budget)) return st;
+    b->classes[cls] = c;
     return FFSRL_OK;
 }

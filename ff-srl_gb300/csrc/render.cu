@@ -133,6 +133,29 @@ __device__ __forceinline__ bool slab(v3 ro, v3 rd, v3 lo, v3 hi, float& tnear) {
     return (tmax >= 0.0f) && (tmax >= tmin);
 }
 
+// Node test of the traversal: intersectAABB's hit && tmin < tMin (render.py:452-454).
+// The slab distances are first formed with the ray's reciprocal direction; when every
+// part of the decision is farther from its threshold than the rounding of that form can
+// move it (8 float ulps of the largest distance), the decision equals the reference's.
+// Otherwise -- and for non-finite distances -- the reference's divisions decide.
+__device__ __forceinline__ bool node_hit(v3 ro, v3 rd, v3 inv, v3 lo, v3 hi, float tMin) {
+    float t1 = (lo.x - ro.x) * inv.x, t2 = (hi.x - ro.x) * inv.x;
+    float t3 = (lo.y - ro.y) * inv.y, t4 = (hi.y - ro.y) * inv.y;
+    float t5 = (lo.z - ro.z) * inv.z, t6 = (hi.z - ro.z) * inv.z;
+    float m = fmaxf(fmaxf(fmaxf(fabsf(t1), fabsf(t2)), fmaxf(fabsf(t3), fabsf(t4))), fmaxf(fabsf(t5), fabsf(t6)));
+    if (m < 3.0e37f) {
+        float tmin = fmax_ref(fmax_ref(fmin_ref(t1, t2), fmin_ref(t3, t4)), fmin_ref(t5, t6));
+        float tmax = fmin_ref(fmin_ref(fmax_ref(t1, t2), fmax_ref(t3, t4)), fmax_ref(t5, t6));
+        float g = m * 4.76837158e-7f;  // 8 * 2^-24 * m
+        // a certainly-false part decides a miss; all parts certainly true decide a hit
+        if (tmax < -g || tmax - tmin < -2.0f * g || tmin > tMin + g) return false;
+        if (tmax > g && tmax - tmin > 2.0f * g && tmin < tMin - g) return true;
+    }
+    float tn;
+    bool h = slab(ro, rd, lo, hi, tn);
+    return h && tn < tMin;
+}
+
 // MTTriRayIntersection (render.py:661-697)
 __device__ __forceinline__ float moller_trumbore(v3 a, v3 b, v3 c, v3 ro, v3 rd, v3& p) {
     v3 ab = b - a, ac = c - a;
@@ -181,15 +204,14 @@ __device__ int query(const EnvView& ev, const float* __restrict__ pts, const int
     float tMin = 1e6f;
     int hit_tri = -1;
     int visits = 0;
+    const v3 inv = mk(1.0f / rd.x, 1.0f / rd.y, 1.0f / rd.z);
     while (count) {
         int node = stack[--count];
         if (++visits > ev.nn) {  // a valid tree visits each node at most once
             atomicExch(err, FFSRL_ERR_STACK_OVERFLOW);
             return -1;
         }
-        float tn;
-        bool hit = slab(ro, rd, ld3(ev.amin, node), ld3(ev.amax, node), tn);
-        if (hit && tn < tMin) {
+        if (node_hit(ro, rd, inv, ld3(ev.amin, node), ld3(ev.amax, node), tMin)) {
             int left = ev.left[node];
             if (left == -1) {
                 int first = ev.first[node];
@@ -302,35 +324,48 @@ __global__ void k_downsample(ffsrl_render r) {
     if (r.depth) r.depth[tid] = d / nsq;
 }
 
-// One thread per output pixel: its 2x2 rays traced in the downsample order, averaged.
-// Blocks cover 8x8 pixel tiles of one env so neighbouring rays share BVH nodes in L1.
-__global__ void __launch_bounds__(64) k_pixel(ffsrl_render r, ffsrl_bvh b) {
+// One thread per ray; the four rays of a pixel sit in consecutive lanes and are summed
+// by shuffles in downsample_kernel's order ((r00 + r01) + r10) + r11, then divided by 4.
+// A block covers an 8x8 pixel tile of one env so neighbouring rays share BVH nodes in L1.
+__global__ void __launch_bounds__(256) k_rays(ffsrl_render r, ffsrl_bvh b) {
     const int R = r.resolution, W = 2 * R, H = 2 * R;
     const int tiles_x = (R + 7) / 8;
     const int tiles = tiles_x * ((R + 7) / 8);
-    int e = blockIdx.x / tiles;
-    int tile = blockIdx.x % tiles;
-    int px = (tile % tiles_x) * 8 + (threadIdx.x & 7);
-    int py = (tile / tiles_x) * 8 + (threadIdx.x >> 3);
-    if (e >= r.num_envs || px >= R || py >= R) return;
-    int cam = r.num_cameras > 1 ? e : 0;
-    v3 ro = ld3(r.camera_pos, cam);
-    float4 q = reinterpret_cast<const float4*>(r.camera_rot)[cam];
-    EnvView ev = env_view(b, e);
-    v3 c = mk(0.0f, 0.0f, 0.0f);
-    float d = 0.0f;
-    for (int i = 0; i < 2; ++i)
-        for (int j = 0; j < 2; ++j) {
-            int rx = 2 * px + j, ry = 2 * py + i;  // ray index (ry * W + rx) as in downsample_kernel
-            int et = ry * W + rx;
-            Shade s = trace(r, ev, ro, q, et % W, H - et / W, W, H);
-            c = mk(c.x + s.color.x, c.y + s.color.y, c.z + s.color.z);
-            d = d + s.depth;
-        }
-    float nsq = float(2 * 2);
-    long long o = (long long)e * R * R + (long long)py * R + px;
-    if (r.color) st3(r.color, o, mk(c.x / nsq, c.y / nsq, c.z / nsq));
-    if (r.depth) r.depth[o] = d / nsq;
+    const int e = blockIdx.x / tiles;
+    const int tile = blockIdx.x % tiles;
+    const int pix = threadIdx.x >> 2, q = threadIdx.x & 3;
+    const int px = (tile % tiles_x) * 8 + (pix & 7);
+    const int py = (tile / tiles_x) * 8 + (pix >> 3);
+    const bool valid = e < r.num_envs && px < R && py < R;
+    Shade s;
+    s.color = mk(0.0f, 0.0f, 0.0f);
+    s.depth = 0.0f;
+    if (valid) {
+        const int cam = r.num_cameras > 1 ? e : 0;
+        const v3 ro = ld3(r.camera_pos, cam);
+        const float4 qr = reinterpret_cast<const float4*>(r.camera_rot)[cam];
+        const EnvView ev = env_view(b, e);
+        const int et = (2 * py + (q >> 1)) * W + 2 * px + (q & 1);  // ray index as in downsample_kernel
+        s = trace(r, ev, ro, qr, et % W, H - et / W, W, H);
+    }
+    float cx = s.color.x, cy = s.color.y, cz = s.color.z, d = s.depth;
+    float ax[3], ay[3], az[3], ad[3];
+#pragma unroll
+    for (int k = 1; k <= 3; ++k) {
+        ax[k - 1] = __shfl_down_sync(0xffffffffu, cx, k);
+        ay[k - 1] = __shfl_down_sync(0xffffffffu, cy, k);
+        az[k - 1] = __shfl_down_sync(0xffffffffu, cz, k);
+        ad[k - 1] = __shfl_down_sync(0xffffffffu, d, k);
+    }
+    if (valid && q == 0) {
+        v3 c = mk(cx, cy, cz);
+        for (int k = 0; k < 3; ++k) c = mk(c.x + ax[k], c.y + ay[k], c.z + az[k]);
+        float dd = ((d + ad[0]) + ad[1]) + ad[2];
+        float nsq = float(2 * 2);
+        long long o = (long long)e * R * R + (long long)py * R + px;
+        if (r.color) st3(r.color, o, mk(c.x / nsq, c.y / nsq, c.z / nsq));
+        if (r.depth) r.depth[o] = dd / nsq;
+    }
 }
 
 int32_t check_bvh(const ffsrl_bvh* b) {
@@ -404,7 +439,7 @@ extern "C" int32_t ffsrl_render_fused(const ffsrl_render* r, const ffsrl_bvh* b,
     k_normal_gather<<<grid_for(P, 256), 256, 0, s>>>(r->vis_point, r->vis_face, r->point_face_start, r->point_face,
                                                      r->vertex_normal, P);
     const int tiles = ((r->resolution + 7) / 8) * ((r->resolution + 7) / 8);
-    k_pixel<<<(unsigned)((long long)tiles * r->num_envs), 64, 0, s>>>(*r, *b);
+    k_rays<<<(unsigned)((long long)tiles * r->num_envs), 256, 0, s>>>(*r, *b);
     FFSRL_LAUNCH_CHECK("ffsrl_render_fused");
     return FFSRL_OK;
 }

@@ -88,10 +88,12 @@ class BatchPlan:
 class SimIntegratorDO:
     """Reference-compatible integrator: ``SimIntegratorDO(device).stepModel(simModel)``."""
 
-    def __init__(self, device="cuda:0", batched: bool = True, blockThreads: int = 0) -> None:
+    def __init__(self, device="cuda:0", batched: bool = True, blockThreads: int = 0, autotune: bool = False) -> None:
         self.device = device
         self.batched = bool(batched)
         self.blockThreads = int(blockThreads)
+        self.autotune = bool(autotune)
+        self.tuning = None
         self._plans = {}
 
     def plan(self, simModel) -> BatchPlan:
@@ -100,6 +102,9 @@ class SimIntegratorDO:
         if p is None or p.model is not simModel:
             p = BatchPlan(simModel, self.blockThreads)
             self._plans[key] = p
+            if self.autotune and self.blockThreads == 0:
+                from .autotune import autotune
+                self.tuning = autotune(p)
         return p
 
     def stepModel(self, simModel, steps: int = 1, stream=None) -> None:

@@ -217,8 +217,8 @@ int32_t ffsrl_bvh_refit_fused(const ffsrl_bvh* bvh, const float* vis_point, cons
 /* renderFunctionNew (render.py:975-1022): zero, vertex_normal_sum (atomics), normalize,
    drawSimBVHKernelManyEnvs over (2R)^2 rays per env, downsample_kernel. */
 int32_t ffsrl_render_reference(const ffsrl_render* r, const ffsrl_bvh* bvh, void* stream);
-/* Same images: normals by CSR gather in face order, one thread per output pixel
-   tracing its 2x2 rays with a register stack, downsample fused. */
+/* Same images: normals by CSR gather in face order, one thread per ray with a register
+   stack, the 2x2 downsample fused through warp shuffles. */
 int32_t ffsrl_render_fused(const ffsrl_render* r, const ffsrl_bvh* bvh, void* stream);
 
 /* ---- batched step ------------------------------------------------------------------ */
@@ -243,6 +243,15 @@ int32_t ffsrl_batch_step(ffsrl_batch* b, int32_t n_steps, void* stream);
 int32_t ffsrl_batch_step_envs(ffsrl_batch* b, const int32_t* env_ids, int32_t n, int32_t n_steps, void* stream);
 /* bytes of device memory the plan holds; per-env shared-memory class */
 int32_t ffsrl_batch_info(const ffsrl_batch* b, int64_t* device_bytes, int32_t* num_classes, int32_t* block_threads);
+/* Size classes (environments grouped by vertex count, one launch each): the class's
+   largest vertex count, storage mode (0 shared, 1 shared positions + global sums,
+   2 global), block size and environment count; its env ids; its block size. */
+int32_t ffsrl_batch_class_info(const ffsrl_batch* b, int32_t cls, int32_t* max_nv, int32_t* mode, int32_t* block,
+                               int32_t* num_envs);
+int32_t ffsrl_batch_class_envs(const ffsrl_batch* b, int32_t cls, int32_t* env_ids);
+int32_t ffsrl_batch_set_class_block(ffsrl_batch* b, int32_t cls, int32_t block);
+/* Copies the float64 plan's state (x, v, predicted, each [3V]) to host memory. */
+int32_t ffsrl_batch_state_f64(const ffsrl_batch* b, double* host_xvx);
 /* per-env status after a step: 0 ok, FFSRL_ERR_NONFINITE if the env's state went non-finite */
 int32_t ffsrl_batch_env_status(const ffsrl_batch* b, int32_t* host_status, int32_t num_envs);
 
