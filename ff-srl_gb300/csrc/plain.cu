@@ -4,6 +4,8 @@
 // the drop-in that the batched form (batched.cu) is measured against.
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <mutex>
+#include <string>
 #include "ffsrl_internal.h"
 #include "vecmath.cuh"
 
@@ -534,4 +536,68 @@ extern "C" int32_t ffsrl_move_tool(float* laparoscope_base, float* laparoscope_t
                                                                                        laparoscope_tip, disp, num_envs);
     FFSRL_LAUNCH_CHECK("ffsrl_move_tool");
     return FFSRL_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// Step without allocation.  Some callers cannot call cudaMalloc: a host application
+// that has already reserved the device's memory for its own pool, or a control loop
+// that must never wait on the driver's allocator.  For them this entry point runs the
+// same step as ffsrl_step_model but keeps the three per-vertex accumulators that step
+// needs (correction sum, contribution count, contact response) in one array compiled
+// into the library, so the caller passes only the model's own inputs and outputs.
+//
+// Limits and rules:
+//  - at most kNoAllocMaxVertices vertices per call (1.75 MB of device memory, held by
+//    every GPU that loads the library until the process exits);
+//  - the array is shared by every call: the first 28 bytes per vertex are cleared at the
+//    start of each call, so nothing carries over between calls (ffsrl_step_model keeps
+//    connector corrections made after the last apply for the next call; with
+//    connectors, use ffsrl_step_model);
+//  - calls whose work overlaps on the GPU (different streams, or different threads
+//    without ordering) race on the array;
+//  - the first call on a device looks up the array's device address (once per device,
+//    with that device current); make that first call before any stream capture.
+namespace {
+constexpr int kNoAllocMaxVertices = 65536;
+constexpr size_t kNoAllocBytesPerVertex = 28;  // dp (12) + collision dp (12) + count (4)
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocMaxVertices * kNoAllocBytesPerVertex];
+constexpr int kMaxDevices = 256;
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[kMaxDevices] = {};
+}  // namespace
+
+extern "C" int32_t ffsrl_step_model_noalloc(const ffsrl_model* m, const ffsrl_params* p, void* stream) {
+    if (!m || !p) return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_step_model_noalloc: null model or params");
+    if (m->num_vertices < 0 || m->num_vertices > kNoAllocMaxVertices)
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_step_model_noalloc: " + std::to_string(m->num_vertices) +
+                                                    " vertices exceed the limit of " +
+                                                    std::to_string(kNoAllocMaxVertices));
+    int dev = 0;
+    FFSRL_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(FFSRL_ERR_UNSUPPORTED, "ffsrl_step_model_noalloc: device ordinal");
+    void* base = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {
+            cudaError_t e = cudaGetSymbolAddress(&g_noalloc_addr[dev], g_noalloc_scratch);
+            if (e != cudaSuccess) {
+                g_noalloc_addr[dev] = nullptr;
+                return cuda_fail(e, "ffsrl_step_model_noalloc: cudaGetSymbolAddress");
+            }
+        }
+        base = g_noalloc_addr[dev];
+    }
+    const size_t V = (size_t)m->num_vertices;
+    unsigned char* s = static_cast<unsigned char*>(base);
+    ffsrl_model mm = *m;
+    mm.dp = reinterpret_cast<float*>(s);
+    mm.collision_dp = reinterpret_cast<float*>(s + 12 * (size_t)kNoAllocMaxVertices);
+    mm.constraints_number = reinterpret_cast<int32_t*>(s + 24 * (size_t)kNoAllocMaxVertices);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (V > 0) {
+        FFSRL_CUDA_TRY(cudaMemsetAsync(mm.dp, 0, 12 * V, st));
+        FFSRL_CUDA_TRY(cudaMemsetAsync(mm.collision_dp, 0, 12 * V, st));
+        FFSRL_CUDA_TRY(cudaMemsetAsync(mm.constraints_number, 0, 4 * V, st));
+    }
+    return ffsrl_step_model(&mm, p, stream);
 }

@@ -119,6 +119,7 @@ def lib() -> C.CDLL:
         "ffsrl_last_error": ([], C.c_char_p),
         "ffsrl_device_info": ([C.POINTER(I32)] * 4, I32),
         "ffsrl_step_model": ([pm, pp, P], I32),
+        "ffsrl_step_model_noalloc": ([pm, pp, P], I32),
         "ffsrl_remap": ([P, P, P, I32, P], I32),
         "ffsrl_update_clamps_drag": ([P, P, P, P, F32, P, P, I32, P], I32),
         "ffsrl_force_clamps_drag": ([P, I32, P, I32, F32, I32, P], I32),

@@ -179,6 +179,18 @@ int32_t ffsrl_device_info(int32_t* sm_count, int32_t* max_smem_per_block, int32_
    PBDStep), one kernel launch per reference kernel, float atomics as the reference. */
 int32_t ffsrl_step_model(const ffsrl_model* model, const ffsrl_params* params, void* stream);
 
+/* No counterpart in the reference.  ffsrl_step_model for callers that cannot allocate
+   device memory (for example a host application that has reserved the device's memory
+   for its own pool, or a control loop that must never wait on the allocator): the
+   correction, count and contact accumulators come from one array compiled into the
+   library instead of model->dp / constraints_number / collision_dp, which are ignored.
+   At most 65536 vertices (larger models are rejected with FFSRL_ERR_INVALID_ARGUMENT);
+   the array is cleared at the start of every call and shared by all calls, so calls
+   that overlap on the GPU race; connector corrections do not carry over between calls.
+   The first call on a device looks up the array's address; make it before any stream
+   capture. */
+int32_t ffsrl_step_model_noalloc(const ffsrl_model* model, const ffsrl_params* params, void* stream);
+
 /* remapAToBKernel (utils.py:32-42): dst[map[2i]] = src[map[2i+1]] for i < count */
 int32_t ffsrl_remap(float* dst, const float* src, const int32_t* map, int32_t count, void* stream);
 
