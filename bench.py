@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--envs", type=int, default=NUM_ENVS)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=5.0)
     return ap.parse_args()
 
 
@@ -311,6 +312,19 @@ def main():
         plain = {"value": envs / (plain_ms / 1000.0), "unit": "env-steps/s", "ms_per_step": plain_ms,
                  "speedup_batched_vs_plain": value / world / (envs / (plain_ms / 1000.0))}
 
+    serving = None
+    if args.serve_seconds > 0:
+        # continuous-batching serving of the same pool: one closed-loop actor per env
+        from ffsrl import scenarios as sc2
+        from ffsrl.serve import EnvServer
+        meshes_s, pool_s = sc2.mixed_meshes(envs, pool_size=POOL, seed=rank)
+        ids = {id(mm): k for k, mm in enumerate(pool_s)}
+        srv = EnvServer(pool_s, [ids[id(mm)] for mm in meshes_s], device, hbm_budget_bytes=60e9, resolution=RES,
+                        autotune=True)
+        serving = srv.run_closed_loop(args.serve_seconds, think_hz=60.0, seed=rank, warmup_s=1.0)
+        serving["what"] = ("closed-loop actors, Poisson think time at 60 Hz, each request = tool move + 8x10 step "
+                           "+ refit + 128x128 ray-cast of its env; latency from arrival to result on the host")
+        del srv
     if rank == 0:
         cpu = None
         if not args.no_cpu:
@@ -330,7 +344,8 @@ def main():
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                              "kernel": "k_batched (batched step, all size classes)", "kernel_ms": step_kernel_ms},
-                "cpu_baseline": cpu, "plain": plain, "gpu_launches": launches, "autotune": integ.tuning,
+                "cpu_baseline": cpu, "plain": plain, "serving": serving, "gpu_launches": launches,
+                "autotune": integ.tuning,
                 "clocks": clk.summary(), "env_status_nonzero": int((status != 0).sum())}
         print(json.dumps(line))
     if world > 1:

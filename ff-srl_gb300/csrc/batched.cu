@@ -642,16 +642,24 @@ struct ffsrl_batch {
         int mode, block, max_nv, grid, members;
         size_t smem, scratch_stride, scratch_offset;
         int work_offset, work_count;
-        cudaStream_t stream;
-        cudaEvent_t done;
     };
     std::vector<Class> classes;
     std::vector<int> env_class;
     std::vector<int> work_host;  // per class, largest first
     std::vector<int64_t> env_cost;
-    cudaEvent_t fork = nullptr;
-    int* h_work_pinned = nullptr;
-    int* d_work_sub = nullptr;
+    // A lane is one in-flight launch sequence: its own class streams, work list, work
+    // counters and scratch, so steps of disjoint env sets on different lanes can overlap.
+    struct Lane {
+        cudaEvent_t fork = nullptr, staged = nullptr;
+        std::vector<cudaStream_t> streams;
+        std::vector<cudaEvent_t> done;
+        int* d_counters = nullptr;
+        int* d_work_sub = nullptr;
+        int* h_work_pinned = nullptr;
+        bool staged_pending = false;
+    };
+    std::vector<Lane> lanes;
+    size_t scratch_per_lane = 0;
 };
 
 namespace {
@@ -674,15 +682,18 @@ void free_batch(ffsrl_batch* b) {
     if (!b) return;
     cudaFree(b->d_env); cudaFree(b->d_tet_idx); cudaFree(b->d_tet_va); cudaFree(b->d_dmA); cudaFree(b->d_dmB);
     cudaFree(b->d_dmC); cudaFree(b->d_tet_vs); cudaFree(b->d_edge_idx); cudaFree(b->d_edge_la); cudaFree(b->d_tri_idx);
-    cudaFree(b->d_work); cudaFree(b->d_counters); cudaFree(b->d_status); cudaFree(b->d_scratch);
-    cudaFree(b->d_state64); cudaFree(b->d_work_sub); cudaFree(b->d_cnt0); cudaFree(b->d_tet_orig);
+    cudaFree(b->d_work); cudaFree(b->d_status); cudaFree(b->d_scratch);
+    cudaFree(b->d_state64); cudaFree(b->d_cnt0); cudaFree(b->d_tet_orig);
     cudaFree(b->d_edge_orig);
-    if (b->h_work_pinned) cudaFreeHost(b->h_work_pinned);
-    for (auto& c : b->classes) {
-        if (c.stream) cudaStreamDestroy(c.stream);
-        if (c.done) cudaEventDestroy(c.done);
+    for (auto& l : b->lanes) {
+        for (auto s : l.streams) if (s) cudaStreamDestroy(s);
+        for (auto e : l.done) if (e) cudaEventDestroy(e);
+        if (l.fork) cudaEventDestroy(l.fork);
+        if (l.staged) cudaEventDestroy(l.staged);
+        cudaFree(l.d_counters);
+        cudaFree(l.d_work_sub);
+        if (l.h_work_pinned) cudaFreeHost(l.h_work_pinned);
     }
-    if (b->fork) cudaEventDestroy(b->fork);
     delete b;
 }
 
@@ -695,7 +706,7 @@ int default_block(int max_nv, int mode) {
 }
 
 template <class R> int32_t launch_class(ffsrl_batch* b, const ffsrl_batch::Class& c, const int* work, int nwork,
-                                        int slot, int nsteps, cudaStream_t s);
+                                        int* counter, unsigned char* scratch, int nsteps, cudaStream_t s);
 
 Dev<float> make_dev_f(ffsrl_batch* b) {
     Dev<float> D;
@@ -721,20 +732,20 @@ Dev<float> make_dev_f(ffsrl_batch* b) {
 }
 
 template <> int32_t launch_class<float>(ffsrl_batch* b, const ffsrl_batch::Class& c, const int* work, int nwork,
-                                        int slot, int nsteps, cudaStream_t s) {
+                                        int* counter, unsigned char* scratch, int nsteps, cudaStream_t s) {
     kern_f k = pick_f(c.block, c.mode);
     if (!k) return fail(FFSRL_ERR_UNSUPPORTED, "ffsrl_batch: no kernel for block/mode");
     Dev<float> D = make_dev_f(b);
     int grid = std::min(c.grid, nwork);
     if (grid <= 0) return FFSRL_OK;
-    k<<<grid, c.block, c.smem, s>>>(D, work, nwork, b->d_counters + slot, nsteps, b->d_scratch + c.scratch_offset,
+    k<<<grid, c.block, c.smem, s>>>(D, work, nwork, counter, nsteps, scratch + c.scratch_offset,
                                     (long long)c.scratch_stride, c.max_nv);
     FFSRL_LAUNCH_CHECK("ffsrl_batch: step kernel");
     return FFSRL_OK;
 }
 
 template <> int32_t launch_class<double>(ffsrl_batch* b, const ffsrl_batch::Class& c, const int* work, int nwork,
-                                         int slot, int nsteps, cudaStream_t s) {
+                                         int* counter, unsigned char* scratch, int nsteps, cudaStream_t s) {
     kern_d k = pick_d(c.block, c.mode);
     if (!k) return fail(FFSRL_ERR_UNSUPPORTED, "ffsrl_batch: no float64 kernel for block/mode");
     Dev<float> F = make_dev_f(b);
@@ -753,33 +764,40 @@ template <> int32_t launch_class<double>(ffsrl_batch* b, const ffsrl_batch::Clas
     D.ks_drag = F.ks_drag; D.vol_c = F.vol_c; D.dev_c = F.dev_c; D.a_dist = F.a_dist; D.a_vol = F.a_vol;
     int grid = std::min(c.grid, nwork);
     if (grid <= 0) return FFSRL_OK;
-    k<<<grid, c.block, c.smem, s>>>(D, work, nwork, b->d_counters + slot, nsteps, b->d_scratch + c.scratch_offset,
+    k<<<grid, c.block, c.smem, s>>>(D, work, nwork, counter, nsteps, scratch + c.scratch_offset,
                                     (long long)c.scratch_stride, c.max_nv);
     FFSRL_LAUNCH_CHECK("ffsrl_batch: float64 step kernel");
     return FFSRL_OK;
 }
 
-int32_t run(ffsrl_batch* b, const std::vector<int>& counts, const int* d_work_base,
+int32_t run(ffsrl_batch* b, int lane, const std::vector<int>& counts, const int* d_work_base,
             const std::vector<int>& offsets, int nsteps, cudaStream_t s) {
-    FFSRL_CUDA_TRY(cudaMemsetAsync(b->d_counters, 0, sizeof(int) * b->classes.size(), s));
-    FFSRL_CUDA_TRY(cudaEventRecord(b->fork, s));
+    auto& L = b->lanes[lane];
+    unsigned char* scratch = b->d_scratch ? b->d_scratch + (size_t)lane * b->scratch_per_lane : nullptr;
+    FFSRL_CUDA_TRY(cudaMemsetAsync(L.d_counters, 0, sizeof(int) * b->classes.size(), s));
+    FFSRL_CUDA_TRY(cudaEventRecord(L.fork, s));
     for (size_t ci = 0; ci < b->classes.size(); ++ci) {
         auto& c = b->classes[ci];
-        FFSRL_CUDA_TRY(cudaStreamWaitEvent(c.stream, b->fork, 0));
+        cudaStream_t cs = L.streams[ci];
+        FFSRL_CUDA_TRY(cudaStreamWaitEvent(cs, L.fork, 0));
         if (counts[ci] > 0) {
             int32_t st = b->precision == 64
-                             ? launch_class<double>(b, c, d_work_base + offsets[ci], counts[ci], (int)ci, nsteps, c.stream)
-                             : launch_class<float>(b, c, d_work_base + offsets[ci], counts[ci], (int)ci, nsteps, c.stream);
+                             ? launch_class<double>(b, c, d_work_base + offsets[ci], counts[ci], L.d_counters + ci,
+                                                    scratch, nsteps, cs)
+                             : launch_class<float>(b, c, d_work_base + offsets[ci], counts[ci], L.d_counters + ci,
+                                                   scratch, nsteps, cs);
             if (st) return st;
         }
-        FFSRL_CUDA_TRY(cudaEventRecord(c.done, c.stream));
-        FFSRL_CUDA_TRY(cudaStreamWaitEvent(s, c.done, 0));
+        FFSRL_CUDA_TRY(cudaEventRecord(L.done[ci], cs));
+        FFSRL_CUDA_TRY(cudaStreamWaitEvent(s, L.done[ci], 0));
     }
     return FFSRL_OK;
 }
 
 // Block size of a class: the instantiation, its shared-memory allowance and the grid
 // from the runtime's occupancy calculator.
+constexpr int kLanes = 2;
+
 int32_t configure_class(ffsrl_batch* b, ffsrl_batch::Class& c, int block, size_t dyn_budget) {
     if (b->precision == 64) block = 256;
     if (c.mode == 1 && block < 256) block = 256;
@@ -1066,9 +1084,8 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
         (st = dalloc(b, &b->d_edge_la, E)) || (st = upload(b->d_edge_la, edge_la)) ||
         (st = dalloc(b, &b->d_tri_idx, F)) || (st = upload(b->d_tri_idx, tri_idx)) ||
         (st = dalloc(b, &b->d_work, (size_t)N)) || (st = upload(b->d_work, b->work_host)) ||
-        (st = dalloc(b, &b->d_work_sub, (size_t)N)) ||
-        (st = dalloc(b, &b->d_counters, b->classes.size() + 1)) || (st = dalloc(b, &b->d_status, (size_t)N)) ||
-        (st = dalloc(b, &b->d_scratch, scratch_total))) {
+        (st = dalloc(b, &b->d_status, (size_t)N)) ||
+        (st = dalloc(b, &b->d_scratch, scratch_total * kLanes))) {
         free_batch(b);
         return st;
     }
@@ -1083,11 +1100,22 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
         for (int64_t i = 0; i < 3 * V; ++i) { h64[i] = hx[i]; h64[3 * V + i] = hv[i]; h64[6 * V + i] = hx[i]; }
         if ((st = upload(b->d_state64, h64))) { free_batch(b); return st; }
     }
-    FFSRL_CUDA_TRY(cudaHostAlloc((void**)&b->h_work_pinned, sizeof(int) * N, cudaHostAllocDefault));
-    FFSRL_CUDA_TRY(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
-    for (auto& c : b->classes) {
-        FFSRL_CUDA_TRY(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
-        FFSRL_CUDA_TRY(cudaEventCreateWithFlags(&c.done, cudaEventDisableTiming));
+    b->scratch_per_lane = scratch_total;
+    b->lanes.resize(kLanes);
+    for (auto& L : b->lanes) {
+        if ((st = dalloc(b, &L.d_counters, b->classes.size() + 1)) || (st = dalloc(b, &L.d_work_sub, (size_t)N))) {
+            free_batch(b);
+            return st;
+        }
+        FFSRL_CUDA_TRY(cudaHostAlloc((void**)&L.h_work_pinned, sizeof(int) * N, cudaHostAllocDefault));
+        FFSRL_CUDA_TRY(cudaEventCreateWithFlags(&L.fork, cudaEventDisableTiming));
+        FFSRL_CUDA_TRY(cudaEventCreateWithFlags(&L.staged, cudaEventDisableTiming));
+        L.streams.resize(b->classes.size());
+        L.done.resize(b->classes.size());
+        for (size_t ci = 0; ci < b->classes.size(); ++ci) {
+            FFSRL_CUDA_TRY(cudaStreamCreateWithFlags(&L.streams[ci], cudaStreamNonBlocking));
+            FFSRL_CUDA_TRY(cudaEventCreateWithFlags(&L.done[ci], cudaEventDisableTiming));
+        }
     }
     *out = b;
     return FFSRL_OK;
@@ -1104,22 +1132,25 @@ extern "C" int32_t ffsrl_batch_step(ffsrl_batch* b, int32_t n_steps, void* strea
     if (n_steps == 0) return FFSRL_OK;
     std::vector<int> counts, offsets;
     for (auto& c : b->classes) { counts.push_back(c.work_count); offsets.push_back(c.work_offset); }
-    return run(b, counts, b->d_work, offsets, n_steps, (cudaStream_t)stream);
+    return run(b, 0, counts, b->d_work, offsets, n_steps, (cudaStream_t)stream);
 }
 
-extern "C" int32_t ffsrl_batch_step_envs(ffsrl_batch* b, const int32_t* env_ids, int32_t n, int32_t n_steps,
-                                         void* stream) {
-    if (!b || n < 0 || n_steps < 0 || (n > 0 && !env_ids)) return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_step_envs");
+extern "C" int32_t ffsrl_batch_step_envs_lane(ffsrl_batch* b, int32_t lane, const int32_t* env_ids, int32_t n,
+                                              int32_t n_steps, void* stream) {
+    if (!b || n < 0 || n_steps < 0 || (n > 0 && !env_ids) || lane < 0 || lane >= (int)b->lanes.size())
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_step_envs: bad argument or lane");
     if (n == 0 || n_steps == 0) return FFSRL_OK;
+    if (n > b->num_envs) return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_step_envs: more ids than envs");
     cudaStream_t s = (cudaStream_t)stream;
-    // the pinned staging buffer is reused: wait for the previous upload to finish reading it
-    FFSRL_CUDA_TRY(cudaStreamSynchronize(s));
+    auto& L = b->lanes[lane];
     std::vector<std::vector<int>> per(b->classes.size());
     for (int i = 0; i < n; ++i) {
         int e = env_ids[i];
         if (e < 0 || e >= b->num_envs) return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_step_envs: env id out of range");
         per[b->env_class[e]].push_back(e);
     }
+    // the lane's pinned staging buffer is reused: wait until its previous upload has read it
+    if (L.staged_pending) FFSRL_CUDA_TRY(cudaEventSynchronize(L.staged));
     std::vector<int> counts, offsets;
     int o = 0;
     for (size_t ci = 0; ci < per.size(); ++ci) {
@@ -1129,10 +1160,17 @@ extern "C" int32_t ffsrl_batch_step_envs(ffsrl_batch* b, const int32_t* env_ids,
         });
         offsets.push_back(o);
         counts.push_back((int)v.size());
-        for (int e : v) b->h_work_pinned[o++] = e;
+        for (int e : v) L.h_work_pinned[o++] = e;
     }
-    FFSRL_CUDA_TRY(cudaMemcpyAsync(b->d_work_sub, b->h_work_pinned, sizeof(int) * o, cudaMemcpyHostToDevice, s));
-    return run(b, counts, b->d_work_sub, offsets, n_steps, s);
+    FFSRL_CUDA_TRY(cudaMemcpyAsync(L.d_work_sub, L.h_work_pinned, sizeof(int) * o, cudaMemcpyHostToDevice, s));
+    FFSRL_CUDA_TRY(cudaEventRecord(L.staged, s));
+    L.staged_pending = true;
+    return run(b, lane, counts, L.d_work_sub, offsets, n_steps, s);
+}
+
+extern "C" int32_t ffsrl_batch_step_envs(ffsrl_batch* b, const int32_t* env_ids, int32_t n, int32_t n_steps,
+                                         void* stream) {
+    return ffsrl_batch_step_envs_lane(b, 0, env_ids, n, n_steps, stream);
 }
 
 extern "C" int32_t ffsrl_batch_info(const ffsrl_batch* b, int64_t* device_bytes, int32_t* num_classes,

@@ -318,6 +318,17 @@ __global__ void k_remap(float* __restrict__ dst, const float* __restrict__ src, 
     st3(dst, a, ld3(src, b));
 }
 
+// remapAToBKernel over one listed env's points per block
+__global__ void k_remap_envs(float* __restrict__ dst, const float* __restrict__ src, const int* __restrict__ map,
+                             const int* __restrict__ pstart, const int* __restrict__ ids, int num_envs) {
+    int e = ids[blockIdx.x];
+    if (e < 0 || e >= num_envs) return;
+    for (int i = pstart[e] + threadIdx.x; i < pstart[e + 1]; i += blockDim.x) {
+        int a = map[2 * i], b = map[2 * i + 1];
+        st3(dst, a, ld3(src, b));
+    }
+}
+
 // updateClampsDragKernel (modelDO.py:247-279)
 __global__ void k_update_clamps(const float* __restrict__ pos, const int* __restrict__ v2e,
                                 const float* __restrict__ tip, float* drag, float radius,
@@ -346,10 +357,13 @@ __global__ void k_force_clamps(float* drag, int vid, const int* __restrict__ env
 // lower candidate position.
 __global__ void k_grasp_nearest(const float* __restrict__ pos, const int* __restrict__ cstart,
                                 const int* __restrict__ cand, const float* __restrict__ tip,
-                                const int* __restrict__ clamp, float radius, float* drag) {
-    int e = blockIdx.x;
+                                const int* __restrict__ clamp, float radius, float* drag,
+                                const int* __restrict__ ids, int num_envs) {
+    const int k = blockIdx.x;        // clamp flag index
+    const int e = ids ? ids[k] : k;  // env
+    if (e < 0 || e >= num_envs) return;
     int c0 = cstart[e], c1 = cstart[e + 1];
-    if (clamp[e] == 0) {
+    if (clamp[k] == 0) {
         for (int k = c0 + threadIdx.x; k < c1; k += blockDim.x) drag[cand[k]] = 0.0f;
         return;
     }
@@ -379,6 +393,19 @@ __global__ void k_grasp_nearest(const float* __restrict__ pos, const int* __rest
     unsigned long long b = s_best[0];
     for (int k = c0 + threadIdx.x; k < c1; k += blockDim.x)
         drag[cand[k]] = (b != ~0ull && (unsigned)(k - c0) == (unsigned)(b & 0xffffffffu)) ? 1.0f : 0.0f;
+}
+
+// env-list variant: disp[i] moves env env_ids[i]
+__global__ void k_move_tool_envs(float* base, float* tip, const float* __restrict__ disp, const int* __restrict__ ids,
+                                 int n, int num_envs) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 4 * n) return;
+    int k = i >> 2;
+    if (ids[k] < 0 || ids[k] >= num_envs) return;
+    long long slot = 4ll * ids[k] + (i & 3);
+    v3 d = ld3(disp, k);
+    st3(base, slot, ld3(base, slot) + d);
+    st3(tip, slot, ld3(tip, slot) + d);
 }
 
 __global__ void k_move_tool(float* base, float* tip, const float* __restrict__ disp, int n) {
@@ -491,6 +518,16 @@ extern "C" int32_t ffsrl_remap(float* dst, const float* src, const int32_t* map,
     return FFSRL_OK;
 }
 
+extern "C" int32_t ffsrl_remap_envs(float* dst, const float* src, const int32_t* map, const int32_t* point_start,
+                                    const int32_t* env_ids, int32_t n, int32_t num_envs, void* stream) {
+    if (n < 0 || num_envs < 0 || (n > 0 && (!dst || !src || !map || !point_start || !env_ids)))
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_remap_envs");
+    if (n == 0) return FFSRL_OK;
+    k_remap_envs<<<n, 256, 0, (cudaStream_t)stream>>>(dst, src, map, point_start, env_ids, num_envs);
+    FFSRL_LAUNCH_CHECK("ffsrl_remap_envs");
+    return FFSRL_OK;
+}
+
 extern "C" int32_t ffsrl_update_clamps_drag(const float* positions, const int32_t* vertex_to_env,
                                             const float* laparoscope_tip, float* drag, float lookup_radius,
                                             const int32_t* state, const int32_t* update, int32_t num_vertices,
@@ -522,8 +559,33 @@ extern "C" int32_t ffsrl_grasp_nearest(const float* positions, const int32_t* ca
         return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_grasp_nearest");
     if (num_envs == 0) return FFSRL_OK;
     k_grasp_nearest<<<num_envs, 256, 0, (cudaStream_t)stream>>>(positions, cand_start, cand, laparoscope_tip, clamp,
-                                                                radius, drag);
+                                                                radius, drag, nullptr, num_envs);
     FFSRL_LAUNCH_CHECK("ffsrl_grasp_nearest");
+    return FFSRL_OK;
+}
+
+extern "C" int32_t ffsrl_grasp_nearest_envs(const float* positions, const int32_t* cand_start, const int32_t* cand,
+                                            const float* laparoscope_tip, const int32_t* clamp, float radius,
+                                            float* drag, const int32_t* env_ids, int32_t n, int32_t num_envs,
+                                            void* stream) {
+    if (n < 0 || num_envs < 0 ||
+        (n > 0 && (!positions || !cand_start || !cand || !laparoscope_tip || !clamp || !drag || !env_ids)))
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_grasp_nearest_envs");
+    if (n == 0) return FFSRL_OK;
+    k_grasp_nearest<<<n, 256, 0, (cudaStream_t)stream>>>(positions, cand_start, cand, laparoscope_tip, clamp, radius,
+                                                         drag, env_ids, num_envs);
+    FFSRL_LAUNCH_CHECK("ffsrl_grasp_nearest_envs");
+    return FFSRL_OK;
+}
+
+extern "C" int32_t ffsrl_move_tool_envs(float* laparoscope_base, float* laparoscope_tip, const float* disp,
+                                        const int32_t* env_ids, int32_t n, int32_t num_envs, void* stream) {
+    if (n < 0 || num_envs < 0 || (n > 0 && (!laparoscope_base || !laparoscope_tip || !disp || !env_ids)))
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_move_tool_envs");
+    if (n == 0) return FFSRL_OK;
+    k_move_tool_envs<<<grid_for(4ll * n, kBlock), kBlock, 0, (cudaStream_t)stream>>>(laparoscope_base, laparoscope_tip,
+                                                                                    disp, env_ids, n, num_envs);
+    FFSRL_LAUNCH_CHECK("ffsrl_move_tool_envs");
     return FFSRL_OK;
 }
 

@@ -63,9 +63,11 @@ __global__ void k_refit_level(ffsrl_bvh b, const float* __restrict__ pts, const 
     refit_node(b, pts, faces, e, n0, b.topo_tri_offset[topo], b.env_node_offset[e], node);
 }
 
-// One block per env: levels deepest first, nodes of a level in parallel.
-__global__ void k_refit_fused(ffsrl_bvh b, const float* __restrict__ pts, const int* __restrict__ faces) {
-    int e = blockIdx.x;
+// One block per env (or per listed env): levels deepest first, nodes of a level in parallel.
+__global__ void k_refit_fused(ffsrl_bvh b, const float* __restrict__ pts, const int* __restrict__ faces,
+                              const int* __restrict__ ids) {
+    int e = ids ? ids[blockIdx.x] : blockIdx.x;
+    if (e < 0 || e >= b.num_envs) return;
     int topo = b.env_topology[e];
     int n0 = b.topo_node_offset[topo], t0 = b.topo_tri_offset[topo];
     int base = b.env_node_offset[e];
@@ -113,6 +115,23 @@ __global__ void k_normal_gather(const float* __restrict__ pts, const int* __rest
         s = s + cross(b - a, c - a);
     }
     st3(nrm, i, normalize(s));
+}
+
+// the same gather for the points of one listed env per block
+__global__ void k_normal_gather_envs(const float* __restrict__ pts, const int* __restrict__ faces,
+                                     const int* __restrict__ start, const int* __restrict__ pf, float* __restrict__ nrm,
+                                     const int* __restrict__ pstart, const int* __restrict__ ids, int num_envs) {
+    int e = ids[blockIdx.x];
+    if (e < 0 || e >= num_envs) return;
+    for (int i = pstart[e] + threadIdx.x; i < pstart[e + 1]; i += blockDim.x) {
+        v3 s = mk(0.0f, 0.0f, 0.0f);
+        for (int k = start[i]; k < start[i + 1]; ++k) {
+            long long f = pf[k];
+            v3 a = ld3(pts, faces[3 * f]), b = ld3(pts, faces[3 * f + 1]), c = ld3(pts, faces[3 * f + 2]);
+            s = s + cross(b - a, c - a);
+        }
+        st3(nrm, i, normalize(s));
+    }
 }
 
 __device__ __forceinline__ v3 quat_rotate(float4 q, v3 x) {
@@ -327,16 +346,17 @@ __global__ void k_downsample(ffsrl_render r) {
 // One thread per ray; the four rays of a pixel sit in consecutive lanes and are summed
 // by shuffles in downsample_kernel's order ((r00 + r01) + r10) + r11, then divided by 4.
 // A block covers an 8x8 pixel tile of one env so neighbouring rays share BVH nodes in L1.
-__global__ void __launch_bounds__(256) k_rays(ffsrl_render r, ffsrl_bvh b) {
+__global__ void __launch_bounds__(256) k_rays(ffsrl_render r, ffsrl_bvh b, const int* __restrict__ ids, int n_ids) {
     const int R = r.resolution, W = 2 * R, H = 2 * R;
     const int tiles_x = (R + 7) / 8;
     const int tiles = tiles_x * ((R + 7) / 8);
-    const int e = blockIdx.x / tiles;
+    const int k = blockIdx.x / tiles;
+    const int e = ids ? (k < n_ids ? ids[k] : r.num_envs) : k;
     const int tile = blockIdx.x % tiles;
     const int pix = threadIdx.x >> 2, q = threadIdx.x & 3;
     const int px = (tile % tiles_x) * 8 + (pix & 7);
     const int py = (tile / tiles_x) * 8 + (pix >> 3);
-    const bool valid = e < r.num_envs && px < R && py < R;
+    const bool valid = e >= 0 && e < r.num_envs && px < R && py < R;
     Shade s;
     s.color = mk(0.0f, 0.0f, 0.0f);
     s.depth = 0.0f;
@@ -406,7 +426,7 @@ extern "C" int32_t ffsrl_bvh_refit_fused(const ffsrl_bvh* b, const float* pts, c
     if (int32_t st = check_bvh(b)) return st;
     if (!pts || !faces || !b->level_node || !b->level_start || !b->topo_level_offset)
         return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_bvh_refit_fused: needs level grouping arrays");
-    k_refit_fused<<<b->num_envs, 256, 0, (cudaStream_t)stream>>>(*b, pts, faces);
+    k_refit_fused<<<b->num_envs, 256, 0, (cudaStream_t)stream>>>(*b, pts, faces, nullptr);
     FFSRL_LAUNCH_CHECK("ffsrl_bvh_refit_fused");
     return FFSRL_OK;
 }
@@ -439,7 +459,34 @@ extern "C" int32_t ffsrl_render_fused(const ffsrl_render* r, const ffsrl_bvh* b,
     k_normal_gather<<<grid_for(P, 256), 256, 0, s>>>(r->vis_point, r->vis_face, r->point_face_start, r->point_face,
                                                      r->vertex_normal, P);
     const int tiles = ((r->resolution + 7) / 8) * ((r->resolution + 7) / 8);
-    k_rays<<<(unsigned)((long long)tiles * r->num_envs), 256, 0, s>>>(*r, *b);
+    k_rays<<<(unsigned)((long long)tiles * r->num_envs), 256, 0, s>>>(*r, *b, nullptr, 0);
     FFSRL_LAUNCH_CHECK("ffsrl_render_fused");
+    return FFSRL_OK;
+}
+
+extern "C" int32_t ffsrl_bvh_refit_fused_envs(const ffsrl_bvh* b, const float* pts, const int32_t* faces,
+                                              const int32_t* env_ids, int32_t n, void* stream) {
+    if (int32_t st = check_bvh(b)) return st;
+    if (n < 0 || (n > 0 && (!pts || !faces || !env_ids || !b->level_node || !b->level_start || !b->topo_level_offset)))
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_bvh_refit_fused_envs");
+    if (n == 0) return FFSRL_OK;
+    k_refit_fused<<<n, 256, 0, (cudaStream_t)stream>>>(*b, pts, faces, env_ids);
+    FFSRL_LAUNCH_CHECK("ffsrl_bvh_refit_fused_envs");
+    return FFSRL_OK;
+}
+
+extern "C" int32_t ffsrl_render_fused_envs(const ffsrl_render* r, const ffsrl_bvh* b, const int32_t* env_ids,
+                                           int32_t n, void* stream) {
+    if (int32_t st = check_render(r)) return st;
+    if (int32_t st = check_bvh(b)) return st;
+    if (n < 0 || (n > 0 && (!env_ids || !r->point_face_start || !r->point_face || !r->env_point_start)))
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_render_fused_envs: needs env ids, point->face CSR, env point ranges");
+    if (n == 0) return FFSRL_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    k_normal_gather_envs<<<n, 256, 0, s>>>(r->vis_point, r->vis_face, r->point_face_start, r->point_face,
+                                           r->vertex_normal, r->env_point_start, env_ids, r->num_envs);
+    const int tiles = ((r->resolution + 7) / 8) * ((r->resolution + 7) / 8);
+    k_rays<<<(unsigned)((long long)tiles * n), 256, 0, s>>>(*r, *b, env_ids, n);
+    FFSRL_LAUNCH_CHECK("ffsrl_render_fused_envs");
     return FFSRL_OK;
 }

@@ -93,7 +93,7 @@ class Render(C.Structure):
         ("point_face_start", P), ("point_face", P),
         ("num_cameras", I32), ("camera_pos", P), ("camera_rot", P), ("camera_tan", F32), ("camera_aspect", F32),
         ("num_lights", I32), ("light_dir", P), ("light_intensity", P),
-        ("color", P), ("depth", P), ("rays", P), ("ray_depth", P), ("error_flag", P),
+        ("color", P), ("depth", P), ("rays", P), ("ray_depth", P), ("error_flag", P), ("env_point_start", P),
     ]
 
 
@@ -121,10 +121,16 @@ def lib() -> C.CDLL:
         "ffsrl_step_model": ([pm, pp, P], I32),
         "ffsrl_step_model_noalloc": ([pm, pp, P], I32),
         "ffsrl_remap": ([P, P, P, I32, P], I32),
+        "ffsrl_remap_envs": ([P, P, P, P, P, I32, I32, P], I32),
         "ffsrl_update_clamps_drag": ([P, P, P, P, F32, P, P, I32, P], I32),
         "ffsrl_force_clamps_drag": ([P, I32, P, I32, F32, I32, P], I32),
         "ffsrl_grasp_nearest": ([P, P, P, P, P, F32, P, I32, P], I32),
         "ffsrl_move_tool": ([P, P, P, I32, P], I32),
+        "ffsrl_move_tool_envs": ([P, P, P, P, I32, I32, P], I32),
+        "ffsrl_grasp_nearest_envs": ([P, P, P, P, P, F32, P, P, I32, I32, P], I32),
+        "ffsrl_bvh_refit_fused_envs": ([pb, P, P, P, I32, P], I32),
+        "ffsrl_render_fused_envs": ([pr, pb, P, I32, P], I32),
+        "ffsrl_batch_step_envs_lane": ([P, I32, P, I32, I32, P], I32),
         "ffsrl_bvh_build_host": ([P, P, I32, I32, I32, P, P, P, P, P, P, P, C.POINTER(I32), C.POINTER(I32)], I32),
         "ffsrl_bvh_refit_levels": ([pb, P, P, P], I32),
         "ffsrl_bvh_refit_fused": ([pb, P, P, P], I32),

@@ -238,6 +238,7 @@ class SimModelDO:
         self.envTetStartT = T(self.envTetStart, **i32)
         self.envEdgeStartT = T(self.envEdgeStart, **i32)
         self.envTriStartT = T(self.envTriStart, **i32)
+        self.envVisPointStartT = T(self.envVisPointStart, **i32)
         self.connectorVertexId = torch.zeros(0, **i32)
         self.connectorTriangleId = torch.zeros(0, **i32)
         self.connectorTriBar = torch.zeros((0, 3), **f32)

@@ -128,6 +128,7 @@ class WarpRaycastRendererDO:
                 self.rayDepth = torch.zeros(self.numEnvs * self.num_rays, dtype=torch.float32, device=self.device)
             r.rays, r.ray_depth = ptr(self.rays), ptr(self.rayDepth)
         r.error_flag = ptr(self.errorFlag)
+        r.env_point_start = ptr(simModel.envVisPointStartT)
         return r
 
     def renderFunctionNew(self, simBVH, stream=None) -> None:

@@ -1,0 +1,328 @@
+"""Continuous-batching server of RL step requests over device-resident environments.
+
+Each actor owns one environment (a mesh from a mixed-size pool) and sends step
+requests: a tool displacement and a clamp flag.  Environments live in slots of one
+batched model, grouped by mesh type; a device-memory budget bounds the number of slots.
+An actor without a slot is admitted into a free slot of its mesh type. If there is none,
+the least recently used idle actor of that type is evicted: its state is copied to
+host memory and restored when it returns.
+
+Requests are served in ticks.  A tick takes every ready request (arrived, its actor not
+already on the GPU, admitted) and runs, for exactly those environments: the tool move,
+grasp changes, one batched step (substeps x iterations), the visual-point remap, the
+BVH refit and the ray-cast observation; then the per-env result (effector position and
+contact count) is copied back.  Two lanes -- each with its own stream, work lists and
+staging -- let the next tick start while the previous one is still on the GPU, so
+requests that arrive mid-tick are served by the next tick on the other lane.  Each
+environment's result depends only on its own inputs (the batched step sums corrections
+in fixed point, the renderer gathers normals in face order), so it is the same whether
+the environment is stepped alone or in any mix.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from . import scenarios as sc
+from ._lib import check, lib, ptr
+from .bvh import SimBVH
+from .integrator import SimIntegratorDO
+from .render import WarpRaycastRendererDO
+
+
+def slot_bytes(mesh: dict, resolution: int) -> int:
+    """Device bytes one slot of ``mesh`` holds: model arrays, batch tables, BVH, images."""
+    V, T, E = len(mesh["vertex"]), len(mesh["tetrahedron"]), len(mesh["edge"])
+    F, P = len(mesh["triangle"]), len(mesh["point_to_vertex"])
+    model = V * (12 * 6 + 4 * 4) + T * (16 + 4 * 5 + 36) + E * (8 + 4 * 3) + F * (12 + 8) + P * (12 * 3 + 8)
+    plan = T * (8 + 8 + 36 + 4) + E * (4 + 8 + 4) + F * 8 + V * 4
+    bvh = 2 * F * (24 + 16) + F * 4
+    image = resolution * resolution * 16
+    return int(model + plan + bvh + image)
+
+
+def plan_slots(pool: list, actor_mesh, hbm_budget_bytes: float, resolution: int) -> np.ndarray:
+    """Slots per mesh type: one per actor when they fit in the budget, otherwise scaled
+    down (at least one per mesh type in use) until the total fits."""
+    actor_mesh = np.asarray(actor_mesh, dtype=np.int64)
+    want = np.bincount(actor_mesh, minlength=len(pool))
+    per = np.array([slot_bytes(m, resolution) for m in pool], dtype=np.float64)
+    if float((want * per).sum()) <= hbm_budget_bytes:
+        return want
+    k = np.floor(want * hbm_budget_bytes / float((want * per).sum())).astype(np.int64)
+    k = np.where(want > 0, np.maximum(k, 1), 0)
+    while float((k * per).sum()) > hbm_budget_bytes and k.max() > 1:
+        k[np.argmax(k * per)] -= 1
+    if float((k * per).sum()) > hbm_budget_bytes:
+        raise L.FFSRLError(L.ERR_BUDGET, "HBM budget too small for one slot per mesh type in use")
+    return k
+
+
+@dataclass
+class Request:
+    actor: int
+    disp: np.ndarray
+    clamp: int
+    t_arrival: float
+    t_done: float = 0.0
+    result: np.ndarray | None = None
+
+
+@dataclass
+class _Lane:
+    stream: torch.cuda.Stream
+    ids_h: torch.Tensor
+    act_h: torch.Tensor
+    res_h: torch.Tensor
+    ids_d: torch.Tensor
+    act_d: torch.Tensor
+    res_d: torch.Tensor
+    gids_d: torch.Tensor
+    gclamp_d: torch.Tensor
+    event: torch.cuda.Event
+    batch: list = field(default_factory=list)
+
+
+class EnvServer:
+    def __init__(self, pool: list, actor_mesh, device="cuda:0", hbm_budget_bytes: float = 60e9, resolution: int = 128,
+                 lanes: int = 2, seed: int = 0, autotune: bool = False, **model_kw):
+        self.device = torch.device(device)
+        self.pool = pool
+        self.actor_mesh = np.asarray(actor_mesh, dtype=np.int64)
+        self.num_actors = len(self.actor_mesh)
+        self.resolution = resolution
+        per = np.array([slot_bytes(m, resolution) for m in pool], dtype=np.float64)
+        self.slot_bytes = per
+        k = plan_slots(pool, self.actor_mesh, hbm_budget_bytes, resolution)
+        self.slots_per_mesh = k
+        self.slot_mesh = np.repeat(np.arange(len(pool)), k)
+        self.num_slots = int(len(self.slot_mesh))
+        self.budget_used = float((k * per).sum())
+        meshes = [pool[m] for m in self.slot_mesh]
+        self.model, _ = sc.liver_model(device, self.num_slots, meshes=meshes, **model_kw)
+        self.integ = SimIntegratorDO(device, autotune=autotune)
+        self.plan = self.integ.plan(self.model)
+        self.bvh = SimBVH(device, self.model)
+        ap = sc.fov_aperture(60.0)
+        self.renderer = WarpRaycastRendererDO(device, self.model, resolution=resolution, mode="headless",
+                                              verticalAperture=ap, horizontalAperture=ap, lightPos=(0.3, 1.0, 0.5),
+                                              lightIntensity=0.8)
+        pos, rot = sc.env_cameras(meshes, seed=seed + 1)
+        self.renderer.setCameras(pos, rot)
+        self.free = {m: list(np.nonzero(self.slot_mesh == m)[0][::-1]) for m in range(len(pool))}
+        self.slot_actor = np.full(self.num_slots, -1, dtype=np.int64)
+        self.actor_slot = np.full(self.num_actors, -1, dtype=np.int64)
+        self.actor_clamp = np.zeros(self.num_actors, dtype=np.int32)
+        self.last_used = np.zeros(self.num_actors)
+        self.in_flight = np.zeros(self.num_actors, dtype=bool)
+        self.snapshots: dict[int, dict] = {}
+        self.evictions = 0
+        self.admissions = 0
+        n = self.num_slots
+        pin = dict(pin_memory=True)
+        self.lanes = [_Lane(stream=torch.cuda.Stream(device=self.device),
+                            ids_h=torch.empty(n, dtype=torch.int32, **pin),
+                            act_h=torch.empty((n, 4), dtype=torch.float32, **pin),
+                            res_h=torch.empty((n, 4), dtype=torch.float32, **pin),
+                            ids_d=torch.empty(n, dtype=torch.int32, device=self.device),
+                            act_d=torch.empty((n, 4), dtype=torch.float32, device=self.device),
+                            res_d=torch.empty((n, 4), dtype=torch.float32, device=self.device),
+                            gids_d=torch.empty(n, dtype=torch.int32, device=self.device),
+                            gclamp_d=torch.empty(n, dtype=torch.int32, device=self.device),
+                            event=torch.cuda.Event())
+                      for _ in range(lanes)]
+        self.pending: list[Request] = []
+        torch.cuda.synchronize()
+
+    # ------------------------------------------------------------ admission
+    def _slot_views(self, s: int):
+        m = self.model
+        v0, v1 = int(m.envVertexStart[s]), int(m.envVertexStart[s + 1])
+        return {"vertex": m.vertex[v0:v1], "velocity": m.velocity[v0:v1], "drag": m.activeDragConstraint[v0:v1],
+                "base": m.laparoscopeBase[4 * s:4 * s + 4], "tip": m.laparoscopeTip[4 * s:4 * s + 4],
+                "incol": m.laparoscopeInCollision[s:s + 1]}
+
+    def _evict(self, a: int, stream) -> None:
+        s = int(self.actor_slot[a])
+        with torch.cuda.stream(stream):
+            snap = {k: v.to("cpu", non_blocking=True) for k, v in self._slot_views(s).items()}
+        stream.synchronize()
+        self.snapshots[a] = snap
+        self.actor_slot[a] = -1
+        self.slot_actor[s] = -1
+        self.free[int(self.slot_mesh[s])].append(s)
+        self.evictions += 1
+
+    def _admit(self, a: int, stream) -> bool:
+        m = int(self.actor_mesh[a])
+        if not self.free[m]:
+            idle = [int(x) for x in self.slot_actor[self.slot_mesh == m] if x >= 0 and not self.in_flight[x]]
+            if not idle:
+                return False
+            self._evict(min(idle, key=lambda x: self.last_used[x]), stream)
+        s = self.free[m].pop()
+        views = self._slot_views(s)
+        mm = self.model
+        with torch.cuda.stream(stream):
+            if a in self.snapshots:
+                snap = self.snapshots.pop(a)
+                for k, v in views.items():
+                    v.copy_(snap[k], non_blocking=True)
+            else:
+                v0, v1 = int(mm.envVertexStart[s]), int(mm.envVertexStart[s + 1])
+                views["vertex"].copy_(mm.initialVertex[v0:v1])
+                views["velocity"].zero_()
+                views["drag"].zero_()
+                views["base"].copy_(mm.laparoscopeInitialBase[4 * s:4 * s + 4])
+                views["tip"].copy_(mm.laparoscopeInitialTip[4 * s:4 * s + 4])
+                views["incol"].zero_()
+                self.actor_clamp[a] = 0
+        self.actor_slot[a] = s
+        self.slot_actor[s] = a
+        self.admissions += 1
+        return True
+
+    # ------------------------------------------------------------ ticks
+    def submit(self, req: Request) -> None:
+        self.pending.append(req)
+
+    def free_lane(self):
+        for ln in self.lanes:
+            if not ln.batch or ln.event.query():
+                return ln
+        return None
+
+    def poll(self) -> list[Request]:
+        done = []
+        now = time.perf_counter()
+        for ln in self.lanes:
+            if ln.batch and ln.event.query():
+                res = ln.res_h[:len(ln.batch)].numpy().copy()
+                for i, r in enumerate(ln.batch):
+                    r.t_done = now
+                    r.result = res[i]
+                    self.in_flight[r.actor] = False
+                done += ln.batch
+                ln.batch = []
+        return done
+
+    def launch(self, max_batch: int | None = None) -> int:
+        """Start a tick on a free lane with every ready request; returns its size."""
+        ln = self.free_lane()
+        if ln is None or not self.pending:
+            return 0
+        if ln.batch:  # finished but not yet collected
+            return 0
+        batch, rest = [], []
+        seen = set()
+        for r in self.pending:
+            if self.in_flight[r.actor] or r.actor in seen or (max_batch and len(batch) >= max_batch):
+                rest.append(r)
+                continue
+            if self.actor_slot[r.actor] < 0 and not self._admit(r.actor, ln.stream):
+                rest.append(r)
+                continue
+            seen.add(r.actor)
+            batch.append(r)
+        self.pending = rest
+        if not batch:
+            return 0
+        n = len(batch)
+        ids = np.array([self.actor_slot[r.actor] for r in batch], dtype=np.int32)
+        acts = np.array([[*r.disp, r.clamp] for r in batch], dtype=np.float32)
+        trans = [i for i, r in enumerate(batch) if r.clamp != self.actor_clamp[r.actor]]
+        m = self.model
+        s = L.stream_handle(ln.stream)
+        with torch.cuda.stream(ln.stream):
+            ln.ids_h[:n].copy_(torch.from_numpy(ids))
+            ln.act_h[:n].copy_(torch.from_numpy(acts))
+            ln.ids_d[:n].copy_(ln.ids_h[:n], non_blocking=True)
+            ln.act_d[:n].copy_(ln.act_h[:n], non_blocking=True)
+            disp = ln.act_d[:n, :3].contiguous()
+            check(lib().ffsrl_move_tool_envs(ptr(m.laparoscopeBase), ptr(m.laparoscopeTip), ptr(disp),
+                                             ptr(ln.ids_d), n, m.numEnvs, s))
+            if trans:
+                t = torch.tensor(trans, dtype=torch.long)
+                gids = torch.from_numpy(ids)[t]
+                gcl = torch.tensor([batch[i].clamp for i in trans], dtype=torch.int32)
+                ln.gids_d[:len(trans)].copy_(gids)
+                ln.gclamp_d[:len(trans)].copy_(gcl)
+                check(lib().ffsrl_grasp_nearest_envs(ptr(m.vertex), ptr(m.graspCandStartT), ptr(m.graspCand),
+                                                     ptr(m.laparoscopeTip), ptr(ln.gclamp_d), m.globalLaparoscopeDragLookupRadius,
+                                                     ptr(m.activeDragConstraint), ptr(ln.gids_d), len(trans), m.numEnvs, s))
+                for i in trans:
+                    self.actor_clamp[batch[i].actor] = batch[i].clamp
+            check(lib().ffsrl_batch_step_envs_lane(self.plan.handle, self.lanes.index(ln), ids.ctypes.data, n, 1, s))
+            check(lib().ffsrl_remap_envs(ptr(m.allVisPoint), ptr(m.vertex), ptr(m.pointToVertex),
+                                         ptr(m.envVisPointStartT), ptr(ln.ids_d), n, m.numEnvs, s))
+            check(lib().ffsrl_bvh_refit_fused_envs(C.byref(self.bvh.desc), ptr(m.allVisPoint), ptr(m.allVisFace),
+                                                   ptr(ln.ids_d), n, s))
+            rd = self.renderer._desc(m)
+            check(lib().ffsrl_render_fused_envs(C.byref(rd), C.byref(self.bvh.desc), ptr(ln.ids_d), n, s))
+            idl = ln.ids_d[:n].long()
+            ln.res_d[:n, :3] = m.laparoscopeTip[4 * idl + 3]
+            ln.res_d[:n, 3] = m.laparoscopeInCollision[idl].float()
+            ln.res_h[:n].copy_(ln.res_d[:n], non_blocking=True)
+            ln.event.record(ln.stream)
+        now = time.perf_counter()
+        for r in batch:
+            self.in_flight[r.actor] = True
+            self.last_used[r.actor] = now
+        ln.batch = batch
+        return n
+
+    def drain(self) -> list[Request]:
+        done = []
+        while any(ln.batch for ln in self.lanes):
+            done += self.poll()
+            time.sleep(0.0002)
+        return done
+
+    # ------------------------------------------------------------ load generator
+    def run_closed_loop(self, duration_s: float, think_hz: float = 60.0, seed: int = 0, warmup_s: float = 0.5,
+                        max_batch: int | None = None) -> dict:
+        """Every actor sends its next request an exponential think time (mean 1/think_hz)
+        after its previous result arrives; requests carry U[-0.1, 0.1] cm displacements
+        and a clamp flag that closes on the first request.  Returns latency percentiles
+        (arrival to result on the host) and served env-steps/s over ``duration_s``."""
+        rng = np.random.Generator(np.random.PCG64(seed))
+        A = self.num_actors
+        t0 = time.perf_counter()
+        nxt = t0 + rng.exponential(1.0 / think_hz, size=A)
+        waiting = np.zeros(A, dtype=bool)  # request outstanding
+        lat, served, t_meas = [], 0, t0 + warmup_s
+        t_end = t_meas + duration_s
+        ticks, batch_sizes = 0, []
+        while True:
+            now = time.perf_counter()
+            if now >= t_end:
+                break
+            due = np.nonzero((~waiting) & (nxt <= now))[0]
+            for a in due:
+                self.submit(Request(int(a), rng.uniform(-0.1, 0.1, size=3).astype(np.float32), 1, float(nxt[a])))
+            waiting[due] = True
+            for r in self.poll():
+                waiting[r.actor] = False
+                nxt[r.actor] = r.t_done + rng.exponential(1.0 / think_hz)
+                if r.t_arrival >= t_meas:
+                    lat.append(r.t_done - r.t_arrival)
+                    served += 1
+            b = self.launch(max_batch)
+            if b:
+                ticks += 1
+                batch_sizes.append(b)
+            else:
+                time.sleep(0.0001)
+        self.drain()
+        lat_ms = np.array(lat) * 1e3
+        return {"p50_ms": float(np.percentile(lat_ms, 50)) if len(lat_ms) else None,
+                "p99_ms": float(np.percentile(lat_ms, 99)) if len(lat_ms) else None,
+                "served_env_steps_per_s": served / duration_s, "requests": served, "ticks": ticks,
+                "mean_batch": float(np.mean(batch_sizes)) if batch_sizes else 0.0, "actors": A,
+                "slots": self.num_slots, "evictions": self.evictions, "budget_bytes_used": self.budget_used}

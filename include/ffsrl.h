@@ -166,6 +166,7 @@ typedef struct {
     float* rays;                     /* [N*(2R)^2*3] per-ray scratch, reference-shaped path only */
     float* ray_depth;                /* [N*(2R)^2]   per-ray scratch, reference-shaped path only */
     int32_t* error_flag;             /* [1] set to FFSRL_ERR_STACK_OVERFLOW by an overflowing ray */
+    const int32_t* env_point_start;  /* [N+1] each env's visual-point range (for the *_envs calls) */
 } ffsrl_render;
 
 /* ---- library ---------------------------------------------------------------- */
@@ -194,6 +195,11 @@ int32_t ffsrl_step_model_noalloc(const ffsrl_model* model, const ffsrl_params* p
 /* remapAToBKernel (utils.py:32-42): dst[map[2i]] = src[map[2i+1]] for i < count */
 int32_t ffsrl_remap(float* dst, const float* src, const int32_t* map, int32_t count, void* stream);
 
+/* remapAToBKernel for the listed envs only: the pairs of env e are map[2*point_start[e]
+   .. 2*point_start[e+1]) (device arrays). */
+int32_t ffsrl_remap_envs(float* dst, const float* src, const int32_t* map, const int32_t* point_start,
+                         const int32_t* env_ids, int32_t n, int32_t num_envs, void* stream);
+
 /* updateClampsDragKernel (modelDO.py:247-279): for every vertex of an env whose drag
    update flag is set, drag = (state==1 && |x - tip[4e+3]| < radius) ? 1 : 0 */
 int32_t ffsrl_update_clamps_drag(const float* positions, const int32_t* vertex_to_env, const float* laparoscope_tip,
@@ -208,6 +214,15 @@ int32_t ffsrl_force_clamps_drag(float* drag, int32_t vertex_id, const int32_t* e
 int32_t ffsrl_grasp_nearest(const float* positions, const int32_t* cand_start, const int32_t* cand,
                             const float* laparoscope_tip, const int32_t* clamp, float radius, float* drag,
                             int32_t num_envs, void* stream);
+/* ffsrl_grasp_nearest for the listed envs only: clamp[i] applies to env env_ids[i]
+   (device arrays); ids outside [0, num_envs) are skipped. */
+int32_t ffsrl_grasp_nearest_envs(const float* positions, const int32_t* cand_start, const int32_t* cand,
+                                 const float* laparoscope_tip, const int32_t* clamp, float radius, float* drag,
+                                 const int32_t* env_ids, int32_t n, int32_t num_envs, void* stream);
+/* Translate env env_ids[i]'s instrument by disp[3i..3i+2] (device arrays); ids outside
+   [0, num_envs) are skipped. */
+int32_t ffsrl_move_tool_envs(float* laparoscope_base, float* laparoscope_tip, const float* disp,
+                             const int32_t* env_ids, int32_t n, int32_t num_envs, void* stream);
 /* Rigidly translate each env's instrument (4 bases + 4 tips) by disp[3e..3e+2]. */
 int32_t ffsrl_move_tool(float* laparoscope_base, float* laparoscope_tip, const float* disp, int32_t num_envs,
                         void* stream);
@@ -225,6 +240,10 @@ int32_t ffsrl_bvh_refit_levels(const ffsrl_bvh* bvh, const float* vis_point, con
 /* Same result in one launch: one block per env walks its tree bottom-up. */
 int32_t ffsrl_bvh_refit_fused(const ffsrl_bvh* bvh, const float* vis_point, const int32_t* vis_face, void* stream);
 
+/* ffsrl_bvh_refit_fused for the listed envs only (device array of env ids). */
+int32_t ffsrl_bvh_refit_fused_envs(const ffsrl_bvh* bvh, const float* vis_point, const int32_t* vis_face,
+                                   const int32_t* env_ids, int32_t n, void* stream);
+
 /* ---- renderer ------------------------------------------------------------------- */
 /* renderFunctionNew (render.py:975-1022): zero, vertex_normal_sum (atomics), normalize,
    drawSimBVHKernelManyEnvs over (2R)^2 rays per env, downsample_kernel. */
@@ -232,6 +251,11 @@ int32_t ffsrl_render_reference(const ffsrl_render* r, const ffsrl_bvh* bvh, void
 /* Same images: normals by CSR gather in face order, one thread per ray with a register
    stack, the 2x2 downsample fused through warp shuffles. */
 int32_t ffsrl_render_fused(const ffsrl_render* r, const ffsrl_bvh* bvh, void* stream);
+
+/* ffsrl_render_fused for the listed envs only (device array of env ids): their vertex
+   normals (needs r->env_point_start) and images; other envs are not touched. */
+int32_t ffsrl_render_fused_envs(const ffsrl_render* r, const ffsrl_bvh* bvh, const int32_t* env_ids, int32_t n,
+                                void* stream);
 
 /* ---- batched step ------------------------------------------------------------------ */
 typedef struct ffsrl_batch ffsrl_batch;
@@ -251,8 +275,14 @@ int32_t ffsrl_batch_create(const ffsrl_model* host_model, const ffsrl_model* dev
 int32_t ffsrl_batch_destroy(ffsrl_batch* b);
 /* n_steps full steps of every env; same semantics as n_steps ffsrl_step_model calls. */
 int32_t ffsrl_batch_step(ffsrl_batch* b, int32_t n_steps, void* stream);
-/* Step only the listed envs (device array of env ids, count n). */
+/* Step only the listed envs (HOST array of env ids, count n).  A plan has 2 lanes, each
+   with its own work list, counters, scratch and class streams: steps of disjoint env
+   sets issued on different lanes (and streams) may run concurrently; the plain call
+   uses lane 0.  A lane's previous call must have finished reading its staging buffer,
+   which the call waits for. */
 int32_t ffsrl_batch_step_envs(ffsrl_batch* b, const int32_t* env_ids, int32_t n, int32_t n_steps, void* stream);
+int32_t ffsrl_batch_step_envs_lane(ffsrl_batch* b, int32_t lane, const int32_t* env_ids, int32_t n, int32_t n_steps,
+                                   void* stream);
 /* bytes of device memory the plan holds; per-env shared-memory class */
 int32_t ffsrl_batch_info(const ffsrl_batch* b, int64_t* device_bytes, int32_t* num_classes, int32_t* block_threads);
 /* Size classes (environments grouped by vertex count, one launch each): the class's
