@@ -39,12 +39,27 @@ __device__ __forceinline__ void refit_node(const ffsrl_bvh& b, const float* __re
             v3 pA = ld3(pts, faces[3 * f]), pB = ld3(pts, faces[3 * f + 1]), pC = ld3(pts, faces[3 * f + 2]);
             lo = vmin(pA, vmin(pB, vmin(pC, lo)));
             hi = vmax(pA, vmax(pB, vmax(pC, hi)));
+            if (b.tri_pos) {
+                float* q = b.tri_pos + 9 * (fofs + first + k);
+                q[0] = pA.x; q[1] = pA.y; q[2] = pA.z; q[3] = pB.x; q[4] = pB.y; q[5] = pB.z;
+                q[6] = pC.x; q[7] = pC.y; q[8] = pC.z;
+            }
+        }
+        if (b.node_box) {
+            float4* nb = reinterpret_cast<float4*>(b.node_box) + 2ll * (base + node);
+            nb[0] = make_float4(lo.x, lo.y, lo.z, __int_as_float(-1));
+            nb[1] = make_float4(hi.x, hi.y, hi.z, __int_as_float(first * 256 + (cnt < 255 ? cnt : 255)));
         }
     } else {
         v3 l0 = ld3(b.aabb_min, base + left), h0 = ld3(b.aabb_max, base + left);
         v3 l1 = ld3(b.aabb_min, base + left + 1), h1 = ld3(b.aabb_max, base + left + 1);
         lo = vmin(l0, l1);
         hi = vmax(h0, h1);
+        if (b.node_box) {
+            float4* nb = reinterpret_cast<float4*>(b.node_box) + 2ll * (base + node);
+            nb[0] = make_float4(lo.x, lo.y, lo.z, __int_as_float(left));
+            nb[1] = make_float4(hi.x, hi.y, hi.z, __int_as_float(0));
+        }
     }
     st3(b.aabb_min, base + node, lo);
     st3(b.aabb_max, base + node, hi);
@@ -196,6 +211,8 @@ __device__ __forceinline__ float moller_trumbore(v3 a, v3 b, v3 c, v3 ro, v3 rd,
 struct EnvView {
     const int* left; const int* first; const int* count; const int* tri;
     const float* amin; const float* amax;
+    const float4* box;   // packed node boxes of the env (or null)
+    const float* tpos;   // leaf triangles of the env in tri-map order (or null)
     long long fofs;
     int nn;  // nodes in the topology
 };
@@ -210,13 +227,72 @@ __device__ __forceinline__ EnvView env_view(const ffsrl_bvh& b, int e) {
     v.amin = b.aabb_min + 3 * base; v.amax = b.aabb_max + 3 * base;
     v.fofs = b.env_face_offset[e];
     v.nn = b.topo_node_offset[topo + 1] - n0;
+    v.box = b.node_box ? reinterpret_cast<const float4*>(b.node_box) + 2 * base : nullptr;
+    v.tpos = b.tri_pos ? b.tri_pos + 9 * v.fofs : nullptr;
     return v;
 }
 
 // meshQueryRayManyEnvs (render.py:411-498): nearest hit with 0 < t < tMin, stack LIFO
 // with the right child popped first.  Returns the global face id or -1.
+// Traversal over the packed copies written by the refit: two 16-byte loads per node and
+// contiguous leaf triangles; the same node order, tests and hits as query().
+__device__ int query_packed(const EnvView& ev, v3 ro, v3 rd, float& t_hit, v3& p_hit, int* err) {
+    int stack[kStackCap];
+    int count = 1;
+    stack[0] = 0;
+    float tMin = 1e6f;
+    int hit_tri = -1;
+    int visits = 0;
+    const v3 inv = mk(1.0f / rd.x, 1.0f / rd.y, 1.0f / rd.z);
+    while (count) {
+        int node = stack[--count];
+        if (++visits > ev.nn) {
+            atomicExch(err, FFSRL_ERR_STACK_OVERFLOW);
+            return -1;
+        }
+        const float4 a = __ldg(ev.box + 2 * node), c = __ldg(ev.box + 2 * node + 1);
+        if (node_hit(ro, rd, inv, mk(a.x, a.y, a.z), mk(c.x, c.y, c.z), tMin)) {
+            int left = __float_as_int(a.w);
+            if (left == -1) {
+                int fc = __float_as_int(c.w);
+                int first = fc >> 8, cnt = fc & 255;
+                if (cnt == 255) cnt = ev.count[node];
+                for (int k = 0; k < cnt; ++k) {
+                    const float* q = ev.tpos + 9ll * (first + k);
+                    v3 A = mk(__ldg(q), __ldg(q + 1), __ldg(q + 2));
+                    v3 B = mk(__ldg(q + 3), __ldg(q + 4), __ldg(q + 5));
+                    v3 C = mk(__ldg(q + 6), __ldg(q + 7), __ldg(q + 8));
+                    v3 p;
+                    float t = moller_trumbore(A, B, C, ro, rd, p);
+                    if (t < tMin && t > 0.0f) {
+                        tMin = t;
+                        hit_tri = (int)(ev.fofs + ev.tri[first + k]);
+                        t_hit = t;
+                        p_hit = p;
+                    }
+                }
+            } else {
+                if (left < 0 || left + 1 >= ev.nn) {
+                    atomicExch(err, FFSRL_ERR_INVALID_ARGUMENT);
+                    return -1;
+                }
+                if (count + 2 > kStackCap) {
+                    atomicExch(err, FFSRL_ERR_STACK_OVERFLOW);
+                    return -1;
+                }
+                stack[count] = left;
+                stack[count + 1] = left + 1;
+                count += 2;
+            }
+        }
+    }
+    if (tMin >= 1e6f) hit_tri = -1;
+    return hit_tri;
+}
+
 __device__ int query(const EnvView& ev, const float* __restrict__ pts, const int* __restrict__ faces, v3 ro, v3 rd,
                      float& t_hit, v3& p_hit, int* err) {
+    if (ev.box && ev.tpos) return query_packed(ev, ro, rd, t_hit, p_hit, err);
     int stack[kStackCap];
     int count = 1;
     stack[0] = 0;

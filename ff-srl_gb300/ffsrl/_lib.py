@@ -82,7 +82,7 @@ class Bvh(C.Structure):
         ("left_node", P), ("first_tri_id", P), ("tri_count", P), ("level", P), ("tri_id", P),
         ("aabb_min", P), ("aabb_max", P),
         ("total_env_nodes", I32), ("total_topology_nodes", I32), ("max_level", I32),
-        ("level_node", P), ("level_start", P), ("topo_level_offset", P),
+        ("level_node", P), ("level_start", P), ("topo_level_offset", P), ("node_box", P), ("tri_pos", P),
     ]
 
 

@@ -61,6 +61,10 @@ class SimBVH:
         self._assemble()
         if save:
             self.saveBVH(path)
+        if self.device.type == "cuda" and simModel.device.type == "cuda":
+            # boxes from the current visual points, as the build computed them, and the
+            # packed traversal copies that only the refit writes
+            self.refitBVH()
 
     # ------------------------------------------------------------------ build
     def _build(self) -> list[dict]:
@@ -142,6 +146,9 @@ class SimBVH:
         amax = np.concatenate([topos[k]["aabb_max"] for k in env_topo])
         self.aabbMin = torch.as_tensor(amin, dtype=torch.float32, device=dev).clone()
         self.aabbMax = torch.as_tensor(amax, dtype=torch.float32, device=dev).clone()
+        # traversal copies the refit writes: packed node boxes and leaf triangles in tri-map order
+        self.nodeBox = torch.zeros((len(amin), 8), dtype=torch.float32, device=dev)
+        self.triPos = torch.zeros((m.numAllVisFaces, 9), dtype=torch.float32, device=dev)
         self.numNodes = int(nn[0])
         self.numAllNodes = int(env_nodes.sum())
         self.maxLevel = int(max(t["max_level"] for t in topos))
@@ -154,7 +161,8 @@ class SimBVH:
                         ("left_node", self.leftNode), ("first_tri_id", self.firstTriId),
                         ("tri_count", self.triCount), ("level", self.level), ("tri_id", self.triId),
                         ("aabb_min", self.aabbMin), ("aabb_max", self.aabbMax), ("level_node", self.levelNode),
-                        ("level_start", self.levelStart), ("topo_level_offset", self.topoLevelOffset)):
+                        ("level_start", self.levelStart), ("topo_level_offset", self.topoLevelOffset),
+                        ("node_box", self.nodeBox), ("tri_pos", self.triPos)):
             setattr(d, name, ptr(t))
         d.total_env_nodes = self.numAllNodes
         d.total_topology_nodes = int(nn.sum())

@@ -138,6 +138,12 @@ typedef struct {
     const int32_t* level_node;       /* [total_topology_nodes] topology-local node ids */
     const int32_t* level_start;      /* [sum_m (topo_max_level[m] + 2)] absolute offsets */
     const int32_t* topo_level_offset;/* [M+1] */
+    /* optional traversal copies written by the refit (both or neither):
+       node_box[2n] = (min.xyz, leftNode), node_box[2n+1] = (max.xyz, first*256 + min(count,255))
+       per env node; tri_pos[9k..9k+8] = the three vertices of the k-th triangle in
+       tri-map order (k = env_face_offset[e] + position in the env's topology map) */
+    float* node_box;                 /* [8 * total_env_nodes] */
+    float* tri_pos;                  /* [9 * total env faces] */
 } ffsrl_bvh;
 
 /* ---- ray-cast renderer (render.py:826-1196) ------------------------------------ */
