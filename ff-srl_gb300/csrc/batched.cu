@@ -34,6 +34,7 @@
 #include <cstring>
 #include <string>
 #include <cmath>
+#include <unordered_map>
 #include "ffsrl_internal.h"
 
 namespace ffsrl {
@@ -90,7 +91,10 @@ template <> struct Store<double> {
     __device__ static double get(A a, const Fixed&) { return a; }
 };
 
-struct EnvRec { int v0, nv, t0, nt, e0, ne, f0, nf; };
+// v0/nv: the env's vertices in the model arrays; t0/e0/f0: its constraint tables, which
+// envs with identical tables share; mt0/me0: its tets/edges in the model arrays (for the
+// XPBD multipliers, which are per env)
+struct EnvRec { int v0, nv, t0, nt, e0, ne, f0, nf, mt0, me0; };
 
 // adds a correction vector to vertex i's accumulator; a component the fixed-point form
 // cannot carry (non-finite or out of range) raises `bad` so the env is reported diverged
@@ -120,8 +124,8 @@ template <class R> struct Dev {
     float* tet_lambda; float* edge_lambda;
     int* env_status;
     const int* cnt0;           // per-vertex static contribution count (global vertex index)
-    const int* tet_orig;       // model tet id of each (colour-ordered) record, for XPBD lambdas
-    const int* edge_orig;      // model edge id of each record
+    const int* tet_orig;       // env-local model tet id of each (colour-ordered) record, for XPBD lambdas
+    const int* edge_orig;      // env-local model edge id of each record
     Fixed fx;
     unsigned flags;
     int substeps, iterations;
@@ -325,9 +329,9 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                     xp[i] = S::make(x + v * dt, inv);
                 }
                 if (fl & FFSRL_VOLUME_XPBD)
-                    for (int t = tid; t < nt; t += BLOCK) D.tet_lambda[E.t0 + t] = 0.0f;
+                    for (int t = tid; t < nt; t += BLOCK) D.tet_lambda[E.mt0 + t] = 0.0f;
                 if (fl & FFSRL_DISTANCE_XPBD)
-                    for (int e = tid; e < ne; e += BLOCK) D.edge_lambda[E.e0 + e] = 0.0f;
+                    for (int e = tid; e < ne; e += BLOCK) D.edge_lambda[E.me0 + e] = 0.0f;
                 __syncthreads();
 
                 for (int it = 0; it < D.iterations; ++it) {
@@ -365,7 +369,7 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                                         }
                                         if (fl & FFSRL_VOLUME_XPBD) {
                                             R alpha = R(D.a_vol);
-                                            const int ot = __ldg(D.tet_orig + gt);
+                                            const int ot = E.mt0 + __ldg(D.tet_orig + gt);
                                             R lam = R(D.tet_lambda[ot]);
                                             R C = s6 / R(6) - R(__ldg(D.tet_vs + gt));
                                             R dl = -(C + alpha * lam) / (w + alpha);
@@ -471,7 +475,7 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                             }
                             if (fl & FFSRL_DISTANCE_XPBD) {
                                 R alpha = R(D.a_dist);
-                                const int oe = __ldg(D.edge_orig + ge);
+                                const int oe = E.me0 + __ldg(D.edge_orig + ge);
                                 R lam = R(D.edge_lambda[oe]);
                                 R dl = -(C + alpha * lam) / (w + alpha);
                                 D.edge_lambda[oe] = float(lam + dl);
@@ -877,7 +881,7 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
     std::vector<float2> edge_la(E);
     std::vector<uint2> tri_idx(F);
     for (int e = 0; e < N; ++e) {
-        EnvRec r;
+        EnvRec r{};
         r.v0 = hm->env_vertex_start[e]; r.nv = hm->env_vertex_start[e + 1] - r.v0;
         r.t0 = hm->env_tet_start[e]; r.nt = hm->env_tet_start[e + 1] - r.t0;
         r.e0 = hm->env_edge_start[e]; r.ne = hm->env_edge_start[e + 1] - r.e0;
@@ -1016,6 +1020,64 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
         permute(dmC, tet_orig); permute(tet_vs, tet_orig); permute(edge_idx, edge_orig); permute(edge_la, edge_orig);
     }
 
+    // ---- share identical constraint tables: envs of one mesh read the same records ----
+    {
+        for (int e = 0; e < N; ++e) {
+            env[e].mt0 = env[e].t0;
+            env[e].me0 = env[e].e0;
+            for (int j = 0; j < env[e].nt; ++j) tet_orig[env[e].t0 + j] -= env[e].t0;
+            for (int j = 0; j < env[e].ne; ++j) edge_orig[env[e].e0 + j] -= env[e].e0;
+        }
+        auto fnv = [](uint64_t h, const void* p, size_t n) {
+            const unsigned char* c = static_cast<const unsigned char*>(p);
+            for (size_t i = 0; i < n; ++i) { h ^= c[i]; h *= 1099511628211ull; }
+            return h;
+        };
+        auto same = [&](const EnvRec& a, const EnvRec& c) {
+            auto eq = [](const auto& v, int o1, int o2, int n) {
+                return n == 0 || v.empty() || std::memcmp(&v[o1], &v[o2], sizeof(v[0]) * (size_t)n) == 0;
+            };
+            return a.nv == c.nv && a.nt == c.nt && a.ne == c.ne && a.nf == c.nf &&
+                   eq(tet_idx, a.t0, c.t0, a.nt) && eq(tet_va, a.t0, c.t0, a.nt) && eq(dmA, a.t0, c.t0, a.nt) &&
+                   eq(dmB, a.t0, c.t0, a.nt) && eq(dmC, a.t0, c.t0, a.nt) && eq(tet_vs, a.t0, c.t0, a.nt) &&
+                   eq(tet_orig, a.t0, c.t0, a.nt) && eq(edge_idx, a.e0, c.e0, a.ne) && eq(edge_la, a.e0, c.e0, a.ne) &&
+                   eq(edge_orig, a.e0, c.e0, a.ne) && eq(tri_idx, a.f0, c.f0, a.nf);
+        };
+        std::vector<uint2> c_tet_idx; std::vector<float2> c_tet_va; std::vector<float4> c_dmA, c_dmB;
+        std::vector<float> c_dmC, c_tet_vs; std::vector<int> c_tet_orig, c_edge_orig;
+        std::vector<unsigned> c_edge_idx; std::vector<float2> c_edge_la; std::vector<uint2> c_tri_idx;
+        std::unordered_map<uint64_t, std::vector<int>> seen;
+        std::vector<EnvRec> out = env;
+        auto app = [](auto& dst, const auto& src, int o, int n) {
+            if (!src.empty()) dst.insert(dst.end(), src.begin() + o, src.begin() + o + n);
+        };
+        for (int e = 0; e < N; ++e) {
+            const EnvRec& r = env[e];
+            uint64_t h = fnv(1469598103934665603ull, &r.nv, sizeof(int) * 1);
+            h = fnv(h, &r.nt, sizeof(int));
+            h = fnv(h, &r.ne, sizeof(int));
+            if (r.nt) h = fnv(h, &tet_idx[r.t0], sizeof(uint2) * (size_t)r.nt);
+            int match = -1;
+            for (int c : seen[h])
+                if (same(r, env[c])) { match = c; break; }
+            if (match >= 0) {
+                out[e].t0 = out[match].t0; out[e].e0 = out[match].e0; out[e].f0 = out[match].f0;
+                continue;
+            }
+            seen[h].push_back(e);
+            out[e].t0 = (int)c_tet_idx.size(); out[e].e0 = (int)c_edge_idx.size(); out[e].f0 = (int)c_tri_idx.size();
+            app(c_tet_idx, tet_idx, r.t0, r.nt); app(c_tet_va, tet_va, r.t0, r.nt); app(c_dmA, dmA, r.t0, r.nt);
+            app(c_dmB, dmB, r.t0, r.nt); app(c_dmC, dmC, r.t0, r.nt); app(c_tet_vs, tet_vs, r.t0, r.nt);
+            app(c_tet_orig, tet_orig, r.t0, r.nt); app(c_edge_idx, edge_idx, r.e0, r.ne);
+            app(c_edge_la, edge_la, r.e0, r.ne); app(c_edge_orig, edge_orig, r.e0, r.ne);
+            app(c_tri_idx, tri_idx, r.f0, r.nf);
+        }
+        env = out;
+        tet_idx.swap(c_tet_idx); tet_va.swap(c_tet_va); dmA.swap(c_dmA); dmB.swap(c_dmB); dmC.swap(c_dmC);
+        tet_vs.swap(c_tet_vs); tet_orig.swap(c_tet_orig); edge_idx.swap(c_edge_idx); edge_la.swap(c_edge_la);
+        edge_orig.swap(c_edge_orig); tri_idx.swap(c_tri_idx);
+    }
+
     // size classes: mode by fit, then by vertex-count band
     const int bands[] = {192, 384, 768, 1536, 3072, 65536};
     b->env_class.assign(N, -1);
@@ -1071,18 +1133,18 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
 
     int32_t st = FFSRL_OK;
     if ((st = dalloc(b, &b->d_cnt0, (size_t)V)) || (st = upload(b->d_cnt0, cnt0)) ||
-        (st = dalloc(b, &b->d_tet_orig, (size_t)T)) || (st = upload(b->d_tet_orig, tet_orig)) ||
-        (st = dalloc(b, &b->d_edge_orig, (size_t)E)) || (st = upload(b->d_edge_orig, edge_orig)) ||
+        (st = dalloc(b, &b->d_tet_orig, tet_orig.size())) || (st = upload(b->d_tet_orig, tet_orig)) ||
+        (st = dalloc(b, &b->d_edge_orig, edge_orig.size())) || (st = upload(b->d_edge_orig, edge_orig)) ||
         (st = dalloc(b, &b->d_env, N)) || (st = upload(b->d_env, env)) ||
-        (st = dalloc(b, &b->d_tet_idx, T)) || (st = upload(b->d_tet_idx, tet_idx)) ||
-        (st = dalloc(b, &b->d_tet_va, T)) || (st = upload(b->d_tet_va, tet_va)) ||
+        (st = dalloc(b, &b->d_tet_idx, tet_idx.size())) || (st = upload(b->d_tet_idx, tet_idx)) ||
+        (st = dalloc(b, &b->d_tet_va, tet_va.size())) || (st = upload(b->d_tet_va, tet_va)) ||
         (st = dalloc(b, &b->d_dmA, dmA.size())) || (st = upload(b->d_dmA, dmA)) ||
         (st = dalloc(b, &b->d_dmB, dmB.size())) || (st = upload(b->d_dmB, dmB)) ||
         (st = dalloc(b, &b->d_dmC, dmC.size())) || (st = upload(b->d_dmC, dmC)) ||
         (st = dalloc(b, &b->d_tet_vs, tet_vs.size())) || (st = upload(b->d_tet_vs, tet_vs)) ||
-        (st = dalloc(b, &b->d_edge_idx, E)) || (st = upload(b->d_edge_idx, edge_idx)) ||
-        (st = dalloc(b, &b->d_edge_la, E)) || (st = upload(b->d_edge_la, edge_la)) ||
-        (st = dalloc(b, &b->d_tri_idx, F)) || (st = upload(b->d_tri_idx, tri_idx)) ||
+        (st = dalloc(b, &b->d_edge_idx, edge_idx.size())) || (st = upload(b->d_edge_idx, edge_idx)) ||
+        (st = dalloc(b, &b->d_edge_la, edge_la.size())) || (st = upload(b->d_edge_la, edge_la)) ||
+        (st = dalloc(b, &b->d_tri_idx, tri_idx.size())) || (st = upload(b->d_tri_idx, tri_idx)) ||
         (st = dalloc(b, &b->d_work, (size_t)N)) || (st = upload(b->d_work, b->work_host)) ||
         (st = dalloc(b, &b->d_status, (size_t)N)) ||
         (st = dalloc(b, &b->d_scratch, scratch_total * kLanes))) {

@@ -53,7 +53,7 @@ def test_beam_config0_100_steps(gpu, oracle_lib, batched):
 
 @pytest.mark.parametrize("batched", [False, True])
 def test_beam_xpbd_variant(gpu, oracle_lib, batched):
-    m, _ = sc.beam_model("cuda:0", xpbd=True)
+    m, _ = sc.beam_model("cuda:0", num_envs=3, xpbd=True)  # identical envs share tables, not multipliers
     x, o = run_pair(m, 100, batched)
     assert rel_err(x, o.a["vertex"], f"beam xpbd 100 steps batched={batched}") < POS_TOL
 
