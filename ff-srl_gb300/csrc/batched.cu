@@ -72,13 +72,13 @@ template <> struct Store<float> {
     typedef unsigned int A;
     __device__ static t3<float> pos(const P& p) { return T3<float>(p.x, p.y, p.z); }
     __device__ static P make(t3<float> v, float w) { return make_float4(v.x, v.y, v.z, w); }
-    // false when the scaled value is outside the per-contribution bound (or not finite)
-    __device__ static bool add(A* a, float v, const Fixed& fx) {
-        float q = v * fx.scale;
-        if (!(fabsf(q) < fx.bound)) return false;
-        atomicAdd(a, (unsigned)__float2int_rn(q));
-        return true;
+    // callers have checked the range (in_range) before adding
+    __device__ static void add(A* a, float v, const Fixed& fx) {
+        atomicAdd(a, (unsigned)__float2int_rn(v * fx.scale));
     }
+    // true when every |component| is below the per-term bound; the sum of magnitudes
+    // also carries NaN and infinity into the test
+    __device__ static bool in_range(float sum_abs, const Fixed& fx) { return sum_abs * fx.scale < fx.bound; }
     __device__ static float get(A a, const Fixed& fx) { return __int2float_rn((int)a) * fx.inv; }
 };
 struct __align__(32) dpos { double x, y, z, w; };
@@ -87,7 +87,8 @@ template <> struct Store<double> {
     typedef double A;
     __device__ static t3<double> pos(const P& p) { return T3<double>(p.x, p.y, p.z); }
     __device__ static P make(t3<double> v, double w) { P r; r.x = v.x; r.y = v.y; r.z = v.z; r.w = w; return r; }
-    __device__ static bool add(A* a, double v, const Fixed&) { atomicAdd(a, v); return isfinite(v); }
+    __device__ static void add(A* a, double v, const Fixed&) { atomicAdd(a, v); }
+    __device__ static bool in_range(double sum_abs, const Fixed&) { return sum_abs < 1.0e300; }
     __device__ static double get(A a, const Fixed&) { return a; }
 };
 
@@ -96,14 +97,26 @@ template <> struct Store<double> {
 // XPBD multipliers, which are per env)
 struct EnvRec { int v0, nv, t0, nt, e0, ne, f0, nf, mt0, me0; };
 
-// adds a correction vector to vertex i's accumulator; a component the fixed-point form
-// cannot carry (non-finite or out of range) raises `bad` so the env is reported diverged
+template <class R> __device__ __forceinline__ R abs_sum(t3<R> d) { return fabs(d.x) + fabs(d.y) + fabs(d.z); }
+
+// adds correction vectors to vertices' accumulators; a group whose magnitudes the
+// fixed-point form cannot carry (non-finite or out of range) is dropped and raises `bad`
+// so the env is reported diverged
 template <class R> __device__ __forceinline__ void add3(typename Store<R>::A* acc, int i, t3<R> d, bool& bad,
                                                         const Fixed& fx) {
-    bool ok = Store<R>::add(acc + 3 * i, d.x, fx);
-    ok &= Store<R>::add(acc + 3 * i + 1, d.y, fx);
-    ok &= Store<R>::add(acc + 3 * i + 2, d.z, fx);
-    bad |= !ok;
+    if (!Store<R>::in_range(abs_sum(d), fx)) { bad = true; return; }
+    Store<R>::add(acc + 3 * i, d.x, fx);
+    Store<R>::add(acc + 3 * i + 1, d.y, fx);
+    Store<R>::add(acc + 3 * i + 2, d.z, fx);
+}
+template <class R> __device__ __forceinline__ void add3x4(typename Store<R>::A* acc, int ia, int ib, int ic, int id,
+                                                          t3<R> dA, t3<R> dB, t3<R> dC, t3<R> dD, bool& bad,
+                                                          const Fixed& fx) {
+    if (!Store<R>::in_range(abs_sum(dA) + abs_sum(dB) + abs_sum(dC) + abs_sum(dD), fx)) { bad = true; return; }
+    Store<R>::add(acc + 3 * ia, dA.x, fx); Store<R>::add(acc + 3 * ia + 1, dA.y, fx); Store<R>::add(acc + 3 * ia + 2, dA.z, fx);
+    Store<R>::add(acc + 3 * ib, dB.x, fx); Store<R>::add(acc + 3 * ib + 1, dB.y, fx); Store<R>::add(acc + 3 * ib + 2, dB.z, fx);
+    Store<R>::add(acc + 3 * ic, dC.x, fx); Store<R>::add(acc + 3 * ic + 1, dC.y, fx); Store<R>::add(acc + 3 * ic + 2, dC.z, fx);
+    Store<R>::add(acc + 3 * id, dD.x, fx); Store<R>::add(acc + 3 * id + 1, dD.y, fx); Store<R>::add(acc + 3 * id + 2, dD.z, fx);
 }
 
 template <class R> struct Dev {
@@ -338,7 +351,7 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                     // ---- tet constraints: volume, XPBD volume, Neo-Hookean ----
                     if (fl & (FFSRL_VOLUME | FFSRL_VOLUME_XPBD | FFSRL_NEOHOOKEAN)) {
                         for (int t = tid; t < nt; t += BLOCK) {
-                            const long long gt = (long long)E.t0 + t;
+                            const int gt = E.t0 + t;
                             const uint2 ix = __ldg(D.tet_idx + gt);
                             const int ia = ix.x & 0xffff, ib = ix.x >> 16, ic = ix.y & 0xffff, id = ix.y >> 16;
                             const P PA = xp[ia], PB = xp[ib], PC = xp[ic], PD = xp[id];
@@ -398,29 +411,21 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                                 t3<R> g0 = -g1 - g2 - g3;
                                 R detF = dot(f0, c0);
                                 R C = detF - R(1) - nh_off;
-                                R w = R(0), l;
-                                l = length(g0); w += l * l * mA;
-                                l = length(g1); w += l * l * mB;
-                                l = length(g2); w += l * l * mC;
-                                l = length(g3); w += l * l * mD;
+                                // |g|^2 as dot(g, g) (the reference squares length(g); equal up to rounding)
+                                R w = dot(g0, g0) * mA + dot(g1, g1) * mB + dot(g2, g2) * mC + dot(g3, g3) * mD;
                                 if (w < R(BEPS)) {
                                     if (anym) ++skip;
                                 } else {
                                     R alpha = nh_uH / rv;
                                     R dl = -C / (w + alpha);
                                     t3<R> hA = g0 * dl * mA, hB = g1 * dl * mB, hC = g2 * dl * mC, hD = g3 * dl * mD;
-                                    R l0 = length(f0), l1 = length(f1), l2 = length(f2);
-                                    R rs = sqrt(l0 * l0 + l1 * l1 + l2 * l2);
+                                    R rs = sqrt(dot(f0, f0) + dot(f1, f1) + dot(f2, f2));
                                     R rsi = R(1) / rs;
                                     g1 = (f0 * d00 + f1 * d01 + f2 * d02) * rsi;
                                     g2 = (f0 * d10 + f1 * d11 + f2 * d12) * rsi;
                                     g3 = (f0 * d20 + f1 * d21 + f2 * d22) * rsi;
                                     g0 = -g1 - g2 - g3;
-                                    w = R(0);
-                                    l = length(g0); w += l * l * mA;
-                                    l = length(g1); w += l * l * mB;
-                                    l = length(g2); w += l * l * mC;
-                                    l = length(g3); w += l * l * mD;
+                                    w = dot(g0, g0) * mA + dot(g1, g1) * mB + dot(g2, g2) * mC + dot(g3, g3) * mD;
                                     if (w < R(BEPS)) {
                                         if (anym) ++skip;
                                     } else {
@@ -433,10 +438,7 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                                     }
                                 }
                             }
-                            if (k) {
-                                add3<R>(acc, ia, dA, bad, fx); add3<R>(acc, ib, dB, bad, fx);
-                                add3<R>(acc, ic, dC, bad, fx); add3<R>(acc, id, dD, bad, fx);
-                            }
+                            if (k) add3x4<R>(acc, ia, ib, ic, id, dA, dB, dC, dD, bad, fx);
                             if (skip) {
                                 atomicSub(cnt + ia, skip); atomicSub(cnt + ib, skip);
                                 atomicSub(cnt + ic, skip); atomicSub(cnt + id, skip);
@@ -447,7 +449,7 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                     // ---- edge constraints: distance (integrator.py:65-109), XPBD (:191-240) ----
                     if (fl & (FFSRL_DISTANCE | FFSRL_DISTANCE_XPBD)) {
                         for (int e = tid; e < ne; e += BLOCK) {
-                            const long long ge = (long long)E.e0 + e;
+                            const int ge = E.e0 + e;
                             const unsigned ix = __ldg(D.edge_idx + ge);
                             const int ia = ix & 0xffff, ib = ix >> 16;
                             const float2 la = __ldg(D.edge_la + ge);

@@ -201,3 +201,34 @@ def test_plain_clamp_kernels(gpu):
     assert float(m.activeDragConstraint[m.envSlice(1)].abs().sum()) == 0.0
     m.forceLaparoscopeClampVertex(7, torch.tensor([0, 1], device="cuda:0"), on=1.0)
     assert float(m.activeDragConstraint[m.envVertexStart[1] + 7]) == 1.0
+
+
+def test_liver_config1_mesh_global_accumulators(gpu, oracle_lib):
+    # the 12/8/6 cm ellipsoid (11,102 vertices) does not fit a block's shared memory
+    # whole: positions stay in shared memory, sums go to global scratch (mode 1)
+    m, meshes = sc.liver_model("cuda:0", 2)
+    assert m.numVertices == 2 * 11102
+    m.graspNearest(torch.ones(2, dtype=torch.int32, device="cuda:0"), radius=0.3)
+    integ = SimIntegratorDO("cuda:0")
+    info = integ.plan(m).info()
+    o = oracle_for(m)
+    integ.stepModel(m, 2)
+    torch.cuda.synchronize()
+    o.step(2)
+    from ffsrl import _lib as LL
+    import ctypes as C
+    mode = C.c_int32()
+    LL.check(LL.lib().ffsrl_batch_class_info(integ.plan(m).handle, 0, None, C.byref(mode), None, None))
+    assert mode.value == 1, info
+    assert rel_err(m.vertex.cpu().numpy(), o.a["vertex"], "liver config-1 mesh (mode 1)") < POS_TOL
+
+
+def test_precision_float32_vs_float64(gpu):
+    # config 3's stiff variant (nu 0.49, 16 substeps x 50 iterations) on the full liver
+    # mesh: float32 (mode 1) against the float64 build of the same kernel (mode 2)
+    from ffsrl.precision import precision_report
+    rep = precision_report([mg.ellipsoid()], steps=3)
+    print("[precision]", rep)
+    assert rep["finite"]
+    assert rep["max_pos_err_rel"] < POS_TOL
+    assert rep["volume_err_f64"]["max"] < 0.5
