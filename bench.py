@@ -146,15 +146,23 @@ def build_workload(device, envs, seed):
     return m, meshes, bvh, r
 
 
-def cpu_sample(meshes, threads, n_env=16, seed=0):
-    """Oracle (C++ restatement) env-steps/s on a bounded sample of the workload."""
+def cpu_sample(meshes, threads, n_env=16):
+    """Oracle (C++ restatement) env-steps/s on a bounded sample of the workload: the full
+    env-step of ``n_env`` envs -- solve, remap, BVH refit and the RES x RES ray-cast --
+    with envs spread over ``threads`` host threads. Set-up is outside the timed call."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
-    from ffsrl import scenarios as sc
+    from ffsrl import SimBVH, WarpRaycastRendererDO, scenarios as sc
     m, _ = sc.liver_model("cpu", n_env, meshes=meshes[:n_env])
-    o = oracle.OracleSim(m)
+    bvh = SimBVH("cpu", m)
+    ap = sc.fov_aperture(60.0)
+    r = WarpRaycastRendererDO("cpu", m, resolution=RES, mode="headless", verticalAperture=ap,
+                              horizontalAperture=ap, lightPos=(0.3, 1.0, 0.5), lightIntensity=0.8)
+    pos, rot = sc.env_cameras(meshes[:n_env], seed=1)
+    r.setCameras(pos, rot)
+    scene = oracle.OracleScene(m, bvh, r)
     t0 = time.perf_counter()
-    o.step(1, threads=threads)
+    scene.step(threads=threads)
     dt = time.perf_counter() - t0
     return n_env / dt, dt
 
@@ -179,7 +187,8 @@ def reference_arm(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
             "config": config(args.envs, world) | {"sample": f"{sample} envs x 1 step per timed step"},
             "cpu_baseline": {"value": v, "unit": "env-steps/s", "cores": threads, "kind": "port",
-                             "sample": f"{sample} envs of the same pool, 1 step (8x10 solve only, no render)"},
+                             "sample": f"{sample} envs of the same pool, 1 full env-step each (8x10 solve, refit, "
+                                       f"{RES}x{RES} ray-cast), OpenMP over envs"},
             "e2e": {"value": v, "unit": "env-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -199,6 +208,7 @@ def main():
     envs = args.envs
     m, meshes, bvh, r = build_workload(device, envs, seed=rank)
     from ffsrl import SimIntegratorDO, scenarios as sc, _lib as L
+    from ffsrl.shard import max_over_ranks
     integ = SimIntegratorDO(device, autotune=True)
     plan = integ.plan(m)
     n_cls = plan.info()["num_classes"]
@@ -230,10 +240,7 @@ def main():
     barrier()
     per = [evs[k].elapsed_time(evs[k + 1]) for k in range(K)]
     total_ms = evs[0].elapsed_time(evs[K])
-    if world > 1:
-        t = torch.tensor([total_ms], device=device)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, device=device)
     r.checkErrors()
     status = integ.envStatus(m)
     value = envs * world * K / (total_ms / 1000.0)
@@ -331,8 +338,10 @@ def main():
             threads = os.cpu_count() or 1
             v, dt = cpu_sample(meshes, threads, n_env=32)
             cpu = {"value": v, "unit": "env-steps/s", "cores": threads, "kind": "port",
-                   "sample": "32 envs of the same pool, 1 step (8x10 solve only, no render), oracle restatement"}
-        launches = K * (n_cls + 4)
+                   "sample": f"32 envs of the same pool, 1 full env-step (8x10 solve, refit, {RES}x{RES} ray-cast), "
+                             "oracle restatement, OpenMP over envs"}
+        # per step: move_tool, one launch per size class, remap, fused refit, normal gather, rays
+        launches = K * (n_cls + 5)
         line = {"metric": METRIC, "value": value, "unit": "env-steps/s", "n_gpus": world, "steps": K,
                 "warmup": W, "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded meshes and random-walk actions)",

@@ -1,0 +1,74 @@
+"""Small, self-ending workloads for profiling one kernel under ncu.
+
+Each case builds its inputs, runs the kernel of interest once (plus whatever set-up
+launches it needs) and exits. The inputs are larger than L2 but hold at most a few GB on
+the device, so a capture of one to six launches ends within a minute or two.
+
+    python -m ffsrl.profile_cases step_mixed [envs]   # every size-class launch of one batched step
+    python -m ffsrl.profile_cases step_big            # one size class of large envs (12k-20k tets)
+    python -m ffsrl.profile_cases render              # refit + ray-cast of 256 envs at 128x128
+
+The step cases draw their meshes from the same seeded 64-mesh pool as the 4096-env
+throughput workload, so per-env-step figures scale to it.
+"""
+
+from __future__ import annotations
+
+import sys
+
+import torch
+
+from . import SimBVH, SimIntegratorDO, WarpRaycastRendererDO
+from . import scenarios as sc
+
+
+def step_mixed(envs: int = 512, device: str = "cuda:0") -> None:
+    meshes, _ = sc.mixed_meshes(envs, pool_size=64, seed=0)
+    m, _ = sc.liver_model(device, envs, meshes=meshes)
+    m.graspNearest(torch.ones(envs, dtype=torch.int32, device=device), radius=0.3)
+    integ = SimIntegratorDO(device, autotune=True)
+    p = integ.plan(m)
+    print(p.info(), integ.tuning)
+    p.step(1)
+    torch.cuda.synchronize()
+
+
+def step_big(device: str = "cuda:0") -> None:
+    meshes, _ = sc.mixed_meshes(304, pool_size=8, seed=3, t_lo=12000, t_hi=20000)
+    m, _ = sc.liver_model(device, 304, meshes=meshes)
+    m.graspNearest(torch.ones(304, dtype=torch.int32, device=device), radius=0.3)
+    p = SimIntegratorDO(device).plan(m)
+    print(p.info())
+    p.step(1)
+    torch.cuda.synchronize()
+
+
+def render(envs: int = 256, device: str = "cuda:0") -> None:
+    meshes, _ = sc.mixed_meshes(envs, pool_size=16, seed=0)
+    m, _ = sc.liver_model(device, envs, meshes=meshes)
+    bvh = SimBVH(device, m)
+    ap = sc.fov_aperture(60.0)
+    r = WarpRaycastRendererDO(device, m, resolution=128, mode="headless", verticalAperture=ap,
+                              horizontalAperture=ap)
+    pos, rot = sc.env_cameras(meshes, seed=1)
+    r.setCameras(pos, rot)
+    bvh.refitBVH()
+    r.renderNew(bvh, m)
+    torch.cuda.synchronize()
+
+
+def main(argv: list[str]) -> None:
+    case = argv[0] if argv else "step_mixed"
+    if case == "step_mixed":
+        step_mixed(int(argv[1]) if len(argv) > 1 else 512)
+    elif case == "step_big":
+        step_big()
+    elif case == "render":
+        render()
+    else:
+        raise SystemExit(f"unknown case {case!r}: step_mixed, step_big or render")
+    print("ok")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

@@ -91,7 +91,7 @@ class _Lane:
 
 class EnvServer:
     def __init__(self, pool: list, actor_mesh, device="cuda:0", hbm_budget_bytes: float = 60e9, resolution: int = 128,
-                 lanes: int = 2, seed: int = 0, autotune: bool = False, **model_kw):
+                 lanes: int = 2, seed: int = 0, autotune: bool = False, block_threads: int = 0, **model_kw):
         self.device = torch.device(device)
         self.pool = pool
         self.actor_mesh = np.asarray(actor_mesh, dtype=np.int64)
@@ -106,7 +106,7 @@ class EnvServer:
         self.budget_used = float((k * per).sum())
         meshes = [pool[m] for m in self.slot_mesh]
         self.model, _ = sc.liver_model(device, self.num_slots, meshes=meshes, **model_kw)
-        self.integ = SimIntegratorDO(device, autotune=autotune)
+        self.integ = SimIntegratorDO(device, blockThreads=block_threads, autotune=autotune)
         self.plan = self.integ.plan(self.model)
         self.bvh = SimBVH(device, self.model)
         ap = sc.fov_aperture(60.0)
@@ -138,6 +138,9 @@ class EnvServer:
                             event=torch.cuda.Event())
                       for _ in range(lanes)]
         self.pending: list[Request] = []
+        # per-tick device timing (start/end events on the lane stream), kept when enabled
+        self.profile_ticks = False
+        self.tick_log: list[tuple] = []
         torch.cuda.synchronize()
 
     # ------------------------------------------------------------ admission
@@ -239,7 +242,11 @@ class EnvServer:
         trans = [i for i, r in enumerate(batch) if r.clamp != self.actor_clamp[r.actor]]
         m = self.model
         s = L.stream_handle(ln.stream)
+        t_host = time.perf_counter()
         with torch.cuda.stream(ln.stream):
+            if self.profile_ticks:
+                ev0 = torch.cuda.Event(enable_timing=True)
+                ev0.record(ln.stream)
             ln.ids_h[:n].copy_(torch.from_numpy(ids))
             ln.act_h[:n].copy_(torch.from_numpy(acts))
             ln.ids_d[:n].copy_(ln.ids_h[:n], non_blocking=True)
@@ -270,7 +277,12 @@ class EnvServer:
             ln.res_d[:n, 3] = m.laparoscopeInCollision[idl].float()
             ln.res_h[:n].copy_(ln.res_d[:n], non_blocking=True)
             ln.event.record(ln.stream)
+            if self.profile_ticks:
+                ev1 = torch.cuda.Event(enable_timing=True)
+                ev1.record(ln.stream)
         now = time.perf_counter()
+        if self.profile_ticks:
+            self.tick_log.append((self.lanes.index(ln), n, ev0, ev1, (now - t_host) * 1e3))
         for r in batch:
             self.in_flight[r.actor] = True
             self.last_used[r.actor] = now
@@ -320,9 +332,25 @@ class EnvServer:
             else:
                 time.sleep(0.0001)
         self.drain()
+        torch.cuda.synchronize()
         lat_ms = np.array(lat) * 1e3
+        prof = None
+        if self.profile_ticks and self.tick_log:
+            first = self.tick_log[0][2]
+            spans = [(ln, n, first.elapsed_time(a), first.elapsed_time(b), h) for ln, n, a, b, h in self.tick_log]
+            dev = np.array([b - a for _, _, a, b, _ in spans])
+            ends = max(b for _, _, _, b, _ in spans)
+            busy = np.zeros(int(ends) + 1)
+            for _, _, a, b, _ in spans:
+                busy[int(a):int(b) + 1] += 1
+            prof = {"tick_device_ms_p50": float(np.median(dev)), "tick_device_ms_mean": float(dev.mean()),
+                    "host_launch_ms_mean": float(np.mean([h for *_, h in spans])),
+                    "frac_time_two_lanes_busy": float((busy >= 2).mean()), "frac_time_idle": float((busy == 0).mean()),
+                    "ticks": [(ln, n, round(a, 2), round(b, 2), round(h, 2)) for ln, n, a, b, h in spans[-40:]]}
+            self.tick_log = []
         return {"p50_ms": float(np.percentile(lat_ms, 50)) if len(lat_ms) else None,
                 "p99_ms": float(np.percentile(lat_ms, 99)) if len(lat_ms) else None,
                 "served_env_steps_per_s": served / duration_s, "requests": served, "ticks": ticks,
                 "mean_batch": float(np.mean(batch_sizes)) if batch_sizes else 0.0, "actors": A,
-                "slots": self.num_slots, "evictions": self.evictions, "budget_bytes_used": self.budget_used}
+                "slots": self.num_slots, "evictions": self.evictions, "budget_bytes_used": self.budget_used,
+                **({"tick_profile": prof} if prof else {})}

@@ -508,38 +508,47 @@ template <class R> int run_steps(const ffsrl_model* m, const ffsrl_params* p, in
 
 // ---------------------------------------------------------------------------------
 // BVH refit (bvh.py:30-104), all levels deepest first.
+void refit_node_level(const ffsrl_bvh* b, const float* pts, const int32_t* faces, int e, int L);
+
 void refit(const ffsrl_bvh* b, const float* pts, const int32_t* faces) {
-    for (int L = b->max_level; L >= 0; --L) {
-        for (int e = 0; e < b->num_envs; ++e) {
-            int topo = b->env_topology[e];
-            int n0 = b->topo_node_offset[topo], n1 = b->topo_node_offset[topo + 1];
-            int t0 = b->topo_tri_offset[topo];
-            int base = b->env_node_offset[e];
-            for (int n = 0; n < n1 - n0; ++n) {
-                if (b->level[n0 + n] != L) continue;
-                int left = b->left_node[n0 + n];
-                V3<float> lo, hi;
-                if (left < 0) {
-                    lo = mk<float>(1e6f, 1e6f, 1e6f);
-                    hi = mk<float>(-1e6f, -1e6f, -1e6f);
-                    int first = b->first_tri_id[n0 + n];
-                    for (int k = 0; k < b->tri_count[n0 + n]; ++k) {
-                        int64_t f = int64_t(b->env_face_offset[e]) + b->tri_id[t0 + first + k];
-                        V3<float> pA = ld3<float>(pts, faces[3 * f]), pB = ld3<float>(pts, faces[3 * f + 1]),
-                                  pC = ld3<float>(pts, faces[3 * f + 2]);
-                        lo = vmin(pA, vmin(pB, vmin(pC, lo)));
-                        hi = vmax(pA, vmax(pB, vmax(pC, hi)));
-                    }
-                } else {
-                    V3<float> l0 = ld3<float>(b->aabb_min, base + left), h0 = ld3<float>(b->aabb_max, base + left);
-                    V3<float> l1 = ld3<float>(b->aabb_min, base + left + 1), h1 = ld3<float>(b->aabb_max, base + left + 1);
-                    lo = vmin(l0, l1);
-                    hi = vmax(h0, h1);
-                }
-                st3(b->aabb_min, base + n, lo);
-                st3(b->aabb_max, base + n, hi);
+    for (int L = b->max_level; L >= 0; --L)
+        for (int e = 0; e < b->num_envs; ++e) refit_node_level(b, pts, faces, e, L);
+}
+
+// one env's tree, all levels deepest first
+void refit_env(const ffsrl_bvh* b, const float* pts, const int32_t* faces, int e) {
+    for (int L = b->max_level; L >= 0; --L) refit_node_level(b, pts, faces, e, L);
+}
+
+// the nodes of env e at level L
+void refit_node_level(const ffsrl_bvh* b, const float* pts, const int32_t* faces, int e, int L) {
+    int topo = b->env_topology[e];
+    int n0 = b->topo_node_offset[topo], n1 = b->topo_node_offset[topo + 1];
+    int t0 = b->topo_tri_offset[topo];
+    int base = b->env_node_offset[e];
+    for (int n = 0; n < n1 - n0; ++n) {
+        if (b->level[n0 + n] != L) continue;
+        int left = b->left_node[n0 + n];
+        V3<float> lo, hi;
+        if (left < 0) {
+            lo = mk<float>(1e6f, 1e6f, 1e6f);
+            hi = mk<float>(-1e6f, -1e6f, -1e6f);
+            int first = b->first_tri_id[n0 + n];
+            for (int k = 0; k < b->tri_count[n0 + n]; ++k) {
+                int64_t f = int64_t(b->env_face_offset[e]) + b->tri_id[t0 + first + k];
+                V3<float> pA = ld3<float>(pts, faces[3 * f]), pB = ld3<float>(pts, faces[3 * f + 1]),
+                          pC = ld3<float>(pts, faces[3 * f + 2]);
+                lo = vmin(pA, vmin(pB, vmin(pC, lo)));
+                hi = vmax(pA, vmax(pB, vmax(pC, hi)));
             }
+        } else {
+            V3<float> l0 = ld3<float>(b->aabb_min, base + left), h0 = ld3<float>(b->aabb_max, base + left);
+            V3<float> l1 = ld3<float>(b->aabb_min, base + left + 1), h1 = ld3<float>(b->aabb_max, base + left + 1);
+            lo = vmin(l0, l1);
+            hi = vmax(h0, h1);
         }
+        st3(b->aabb_min, base + n, lo);
+        st3(b->aabb_max, base + n, hi);
     }
 }
 
@@ -635,7 +644,12 @@ int query(const ffsrl_bvh* b, const ffsrl_render* r, int e, V3<float> ro, V3<flo
     return 0;
 }
 
-int render(const ffsrl_render* r, const ffsrl_bvh* b, int stack_cap) {
+int render_env(const ffsrl_render* r, const ffsrl_bvh* b, int stack_cap, int e, const float* nrmp,
+               std::vector<float>& ray, std::vector<float>& rdep);
+
+// Normals serially in face order, then each env's rays; `threads` > 1 spreads the envs
+// over OpenMP threads (envs share nothing, so the images are the same).
+int render(const ffsrl_render* r, const ffsrl_bvh* b, int stack_cap, int threads = 1) {
     int64_t P = r->num_vis_points;
     std::vector<float> nsum(3 * P, 0.0f);
     for (int64_t f = 0; f < r->num_vis_faces; ++f) {  // vertex_normal_sum_kernel, serial order
@@ -649,8 +663,31 @@ int render(const ffsrl_render* r, const ffsrl_bvh* b, int stack_cap) {
     if (r->vertex_normal) std::copy(nrm.begin(), nrm.end(), r->vertex_normal);
 
     const int R = r->resolution, W = 2 * R, H = 2 * R;
-    std::vector<float> ray(3 * (size_t)W * H), rdep((size_t)W * H);
-    for (int e = 0; e < r->num_envs; ++e) {
+    int status = 0;
+    if (threads <= 1) {
+        std::vector<float> ray(3 * (size_t)W * H), rdep((size_t)W * H);
+        for (int e = 0; e < r->num_envs && !status; ++e) status = render_env(r, b, stack_cap, e, nrm.data(), ray, rdep);
+        return status;
+    }
+#pragma omp parallel num_threads(threads)
+    {
+        std::vector<float> ray(3 * (size_t)W * H), rdep((size_t)W * H);
+#pragma omp for schedule(dynamic, 1)
+        for (int e = 0; e < r->num_envs; ++e) {
+            int st = render_env(r, b, stack_cap, e, nrm.data(), ray, rdep);
+            if (st) {
+#pragma omp critical
+                status = st;
+            }
+        }
+    }
+    return status;
+}
+
+int render_env(const ffsrl_render* r, const ffsrl_bvh* b, int stack_cap, int e, const float* nrmp,
+               std::vector<float>& ray, std::vector<float>& rdep) {
+    const int R = r->resolution, W = 2 * R, H = 2 * R;
+    {
         int cam = r->num_cameras > 1 ? e : 0;
         V3<float> ro = ld3<float>(r->camera_pos, cam);
         const float* q = r->camera_rot + 4 * cam;
@@ -673,7 +710,7 @@ int render(const ffsrl_render* r, const ffsrl_bvh* b, int stack_cap) {
                 float w = length(cross(bb - a, p - a)) / area;
                 float v = length(cross(p - a, c - a)) / area;
                 float u = 1.0f - w - v;
-                V3<float> n = u * ld3<float>(nrm.data(), i) + v * ld3<float>(nrm.data(), j) + w * ld3<float>(nrm.data(), k);
+                V3<float> n = u * ld3<float>(nrmp, i) + v * ld3<float>(nrmp, j) + w * ld3<float>(nrmp, k);
                 V3<float> vc = (ld3<float>(r->vis_point_color, i) + ld3<float>(r->vis_point_color, j) +
                                 ld3<float>(r->vis_point_color, k)) / 3.0f;
                 float lam = 0.0f;
@@ -738,5 +775,17 @@ void oracle_remap(float* dst, const float* src, const int32_t* map, int32_t coun
 void oracle_refit(const ffsrl_bvh* b, const float* pts, const int32_t* faces) { refit(b, pts, faces); }
 
 int oracle_render(const ffsrl_render* r, const ffsrl_bvh* b, int stack_cap) { return render(r, b, stack_cap); }
+
+// Same images as oracle_render, envs spread over `threads` host threads (CPU timing).
+int oracle_render_mt(const ffsrl_render* r, const ffsrl_bvh* b, int stack_cap, int threads) {
+    return render(r, b, stack_cap, threads);
+}
+
+// Same boxes as oracle_refit, envs spread over `threads` host threads: each env's tree
+// is refit bottom-up on its own (the levels of one env stay in order).
+void oracle_refit_mt(const ffsrl_bvh* b, const float* pts, const int32_t* faces, int threads) {
+#pragma omp parallel for schedule(dynamic, 4) num_threads(threads)
+    for (int e = 0; e < b->num_envs; ++e) refit_env(b, pts, faces, e);
+}
 
 }  // extern "C"

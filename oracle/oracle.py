@@ -50,7 +50,9 @@ def lib() -> C.CDLL:
         _lib.oracle_remap.argtypes = [P, P, P, C.c_int32]
         _lib.oracle_refit.argtypes = [C.POINTER(L.Bvh), P, P]
         _lib.oracle_render.argtypes = [C.POINTER(L.Render), C.POINTER(L.Bvh), C.c_int]
-        for f in ("oracle_step_f32", "oracle_step_f64", "oracle_render"):
+        _lib.oracle_refit_mt.argtypes = [C.POINTER(L.Bvh), P, P, C.c_int]
+        _lib.oracle_render_mt.argtypes = [C.POINTER(L.Render), C.POINTER(L.Bvh), C.c_int, C.c_int]
+        for f in ("oracle_step_f32", "oracle_step_f64", "oracle_render", "oracle_render_mt"):
             getattr(_lib, f).restype = C.c_int
     return _lib
 
@@ -149,14 +151,8 @@ def refit(bvh, vis_points: np.ndarray, vis_face: np.ndarray) -> tuple[np.ndarray
     return arrays["aabb_min"], arrays["aabb_max"]
 
 
-def render(renderer, bvh, vis_points: np.ndarray, aabb: tuple | None = None, stack_cap: int = 64):
-    """Oracle images (colour [N,R,R,3], depth [N,R,R]) for a WarpRaycastRendererDO's settings."""
+def _render_desc(renderer, vis_points: np.ndarray):
     m = renderer.simModel
-    arrays = {}
-    d = bvh_desc(bvh, arrays)
-    if aabb is not None:
-        arrays["aabb_min"][:] = aabb[0]
-        arrays["aabb_max"][:] = aabb[1]
     N, R = renderer.numEnvs, renderer.width
     a = {
         "vis_point": np.ascontiguousarray(vis_points, dtype=np.float32),
@@ -178,7 +174,47 @@ def render(renderer, bvh, vis_points: np.ndarray, aabb: tuple | None = None, sta
     r.num_cameras = a["camera_pos"].shape[0]
     r.camera_tan, r.camera_aspect = renderer.camera_tan, renderer.camera_aspect
     r.num_lights = a["light_dir"].shape[0]
+    return r, a
+
+
+def render(renderer, bvh, vis_points: np.ndarray, aabb: tuple | None = None, stack_cap: int = 64):
+    """Oracle images (colour [N,R,R,3], depth [N,R,R]) for a WarpRaycastRendererDO's settings."""
+    arrays = {}
+    d = bvh_desc(bvh, arrays)
+    if aabb is not None:
+        arrays["aabb_min"][:] = aabb[0]
+        arrays["aabb_max"][:] = aabb[1]
+    N, R = renderer.numEnvs, renderer.width
+    r, a = _render_desc(renderer, vis_points)
     rc = lib().oracle_render(C.byref(r), C.byref(d), int(stack_cap))
     if rc:
         raise RuntimeError(f"oracle render failed: {rc}")
     return a["color"].reshape(N, R, R, 3), a["depth"].reshape(N, R, R), a["vertex_normal"]
+
+
+class OracleScene:
+    """One full env-step on the host, the reference's order: the solve (8 substeps x I
+    iterations), visual-point remap, BVH refit and ray-cast. All four run in the C++
+    restatement on host-side copies; ``threads`` spreads envs over OpenMP threads. Used
+    to time the CPU baseline; the images match ``render``'s."""
+
+    def __init__(self, model, bvh, renderer, stack_cap: int = 64):
+        self.sim = OracleSim(model)
+        self.model = model
+        self.ptv = np.ascontiguousarray(model.host["pointToVertex"], dtype=np.int32)
+        self.faces = np.ascontiguousarray(model.host["allVisFace"], dtype=np.int32)
+        self.bvh_arrays = {}
+        self.bvh = bvh_desc(bvh, self.bvh_arrays)
+        self.r, self.a = _render_desc(renderer, self.sim.vis_points())
+        self.stack_cap = stack_cap
+
+    def step(self, threads: int = 1) -> None:
+        lib_ = lib()
+        self.sim.step(1, threads=threads)
+        vp = self.a["vis_point"]
+        lib_.oracle_remap(vp.ctypes.data, self.sim.a["vertex"].ctypes.data, self.ptv.ctypes.data,
+                          self.model.numVisPoints)
+        lib_.oracle_refit_mt(C.byref(self.bvh), vp.ctypes.data, self.faces.ctypes.data, int(threads))
+        rc = lib_.oracle_render_mt(C.byref(self.r), C.byref(self.bvh), int(self.stack_cap), int(threads))
+        if rc:
+            raise RuntimeError(f"oracle render failed: {rc}")

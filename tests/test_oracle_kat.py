@@ -247,3 +247,29 @@ def test_refit_known_boxes(oracle_lib):
     np.testing.assert_array_equal(hi[0], [31, 1, 2])
     np.testing.assert_array_equal(lo[6], [30, 0, 2])
     np.testing.assert_array_equal(hi[2], [31, 1, 2])
+
+
+def test_threaded_scene_matches_serial(oracle_lib):
+    # the CPU baseline's threaded step (solve, remap, refit, render spread over envs)
+    # must give the serial oracle's boxes and images bit for bit
+    from ffsrl import scenarios as sc
+    meshes, _ = sc.mixed_meshes(3, pool_size=3, seed=5, t_lo=150, t_hi=400)
+    m, _ = sc.liver_model("cpu", 3, meshes=meshes)
+    bvh = SimBVH("cpu", m)
+    r = WarpRaycastRendererDO("cpu", m, resolution=8, mode="headless", verticalAperture=sc.fov_aperture(60.0),
+                              horizontalAperture=sc.fov_aperture(60.0))
+    pos, rot = sc.env_cameras(meshes, seed=1)
+    r.setCameras(pos, rot)
+    scene = oracle.OracleScene(m, bvh, r)
+    scene.step(threads=3)
+    o = oracle.OracleSim(m)
+    o.step(1)
+    vp = o.vis_points()
+    lo, hi = oracle.refit(bvh, vp, m.host["allVisFace"])
+    col, dep, _ = oracle.render(r, bvh, vp, aabb=(lo, hi))
+    np.testing.assert_array_equal(scene.sim.a["vertex"], o.a["vertex"])
+    np.testing.assert_array_equal(scene.bvh_arrays["aabb_min"], lo)
+    np.testing.assert_array_equal(scene.bvh_arrays["aabb_max"], hi)
+    np.testing.assert_array_equal(scene.a["color"].reshape(col.shape), col)
+    np.testing.assert_array_equal(scene.a["depth"].reshape(dep.shape), dep)
+    assert (dep > 0).any()
