@@ -123,9 +123,8 @@ template <class R> struct Dev {
     const EnvRec* env;
     const uint2* tet_idx;      // 4 x u16 local ids
     const float2* tet_va;      // (|V0|, active)
-    const float4* dmA;         // Dm^-1 row-major entries 0..3
-    const float4* dmB;         // entries 4..7
-    const float* dmC;          // entry 8
+    const float4* nh0;         // Neo-Hookean: M = Dm^-1 Dm^-T entries (00, 01, 02, 11)
+    const float4* nh1;         // (M12, M22, det Dm^-1, 0)
     const float* tet_vs;       // signed rest volume (XPBD)
     const unsigned* edge_idx;  // 2 x u16 local ids
     const float2* edge_la;     // (L0, active)
@@ -363,20 +362,22 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                             int skip = 0;  // statically counted constraints that skipped on degenerate geometry
                             const float2 va = __ldg(D.tet_va + gt);
                             const bool anym = mA != R(0) || mB != R(0) || mC != R(0) || mD != R(0);
+                            // cofactor columns of Ds = [p1 p2 p3]: the volume gradient, and (times det Dm^-1) the
+                            // Neo-Hookean hydrostatic gradient cof(F) Dm^-T = det(Dm^-1) cof(Ds)
+                            const t3<R> q1 = cross(p2, p3), q2 = cross(p3, p1), q3 = cross(p1, p2);
+                            const t3<R> q0 = -q1 - q2 - q3;
+                            const R wq = mA * dot(q0, q0) + mB * dot(q1, q1) + mC * dot(q2, q2) + mD * dot(q3, q3);
+                            const R s6 = dot(q3, p3);  // det Ds = 6 x signed volume
                             if (fl & (FFSRL_VOLUME | FFSRL_VOLUME_XPBD)) {
                                 // volumeConstraints (integrator.py:444-504) / XPBD (:507-576)
                                 const R active = R(va.y);
                                 if (active == R(1)) {
-                                    t3<R> q2 = cross(p3, p1), q1 = cross(p2, p3), q3 = cross(p1, p2);
-                                    t3<R> q0 = -q1 - q2 - q3;
-                                    R w = mA * dot(q0, q0) + mB * dot(q1, q1) + mC * dot(q2, q2) + mD * dot(q3, q3);
-                                    if (fabs(w) < R(BEPS)) {
+                                    if (fabs(wq) < R(BEPS)) {
                                         if (anym) skip += ((fl & FFSRL_VOLUME) ? 1 : 0) + ((fl & FFSRL_VOLUME_XPBD) ? 1 : 0);
                                     } else {
-                                        R s6 = dot(cross(p1, p2), p3);
                                         if (fl & FFSRL_VOLUME) {
                                             R C = R(va.x) - fabs(s6) / R(6);
-                                            R dl = -R(D.ks_volume) * active * C / w;
+                                            R dl = -R(D.ks_volume) * active * C / wq;
                                             dA = q0 * dl * mA; dB = q1 * dl * mB; dC = q2 * dl * mC; dD = q3 * dl * mD;
                                             ++k;
                                         }
@@ -385,55 +386,42 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                                             const int ot = E.mt0 + __ldg(D.tet_orig + gt);
                                             R lam = R(D.tet_lambda[ot]);
                                             R C = s6 / R(6) - R(__ldg(D.tet_vs + gt));
-                                            R dl = -(C + alpha * lam) / (w + alpha);
+                                            R dl = -(C + alpha * lam) / (wq + alpha);
                                             D.tet_lambda[ot] = float(lam + dl);
-                                            dA = dA + q0 * dl * mA; dB = dB + q1 * dl * mB;
-                                            dC = dC + q2 * dl * mC; dD = dD + q3 * dl * mD;
+                                            dA = dA + q0 * dl * mA; dB = dB + q1 * dl * mB; dC = dC + q2 * dl * mC; dD = dD + q3 * dl * mD;
                                             ++k;
                                         }
                                     }
                                 }
                             }
                             if (fl & FFSRL_NEOHOOKEAN) {
-                                // neoHookeanConstraints (integrator.py:578-698)
-                                const float4 a4 = __ldg(D.dmA + gt), b4 = __ldg(D.dmB + gt);
-                                const R d00 = R(a4.x), d01 = R(a4.y), d02 = R(a4.z), d10 = R(a4.w);
-                                const R d11 = R(b4.x), d12 = R(b4.y), d20 = R(b4.z), d21 = R(b4.w);
-                                const R d22 = R(__ldg(D.dmC + gt));
+                                // neoHookeanConstraints (integrator.py:578-698) with F = Ds Dm^-1 written through
+                                // M = Dm^-1 Dm^-T: |F|^2 = sum_ij (Ds^T Ds)_ij M_ij, F Dm^-T = Ds M, det F = det Ds det Dm^-1
+                                const float4 n0 = __ldg(D.nh0 + gt), n1 = __ldg(D.nh1 + gt);
+                                const R m00 = R(n0.x), m01 = R(n0.y), m02 = R(n0.z), m11 = R(n0.w);
+                                const R m12 = R(n1.x), m22 = R(n1.y), detD = R(n1.z);
                                 const R rv = R(va.x);
-                                t3<R> f0 = p1 * d00 + p2 * d10 + p3 * d20;
-                                t3<R> f1 = p1 * d01 + p2 * d11 + p3 * d21;
-                                t3<R> f2 = p1 * d02 + p2 * d12 + p3 * d22;
-                                t3<R> c0 = cross(f1, f2), c1 = cross(f2, f0), c2 = cross(f0, f1);
-                                t3<R> g1 = c0 * d00 + c1 * d01 + c2 * d02;
-                                t3<R> g2 = c0 * d10 + c1 * d11 + c2 * d12;
-                                t3<R> g3 = c0 * d20 + c1 * d21 + c2 * d22;
-                                t3<R> g0 = -g1 - g2 - g3;
-                                R detF = dot(f0, c0);
-                                R C = detF - R(1) - nh_off;
-                                // |g|^2 as dot(g, g) (the reference squares length(g); equal up to rounding)
-                                R w = dot(g0, g0) * mA + dot(g1, g1) * mB + dot(g2, g2) * mC + dot(g3, g3) * mD;
-                                if (w < R(BEPS)) {
+                                const R C = s6 * detD - R(1) - nh_off;
+                                const R wH = wq * detD * detD;
+                                if (wH < R(BEPS)) {
                                     if (anym) ++skip;
                                 } else {
-                                    R alpha = nh_uH / rv;
-                                    R dl = -C / (w + alpha);
-                                    t3<R> hA = g0 * dl * mA, hB = g1 * dl * mB, hC = g2 * dl * mC, hD = g3 * dl * mD;
-                                    R rs = sqrt(dot(f0, f0) + dot(f1, f1) + dot(f2, f2));
-                                    R rsi = R(1) / rs;
-                                    g1 = (f0 * d00 + f1 * d01 + f2 * d02) * rsi;
-                                    g2 = (f0 * d10 + f1 * d11 + f2 * d12) * rsi;
-                                    g3 = (f0 * d20 + f1 * d21 + f2 * d22) * rsi;
-                                    g0 = -g1 - g2 - g3;
-                                    w = dot(g0, g0) * mA + dot(g1, g1) * mB + dot(g2, g2) * mC + dot(g3, g3) * mD;
-                                    if (w < R(BEPS)) {
+                                    const R dlH = -C / (wH + nh_uH / rv);
+                                    const R rs = sqrt(dot(p1, p1) * m00 + dot(p2, p2) * m11 + dot(p3, p3) * m22 +
+                                                      R(2) * (dot(p1, p2) * m01 + dot(p1, p3) * m02 + dot(p2, p3) * m12));
+                                    const R rsi = R(1) / rs;
+                                    const t3<R> e1 = p1 * m00 + p2 * m01 + p3 * m02;
+                                    const t3<R> e2 = p1 * m01 + p2 * m11 + p3 * m12;
+                                    const t3<R> e3 = p1 * m02 + p2 * m12 + p3 * m22;
+                                    const t3<R> e0 = -e1 - e2 - e3;
+                                    const R wD = (mA * dot(e0, e0) + mB * dot(e1, e1) + mC * dot(e2, e2) + mD * dot(e3, e3)) * (rsi * rsi);
+                                    if (wD < R(BEPS)) {
                                         if (anym) ++skip;
                                     } else {
-                                        alpha = nh_uD / rv;
-                                        dl = -rs / (w + alpha);
-                                        hA = hA + g0 * dl * mA; hB = hB + g1 * dl * mB;
-                                        hC = hC + g2 * dl * mC; hD = hD + g3 * dl * mD;
-                                        dA = dA + hA; dB = dB + hB; dC = dC + hC; dD = dD + hD;
+                                        const R ce = -rs / (wD + nh_uD / rv) * rsi;
+                                        const R ch = dlH * detD;
+                                        dA = dA + (q0 * (ch * mA) + e0 * (ce * mA)); dB = dB + (q1 * (ch * mB) + e1 * (ce * mB));
+                                        dC = dC + (q2 * (ch * mC) + e2 * (ce * mC)); dD = dD + (q3 * (ch * mD) + e3 * (ce * mD));
                                         ++k;
                                     }
                                 }
@@ -632,7 +620,7 @@ struct ffsrl_batch {
     // device tables
     EnvRec* d_env = nullptr;
     uint2* d_tet_idx = nullptr; float2* d_tet_va = nullptr;
-    float4* d_dmA = nullptr; float4* d_dmB = nullptr; float* d_dmC = nullptr; float* d_tet_vs = nullptr;
+    float4* d_nh0 = nullptr; float4* d_nh1 = nullptr; float* d_tet_vs = nullptr;
     unsigned* d_edge_idx = nullptr; float2* d_edge_la = nullptr; uint2* d_tri_idx = nullptr;
     int* d_work = nullptr; int* d_counters = nullptr; int* d_status = nullptr;
     unsigned char* d_scratch = nullptr;
@@ -686,8 +674,8 @@ template <class T> int32_t upload(T* d, const std::vector<T>& h) {
 
 void free_batch(ffsrl_batch* b) {
     if (!b) return;
-    cudaFree(b->d_env); cudaFree(b->d_tet_idx); cudaFree(b->d_tet_va); cudaFree(b->d_dmA); cudaFree(b->d_dmB);
-    cudaFree(b->d_dmC); cudaFree(b->d_tet_vs); cudaFree(b->d_edge_idx); cudaFree(b->d_edge_la); cudaFree(b->d_tri_idx);
+    cudaFree(b->d_env); cudaFree(b->d_tet_idx); cudaFree(b->d_tet_va); cudaFree(b->d_nh0); cudaFree(b->d_nh1);
+    cudaFree(b->d_tet_vs); cudaFree(b->d_edge_idx); cudaFree(b->d_edge_la); cudaFree(b->d_tri_idx);
     cudaFree(b->d_work); cudaFree(b->d_status); cudaFree(b->d_scratch);
     cudaFree(b->d_state64); cudaFree(b->d_cnt0); cudaFree(b->d_tet_orig);
     cudaFree(b->d_edge_orig);
@@ -717,8 +705,8 @@ template <class R> int32_t launch_class(ffsrl_batch* b, const ffsrl_batch::Class
 Dev<float> make_dev_f(ffsrl_batch* b) {
     Dev<float> D;
     const ffsrl_params& p = b->params;
-    D.env = b->d_env; D.tet_idx = b->d_tet_idx; D.tet_va = b->d_tet_va; D.dmA = b->d_dmA; D.dmB = b->d_dmB;
-    D.dmC = b->d_dmC; D.tet_vs = b->d_tet_vs; D.edge_idx = b->d_edge_idx; D.edge_la = b->d_edge_la;
+    D.env = b->d_env; D.tet_idx = b->d_tet_idx; D.tet_va = b->d_tet_va; D.nh0 = b->d_nh0; D.nh1 = b->d_nh1;
+    D.tet_vs = b->d_tet_vs; D.edge_idx = b->d_edge_idx; D.edge_la = b->d_edge_la;
     D.tri_idx = b->d_tri_idx;
     D.vertex = b->dm.vertex; D.velocity = b->dm.velocity; D.predicted = b->dm.predicted_vertex;
     D.inv_mass = b->dm.inverse_mass; D.drag = b->dm.active_drag_constraint;
@@ -757,7 +745,7 @@ template <> int32_t launch_class<double>(ffsrl_batch* b, const ffsrl_batch::Clas
     Dev<float> F = make_dev_f(b);
     Dev<double> D;
     // same tables and parameters; state in the plan's double arrays
-    D.env = F.env; D.tet_idx = F.tet_idx; D.tet_va = F.tet_va; D.dmA = F.dmA; D.dmB = F.dmB; D.dmC = F.dmC;
+    D.env = F.env; D.tet_idx = F.tet_idx; D.tet_va = F.tet_va; D.nh0 = F.nh0; D.nh1 = F.nh1;
     D.tet_vs = F.tet_vs; D.edge_idx = F.edge_idx; D.edge_la = F.edge_la; D.tri_idx = F.tri_idx;
     int64_t V = b->dm.num_vertices;
     D.vertex = b->d_state64; D.velocity = b->d_state64 + 3 * V; D.predicted = b->d_state64 + 6 * V;
@@ -870,14 +858,14 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
     std::vector<EnvRec> env(N);
     std::vector<uint2> tet_idx(T);
     std::vector<float2> tet_va(T);
-    std::vector<float4> dmA, dmB;
-    std::vector<float> dmC, tet_vs;
+    std::vector<float4> nh0, nh1;
+    std::vector<float> tet_vs;
     const bool nh = (p->flags & FFSRL_NEOHOOKEAN) != 0;
     const bool xv = (p->flags & FFSRL_VOLUME_XPBD) != 0;
     if (nh && !hm->tetrahedron_dm_inv) { free_batch(b); return fail(FFSRL_ERR_INVALID_ARGUMENT, "Neo-Hookean needs tetrahedron_dm_inv"); }
     if (xv && (!hm->xpbd_rest_volume || !dmod->tetrahedron_lambda)) { free_batch(b); return fail(FFSRL_ERR_INVALID_ARGUMENT, "XPBD volume needs xpbd_rest_volume and lambdas"); }
     if ((p->flags & FFSRL_DISTANCE_XPBD) && !dmod->edge_lambda) { free_batch(b); return fail(FFSRL_ERR_INVALID_ARGUMENT, "XPBD distance needs edge_lambda"); }
-    if (nh) { dmA.resize(T); dmB.resize(T); dmC.resize(T); }
+    if (nh) { nh0.resize(T); nh1.resize(T); }
     if (xv) tet_vs.resize(T);
     std::vector<unsigned> edge_idx(E);
     std::vector<float2> edge_la(E);
@@ -911,10 +899,15 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
             tet_va[t] = make_float2(hm->tetrahedron_rest_volume ? hm->tetrahedron_rest_volume[t] : 0.0f,
                                     hm->active_tetrahedron ? hm->active_tetrahedron[t] : 1.0f);
             if (nh) {
-                const float* d = hm->tetrahedron_dm_inv + 9ll * t;
-                dmA[t] = make_float4(d[0], d[1], d[2], d[3]);
-                dmB[t] = make_float4(d[4], d[5], d[6], d[7]);
-                dmC[t] = d[8];
+                // M = D D^T and det D of the stored D = Dm^-1 (row-major), in double
+                const float* f = hm->tetrahedron_dm_inv + 9ll * t;
+                double d[9];
+                for (int k = 0; k < 9; ++k) d[k] = f[k];
+                auto mm = [&](int i, int j) { return d[3 * i] * d[3 * j] + d[3 * i + 1] * d[3 * j + 1] + d[3 * i + 2] * d[3 * j + 2]; };
+                double det = d[0] * (d[4] * d[8] - d[5] * d[7]) - d[1] * (d[3] * d[8] - d[5] * d[6]) +
+                             d[2] * (d[3] * d[7] - d[4] * d[6]);
+                nh0[t] = make_float4((float)mm(0, 0), (float)mm(0, 1), (float)mm(0, 2), (float)mm(1, 1));
+                nh1[t] = make_float4((float)mm(1, 2), (float)mm(2, 2), (float)det, 0.0f);
             }
             if (xv) tet_vs[t] = hm->xpbd_rest_volume[t];
         }
@@ -1018,8 +1011,8 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
             auto c = v;
             for (size_t i = 0; i < orig.size(); ++i) v[i] = c[orig[i]];
         };
-        permute(tet_idx, tet_orig); permute(tet_va, tet_orig); permute(dmA, tet_orig); permute(dmB, tet_orig);
-        permute(dmC, tet_orig); permute(tet_vs, tet_orig); permute(edge_idx, edge_orig); permute(edge_la, edge_orig);
+        permute(tet_idx, tet_orig); permute(tet_va, tet_orig); permute(nh0, tet_orig); permute(nh1, tet_orig);
+        permute(tet_vs, tet_orig); permute(edge_idx, edge_orig); permute(edge_la, edge_orig);
     }
 
     // ---- share identical constraint tables: envs of one mesh read the same records ----
@@ -1040,13 +1033,13 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
                 return n == 0 || v.empty() || std::memcmp(&v[o1], &v[o2], sizeof(v[0]) * (size_t)n) == 0;
             };
             return a.nv == c.nv && a.nt == c.nt && a.ne == c.ne && a.nf == c.nf &&
-                   eq(tet_idx, a.t0, c.t0, a.nt) && eq(tet_va, a.t0, c.t0, a.nt) && eq(dmA, a.t0, c.t0, a.nt) &&
-                   eq(dmB, a.t0, c.t0, a.nt) && eq(dmC, a.t0, c.t0, a.nt) && eq(tet_vs, a.t0, c.t0, a.nt) &&
+                   eq(tet_idx, a.t0, c.t0, a.nt) && eq(tet_va, a.t0, c.t0, a.nt) && eq(nh0, a.t0, c.t0, a.nt) &&
+                   eq(nh1, a.t0, c.t0, a.nt) && eq(tet_vs, a.t0, c.t0, a.nt) &&
                    eq(tet_orig, a.t0, c.t0, a.nt) && eq(edge_idx, a.e0, c.e0, a.ne) && eq(edge_la, a.e0, c.e0, a.ne) &&
                    eq(edge_orig, a.e0, c.e0, a.ne) && eq(tri_idx, a.f0, c.f0, a.nf);
         };
-        std::vector<uint2> c_tet_idx; std::vector<float2> c_tet_va; std::vector<float4> c_dmA, c_dmB;
-        std::vector<float> c_dmC, c_tet_vs; std::vector<int> c_tet_orig, c_edge_orig;
+        std::vector<uint2> c_tet_idx; std::vector<float2> c_tet_va; std::vector<float4> c_nh0, c_nh1;
+        std::vector<float> c_tet_vs; std::vector<int> c_tet_orig, c_edge_orig;
         std::vector<unsigned> c_edge_idx; std::vector<float2> c_edge_la; std::vector<uint2> c_tri_idx;
         std::unordered_map<uint64_t, std::vector<int>> seen;
         std::vector<EnvRec> out = env;
@@ -1068,14 +1061,14 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
             }
             seen[h].push_back(e);
             out[e].t0 = (int)c_tet_idx.size(); out[e].e0 = (int)c_edge_idx.size(); out[e].f0 = (int)c_tri_idx.size();
-            app(c_tet_idx, tet_idx, r.t0, r.nt); app(c_tet_va, tet_va, r.t0, r.nt); app(c_dmA, dmA, r.t0, r.nt);
-            app(c_dmB, dmB, r.t0, r.nt); app(c_dmC, dmC, r.t0, r.nt); app(c_tet_vs, tet_vs, r.t0, r.nt);
+            app(c_tet_idx, tet_idx, r.t0, r.nt); app(c_tet_va, tet_va, r.t0, r.nt); app(c_nh0, nh0, r.t0, r.nt);
+            app(c_nh1, nh1, r.t0, r.nt); app(c_tet_vs, tet_vs, r.t0, r.nt);
             app(c_tet_orig, tet_orig, r.t0, r.nt); app(c_edge_idx, edge_idx, r.e0, r.ne);
             app(c_edge_la, edge_la, r.e0, r.ne); app(c_edge_orig, edge_orig, r.e0, r.ne);
             app(c_tri_idx, tri_idx, r.f0, r.nf);
         }
         env = out;
-        tet_idx.swap(c_tet_idx); tet_va.swap(c_tet_va); dmA.swap(c_dmA); dmB.swap(c_dmB); dmC.swap(c_dmC);
+        tet_idx.swap(c_tet_idx); tet_va.swap(c_tet_va); nh0.swap(c_nh0); nh1.swap(c_nh1);
         tet_vs.swap(c_tet_vs); tet_orig.swap(c_tet_orig); edge_idx.swap(c_edge_idx); edge_la.swap(c_edge_la);
         edge_orig.swap(c_edge_orig); tri_idx.swap(c_tri_idx);
     }
@@ -1140,9 +1133,8 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
         (st = dalloc(b, &b->d_env, N)) || (st = upload(b->d_env, env)) ||
         (st = dalloc(b, &b->d_tet_idx, tet_idx.size())) || (st = upload(b->d_tet_idx, tet_idx)) ||
         (st = dalloc(b, &b->d_tet_va, tet_va.size())) || (st = upload(b->d_tet_va, tet_va)) ||
-        (st = dalloc(b, &b->d_dmA, dmA.size())) || (st = upload(b->d_dmA, dmA)) ||
-        (st = dalloc(b, &b->d_dmB, dmB.size())) || (st = upload(b->d_dmB, dmB)) ||
-        (st = dalloc(b, &b->d_dmC, dmC.size())) || (st = upload(b->d_dmC, dmC)) ||
+        (st = dalloc(b, &b->d_nh0, nh0.size())) || (st = upload(b->d_nh0, nh0)) ||
+        (st = dalloc(b, &b->d_nh1, nh1.size())) || (st = upload(b->d_nh1, nh1)) ||
         (st = dalloc(b, &b->d_tet_vs, tet_vs.size())) || (st = upload(b->d_tet_vs, tet_vs)) ||
         (st = dalloc(b, &b->d_edge_idx, edge_idx.size())) || (st = upload(b->d_edge_idx, edge_idx)) ||
         (st = dalloc(b, &b->d_edge_la, edge_la.size())) || (st = upload(b->d_edge_la, edge_la)) ||
