@@ -62,6 +62,20 @@ template <class R> __device__ __forceinline__ t3<R> normalize(t3<R> a) {
 }
 template <class R> __device__ __forceinline__ R rmin(R a, R b) { return a < b ? a : b; }
 template <class R> __device__ __forceinline__ R rmax(R a, R b) { return a > b ? a : b; }
+// Reciprocal and reciprocal square root: one hardware approximation each in float32
+// (PTX rcp.approx / rsqrt.approx, about 1 ulp), exact division and sqrt in float64
+__device__ __forceinline__ float rcp(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
+__device__ __forceinline__ float rsqrt_(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ double rsqrt_(double x) { return 1.0 / sqrt(x); }
 
 // per-precision storage: predicted position + inverse mass, accumulator word
 template <class R> struct Store;
@@ -124,7 +138,7 @@ template <class R> struct Dev {
     const uint2* tet_idx;      // 4 x u16 local ids
     const float2* tet_va;      // (|V0|, active)
     const float4* nh0;         // Neo-Hookean: M = Dm^-1 Dm^-T entries (00, 01, 02, 11)
-    const float4* nh1;         // (M12, M22, det Dm^-1, 0)
+    const float4* nh1;         // (M12, M22, det Dm^-1, 1/|V0|)
     const float* tet_vs;       // signed rest volume (XPBD)
     const unsigned* edge_idx;  // 2 x u16 local ids
     const float2* edge_la;     // (L0, active)
@@ -376,8 +390,8 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                                         if (anym) skip += ((fl & FFSRL_VOLUME) ? 1 : 0) + ((fl & FFSRL_VOLUME_XPBD) ? 1 : 0);
                                     } else {
                                         if (fl & FFSRL_VOLUME) {
-                                            R C = R(va.x) - fabs(s6) / R(6);
-                                            R dl = -R(D.ks_volume) * active * C / wq;
+                                            R C = R(va.x) - fabs(s6) * R(1.0 / 6.0);
+                                            R dl = -R(D.ks_volume) * active * C * rcp(wq);
                                             dA = q0 * dl * mA; dB = q1 * dl * mB; dC = q2 * dl * mC; dD = q3 * dl * mD;
                                             ++k;
                                         }
@@ -399,17 +413,17 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                                 // M = Dm^-1 Dm^-T: |F|^2 = sum_ij (Ds^T Ds)_ij M_ij, F Dm^-T = Ds M, det F = det Ds det Dm^-1
                                 const float4 n0 = __ldg(D.nh0 + gt), n1 = __ldg(D.nh1 + gt);
                                 const R m00 = R(n0.x), m01 = R(n0.y), m02 = R(n0.z), m11 = R(n0.w);
-                                const R m12 = R(n1.x), m22 = R(n1.y), detD = R(n1.z);
-                                const R rv = R(va.x);
+                                const R m12 = R(n1.x), m22 = R(n1.y), detD = R(n1.z), inv_rv = R(n1.w);
                                 const R C = s6 * detD - R(1) - nh_off;
                                 const R wH = wq * detD * detD;
                                 if (wH < R(BEPS)) {
                                     if (anym) ++skip;
                                 } else {
-                                    const R dlH = -C / (wH + nh_uH / rv);
-                                    const R rs = sqrt(dot(p1, p1) * m00 + dot(p2, p2) * m11 + dot(p3, p3) * m22 +
-                                                      R(2) * (dot(p1, p2) * m01 + dot(p1, p3) * m02 + dot(p2, p3) * m12));
-                                    const R rsi = R(1) / rs;
+                                    const R dlH = -C * rcp(wH + nh_uH * inv_rv);
+                                    const R rs2 = dot(p1, p1) * m00 + dot(p2, p2) * m11 + dot(p3, p3) * m22 +
+                                                  R(2) * (dot(p1, p2) * m01 + dot(p1, p3) * m02 + dot(p2, p3) * m12);
+                                    const R rsi = rsqrt_(rs2);
+                                    const R rs = rs2 * rsi;
                                     const t3<R> e1 = p1 * m00 + p2 * m01 + p3 * m02;
                                     const t3<R> e2 = p1 * m01 + p2 * m11 + p3 * m12;
                                     const t3<R> e3 = p1 * m02 + p2 * m12 + p3 * m22;
@@ -418,7 +432,7 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                                     if (wD < R(BEPS)) {
                                         if (anym) ++skip;
                                     } else {
-                                        const R ce = -rs / (wD + nh_uD / rv) * rsi;
+                                        const R ce = -rs * rcp(wD + nh_uD * inv_rv) * rsi;
                                         const R ch = dlH * detD;
                                         dA = dA + (q0 * (ch * mA) + e0 * (ce * mA)); dB = dB + (q1 * (ch * mB) + e1 * (ce * mB));
                                         dC = dC + (q2 * (ch * mC) + e2 * (ce * mC)); dD = dD + (q3 * (ch * mD) + e3 * (ce * mD));
@@ -447,19 +461,20 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                             R mA = PA.w, mB = PB.w;
                             R w = mA + mB;
                             if (w < R(BEPS)) continue;  // never counted
-                            t3<R> dir = S::pos(PB) - S::pos(PA);
-                            R len = length(dir);
-                            if (len < R(BEPS)) {
+                            const t3<R> dir = S::pos(PB) - S::pos(PA);
+                            const R dd = dot(dir, dir);
+                            if (dd < R(BEPS * BEPS)) {  // length below FLOAT_EPSILON
                                 const int skip = ((fl & FFSRL_DISTANCE) ? 1 : 0) + ((fl & FFSRL_DISTANCE_XPBD) ? 1 : 0);
                                 atomicSub(cnt + ia, skip); atomicSub(cnt + ib, skip);
                                 s_dyn_it = it;
                                 continue;
                             }
-                            R C = len - L0;
+                            const R rl = rsqrt_(dd);
+                            const R C = dd * rl - L0;
                             t3<R> dA = T3<R>(0, 0, 0), dB = dA;
                             int k = 0;
                             if (fl & FFSRL_DISTANCE) {
-                                t3<R> d = -C * (dir / len) * R(D.ks_distance) * active / w;
+                                t3<R> d = dir * (-C * rl * R(D.ks_distance) * active * rcp(w));
                                 dA = -(d * mA); dB = d * mB;
                                 ++k;
                             }
@@ -469,7 +484,7 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                                 R lam = R(D.edge_lambda[oe]);
                                 R dl = -(C + alpha * lam) / (w + alpha);
                                 D.edge_lambda[oe] = float(lam + dl);
-                                t3<R> d = dl * normalize(dir);
+                                t3<R> d = dir * (dl * rl);
                                 dA = dA - d * mA; dB = dB + d * mB;
                                 ++k;
                             }
@@ -484,9 +499,9 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                         P q = xp[i];
                         t3<R> x = S::pos(q);
                         if (c > 0) {
-                            R N = R(c);
-                            x = x + T3<R>(S::get(acc[3 * i], fx) / N, S::get(acc[3 * i + 1], fx) / N,
-                                          S::get(acc[3 * i + 2], fx) / N);
+                            const R rN = rcp(R(c));
+                            x = x + T3<R>(S::get(acc[3 * i], fx) * rN, S::get(acc[3 * i + 1], fx) * rN,
+                                          S::get(acc[3 * i + 2], fx) * rN);
                             acc[3 * i] = A(0); acc[3 * i + 1] = A(0); acc[3 * i + 2] = A(0);
                         }
                         if (restore) cnt[i] = __ldg(D.cnt0 + E.v0 + i);
@@ -907,7 +922,8 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
                 double det = d[0] * (d[4] * d[8] - d[5] * d[7]) - d[1] * (d[3] * d[8] - d[5] * d[6]) +
                              d[2] * (d[3] * d[7] - d[4] * d[6]);
                 nh0[t] = make_float4((float)mm(0, 0), (float)mm(0, 1), (float)mm(0, 2), (float)mm(1, 1));
-                nh1[t] = make_float4((float)mm(1, 2), (float)mm(2, 2), (float)det, 0.0f);
+                const double v0 = hm->tetrahedron_rest_volume ? (double)hm->tetrahedron_rest_volume[t] : 0.0;
+                nh1[t] = make_float4((float)mm(1, 2), (float)mm(2, 2), (float)det, (float)(1.0 / (double)(float)v0));
             }
             if (xv) tet_vs[t] = hm->xpbd_rest_volume[t];
         }

@@ -7,6 +7,9 @@ the device, so a capture of one to six launches ends within a minute or two.
     python -m ffsrl.profile_cases step_mixed [envs]   # every size-class launch of one batched step
     python -m ffsrl.profile_cases step_big            # one size class of large envs (12k-20k tets)
     python -m ffsrl.profile_cases render              # refit + ray-cast of 256 envs at 128x128
+    python -m ffsrl.profile_cases step_uniform [constraints] [block]
+                                                      # 152 copies of one 16k-tet mesh, one step with the
+                                                      # named constraints (e.g. VOLUME+DISTANCE; default: all)
 
 The step cases draw their meshes from the same seeded 64-mesh pool as the 4096-env
 throughput workload, so per-env-step figures scale to it.
@@ -43,6 +46,21 @@ def step_big(device: str = "cuda:0") -> None:
     torch.cuda.synchronize()
 
 
+def step_uniform(constraints: str = "", block: int = 1024, envs: int = 152, device: str = "cuda:0") -> None:
+    from . import _lib as L
+    from . import meshgen as mg
+    mesh = mg.ellipsoid_for_tets(16000, seed=7)
+    m, _ = sc.liver_model(device, envs, meshes=[mesh] * envs)
+    if constraints:
+        m.constraintFlags = 0
+        for name in constraints.split("+"):
+            m.constraintFlags |= getattr(L, name)
+    p = SimIntegratorDO(device, blockThreads=block).plan(m)
+    print(p.info(), hex(m.constraintFlags))
+    p.step(1)
+    torch.cuda.synchronize()
+
+
 def render(envs: int = 256, device: str = "cuda:0") -> None:
     meshes, _ = sc.mixed_meshes(envs, pool_size=16, seed=0)
     m, _ = sc.liver_model(device, envs, meshes=meshes)
@@ -63,10 +81,12 @@ def main(argv: list[str]) -> None:
         step_mixed(int(argv[1]) if len(argv) > 1 else 512)
     elif case == "step_big":
         step_big()
+    elif case == "step_uniform":
+        step_uniform(argv[1] if len(argv) > 1 else "", int(argv[2]) if len(argv) > 2 else 1024)
     elif case == "render":
         render()
     else:
-        raise SystemExit(f"unknown case {case!r}: step_mixed, step_big or render")
+        raise SystemExit(f"unknown case {case!r}: step_mixed, step_big, step_uniform or render")
     print("ok")
 
 
