@@ -150,6 +150,9 @@ template <class R> struct Dev {
     float* tet_lambda; float* edge_lambda;
     int* env_status;
     const int* cnt0;           // per-vertex static contribution count (global vertex index)
+    const float4* tet_ed;      // distance constraints solved by the tet: (L0 of A-B, active, +-L0, active);
+                               // the second is C-D for +L0 and A-C for -L0; active 0 = none
+    int fold;                  // distance constraints folded into the tet records
     const int* tet_orig;       // env-local model tet id of each (colour-ordered) record, for XPBD lambdas
     const int* edge_orig;      // env-local model edge id of each record
     Fixed fx;
@@ -237,6 +240,29 @@ template <class R> __device__ __forceinline__ bool capsule_response(t3<R> tip, t
     return true;
 }
 
+// One distance constraint between two of a tet's vertices, added to the tet's corrections
+// (u gets -d m_u, v gets +d m_v).  Returns 1 when it contributed.  A degenerate length
+// decrements the two static counts and records the iteration in *dyn_it.
+template <class R> __device__ __forceinline__ int fold_edge(t3<R> pu, t3<R> pv, R mu, R mv, R L0, R active,
+                                                            t3<R>& du, t3<R>& dv, int iu, int iv, int* cnt,
+                                                            int it, R ks, int* dyn_it) {
+    const R w = mu + mv;
+    if (w < R(BEPS)) return 0;  // never counted
+    const t3<R> dir = pv - pu;
+    const R dd = dot(dir, dir);
+    if (dd < R(BEPS * BEPS)) {
+        atomicSub(cnt + iu, 1); atomicSub(cnt + iv, 1);
+        *dyn_it = it;
+        return 0;
+    }
+    const R rl = rsqrt_(dd);
+    const R C = dd * rl - L0;
+    const t3<R> d = dir * (-C * rl * ks * active * rcp(w));
+    du = du - d * mu;
+    dv = dv + d * mv;
+    return 1;
+}
+
 template <class R> struct ToolShared {
     t3<R> base[3], tip[3];
     R radius[3];
@@ -247,7 +273,7 @@ template <class R> struct ToolShared {
 // MODE 0: positions and accumulators in shared memory.  MODE 1: positions in shared
 // memory, accumulators in the block's global scratch.  MODE 2: both in global scratch.
 template <class R, int BLOCK, int MODE>
-__global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __restrict__ work, int nwork,
+__global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_batched(const Dev<R> D, const int* __restrict__ work, int nwork,
                                                    int* counter, int nsteps, unsigned char* scratch,
                                                    long long scratch_stride, int max_nv) {
     typedef Store<R> S;
@@ -438,6 +464,15 @@ __global__ void __launch_bounds__(BLOCK) k_batched(const Dev<R> D, const int* __
                                         dC = dC + (q2 * (ch * mC) + e2 * (ce * mC)); dD = dD + (q3 * (ch * mD) + e3 * (ce * mD));
                                         ++k;
                                     }
+                                }
+                            }
+                            if (D.fold) {
+                                // distanceConstraints (integrator.py:65-109) of the edges this tet solves
+                                const float4 ed = __ldg(D.tet_ed + gt);
+                                if (ed.y != 0.0f) k += fold_edge<R>(pa, pb, mA, mB, R(ed.x), R(ed.y), dA, dB, ia, ib, cnt, it, R(D.ks_distance), &s_dyn_it);
+                                if (ed.w != 0.0f) {
+                                    if (ed.z > 0.0f) k += fold_edge<R>(pc, pd, mC, mD, R(ed.z), R(ed.w), dC, dD, ic, id, cnt, it, R(D.ks_distance), &s_dyn_it);
+                                    else k += fold_edge<R>(pa, pc, mA, mC, R(-ed.z), R(ed.w), dA, dC, ia, ic, cnt, it, R(D.ks_distance), &s_dyn_it);
                                 }
                             }
                             if (k) add3x4<R>(acc, ia, ib, ic, id, dA, dB, dC, dD, bad, fx);
@@ -635,7 +670,7 @@ struct ffsrl_batch {
     // device tables
     EnvRec* d_env = nullptr;
     uint2* d_tet_idx = nullptr; float2* d_tet_va = nullptr;
-    float4* d_nh0 = nullptr; float4* d_nh1 = nullptr; float* d_tet_vs = nullptr;
+    float4* d_nh0 = nullptr; float4* d_nh1 = nullptr; float* d_tet_vs = nullptr; float4* d_tet_ed = nullptr;
     unsigned* d_edge_idx = nullptr; float2* d_edge_la = nullptr; uint2* d_tri_idx = nullptr;
     int* d_work = nullptr; int* d_counters = nullptr; int* d_status = nullptr;
     unsigned char* d_scratch = nullptr;
@@ -689,7 +724,7 @@ template <class T> int32_t upload(T* d, const std::vector<T>& h) {
 
 void free_batch(ffsrl_batch* b) {
     if (!b) return;
-    cudaFree(b->d_env); cudaFree(b->d_tet_idx); cudaFree(b->d_tet_va); cudaFree(b->d_nh0); cudaFree(b->d_nh1);
+    cudaFree(b->d_env); cudaFree(b->d_tet_idx); cudaFree(b->d_tet_va); cudaFree(b->d_nh0); cudaFree(b->d_nh1); cudaFree(b->d_tet_ed);
     cudaFree(b->d_tet_vs); cudaFree(b->d_edge_idx); cudaFree(b->d_edge_la); cudaFree(b->d_tri_idx);
     cudaFree(b->d_work); cudaFree(b->d_status); cudaFree(b->d_scratch);
     cudaFree(b->d_state64); cudaFree(b->d_cnt0); cudaFree(b->d_tet_orig);
@@ -730,6 +765,7 @@ Dev<float> make_dev_f(ffsrl_batch* b) {
     D.tet_lambda = b->dm.tetrahedron_lambda; D.edge_lambda = b->dm.edge_lambda;
     D.env_status = b->d_status;
     D.cnt0 = b->d_cnt0; D.tet_orig = b->d_tet_orig; D.edge_orig = b->d_edge_orig; D.fx = b->fx;
+    D.tet_ed = b->d_tet_ed; D.fold = b->d_tet_ed != nullptr;
     D.flags = p.flags; D.substeps = p.substeps; D.iterations = p.iterations;
     D.dt = p.dt; D.gx = p.gravity[0]; D.gy = p.gravity[1]; D.gz = p.gravity[2];
     D.damping = p.velocity_dampening; D.ground = p.ground_level;
@@ -768,6 +804,7 @@ template <> int32_t launch_class<double>(ffsrl_batch* b, const ffsrl_batch::Clas
     D.lap_radius = F.lap_radius; D.in_collision = F.in_collision; D.tet_lambda = F.tet_lambda;
     D.edge_lambda = F.edge_lambda; D.env_status = F.env_status; D.flags = F.flags; D.substeps = F.substeps;
     D.cnt0 = F.cnt0; D.tet_orig = F.tet_orig; D.edge_orig = F.edge_orig; D.fx = F.fx;
+    D.tet_ed = F.tet_ed; D.fold = F.fold;
     D.iterations = F.iterations; D.dt = F.dt; D.gx = F.gx; D.gy = F.gy; D.gz = F.gz; D.damping = F.damping;
     D.ground = F.ground; D.ks_distance = F.ks_distance; D.ks_volume = F.ks_volume; D.ks_contact = F.ks_contact;
     D.ks_drag = F.ks_drag; D.vol_c = F.vol_c; D.dev_c = F.dev_c; D.a_dist = F.a_dist; D.a_vol = F.a_vol;
@@ -987,8 +1024,161 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
         b->fx.bound = std::ldexp(1.0f, 31) / (float)(max_terms + 1);
     }
 
+    // ---- fold distance constraints into tets: each edge is solved by one tet that holds
+    // both its vertices, inside that tet's thread, so its correction joins the tet's four
+    // accumulator updates.  A tet takes at most two edges; its vertices are reordered by an
+    // even permutation (same orientation, Neo-Hookean tables recomputed for the new order)
+    // so that the edges sit at A-B, and C-D or A-C.  Edges no tet can take stay in the
+    // edge loop.  Not with XPBD distance (per-edge multipliers), so edge records keep their
+    // model order otherwise. ----
+    std::vector<float4> tet_ed;
+    std::vector<unsigned char> tet_cls(T, 0);  // 0 none, 1 A-B, 2 A-B + C-D, 3 A-B + A-C
+    const bool fold = (fl & FFSRL_DISTANCE) && !(fl & FFSRL_DISTANCE_XPBD) &&
+                      (fl & (FFSRL_VOLUME | FFSRL_VOLUME_XPBD | FFSRL_NEOHOOKEAN)) && T > 0 && E > 0;
+    if (fold) {
+        tet_ed.assign(T, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+        std::vector<unsigned> n_edge_idx;
+        std::vector<float2> n_edge_la;
+        std::vector<int> adj_start, adj;
+        std::vector<int> owned_n(T, 0), owned(2 * T, -1);
+        for (int e = 0; e < N; ++e) {
+            EnvRec& r = env[e];
+            // vertex -> incident tets of this env
+            adj_start.assign(r.nv + 1, 0);
+            for (int t = r.t0; t < r.t0 + r.nt; ++t) {
+                uint2 ix = tet_idx[t];
+                int l[4] = {(int)(ix.x & 0xffff), (int)(ix.x >> 16), (int)(ix.y & 0xffff), (int)(ix.y >> 16)};
+                for (int k = 0; k < 4; ++k) adj_start[l[k] + 1]++;
+            }
+            for (int v = 0; v < r.nv; ++v) adj_start[v + 1] += adj_start[v];
+            adj.assign(adj_start[r.nv], 0);
+            {
+                std::vector<int> fill(adj_start.begin(), adj_start.end() - 1);
+                for (int t = r.t0; t < r.t0 + r.nt; ++t) {
+                    uint2 ix = tet_idx[t];
+                    int l[4] = {(int)(ix.x & 0xffff), (int)(ix.x >> 16), (int)(ix.y & 0xffff), (int)(ix.y >> 16)};
+                    for (int k = 0; k < 4; ++k) adj[fill[l[k]]++] = t;
+                }
+            }
+            const int ne_new0 = (int)n_edge_idx.size();
+            for (int k = r.e0; k < r.e0 + r.ne; ++k) {
+                const int a = edge_idx[k] & 0xffff, c = edge_idx[k] >> 16;
+                const float2 la = edge_la[k];
+                const float w = hm->inverse_mass[r.v0 + a] + hm->inverse_mass[r.v0 + c];
+                if (la.y == 0.0f || la.x < feps || w < feps) continue;  // never contributes or counts
+                int best = -1;
+                for (int j = adj_start[a]; j < adj_start[a + 1]; ++j) {
+                    const int t = adj[j];
+                    if (owned_n[t] >= 2) continue;
+                    uint2 ix = tet_idx[t];
+                    int l[4] = {(int)(ix.x & 0xffff), (int)(ix.x >> 16), (int)(ix.y & 0xffff), (int)(ix.y >> 16)};
+                    if (l[0] != c && l[1] != c && l[2] != c && l[3] != c) continue;
+                    if (best < 0 || owned_n[t] < owned_n[best]) best = t;
+                }
+                if (best >= 0) {
+                    owned[2 * best + owned_n[best]++] = k;
+                } else {
+                    n_edge_idx.push_back(edge_idx[k]);
+                    n_edge_la.push_back(la);
+                }
+            }
+            // reorder each owning tet and record its edges
+            for (int t = r.t0; t < r.t0 + r.nt; ++t) {
+                if (!owned_n[t]) continue;
+                uint2 ix = tet_idx[t];
+                int l[4] = {(int)(ix.x & 0xffff), (int)(ix.x >> 16), (int)(ix.y & 0xffff), (int)(ix.y >> 16)};
+                auto pos = [&](int v) { for (int q = 0; q < 4; ++q) if (l[q] == v) return q; return -1; };
+                const int k1 = owned[2 * t], k2 = owned_n[t] > 1 ? owned[2 * t + 1] : -1;
+                const int i1 = pos(edge_idx[k1] & 0xffff), j1 = pos(edge_idx[k1] >> 16);
+                int nw[4];
+                int cls = 1;
+                if (k2 < 0) {
+                    nw[0] = i1; nw[1] = j1;
+                    int o = 2;
+                    for (int q = 0; q < 4; ++q) if (q != i1 && q != j1) nw[o++] = q;
+                } else {
+                    const int i2 = pos(edge_idx[k2] & 0xffff), j2 = pos(edge_idx[k2] >> 16);
+                    if (i2 != i1 && i2 != j1 && j2 != i1 && j2 != j1) {  // opposite: A-B, C-D
+                        nw[0] = i1; nw[1] = j1; nw[2] = i2; nw[3] = j2;
+                        cls = 2;
+                    } else {  // adjacent: the shared vertex is A, then B and C
+                        const int sh = (i2 == i1 || j2 == i1) ? i1 : j1;
+                        const int o1 = sh == i1 ? j1 : i1, o2 = i2 == sh ? j2 : i2;
+                        nw[0] = sh; nw[1] = o1; nw[2] = o2;
+                        for (int q = 0; q < 4; ++q) if (q != sh && q != o1 && q != o2) nw[3] = q;
+                        cls = 3;
+                    }
+                }
+                // make the permutation even by swapping the two entries that carry no
+                // edge constraint of their own (C and D for one edge; for two edges the
+                // swap of A-B's ends or of the second pair's ends keeps the pairs)
+                int inv = 0;
+                for (int x = 0; x < 4; ++x)
+                    for (int y = x + 1; y < 4; ++y) inv += nw[x] > nw[y];
+                if (inv & 1) {
+                    if (cls == 1 || cls == 2) std::swap(nw[2], nw[3]);
+                    else std::swap(nw[1], nw[2]);  // A-B and A-C trade places: edges follow below
+                }
+                int nl[4];
+                for (int q = 0; q < 4; ++q) nl[q] = l[nw[q]];
+                tet_idx[t] = make_uint2((unsigned)nl[0] | ((unsigned)nl[1] << 16), (unsigned)nl[2] | ((unsigned)nl[3] << 16));
+                // edge rest lengths in the new local pairs
+                auto edge_at = [&](int u, int v) {
+                    for (int m = 0; m < owned_n[t]; ++m) {
+                        const int kk = owned[2 * t + m];
+                        const int a = edge_idx[kk] & 0xffff, c = edge_idx[kk] >> 16;
+                        if ((a == u && c == v) || (a == v && c == u)) return kk;
+                    }
+                    return -1;
+                };
+                const int eAB = edge_at(nl[0], nl[1]);
+                float4 ed = make_float4(edge_la[eAB].x, edge_la[eAB].y, 0.0f, 0.0f);
+                if (cls == 2) {
+                    const int eCD = edge_at(nl[2], nl[3]);
+                    ed.z = edge_la[eCD].x; ed.w = edge_la[eCD].y;
+                } else if (cls == 3) {
+                    const int eAC = edge_at(nl[0], nl[2]);
+                    ed.z = -edge_la[eAC].x; ed.w = edge_la[eAC].y;
+                }
+                tet_ed[t] = ed;
+                tet_cls[t] = (unsigned char)cls;
+                // Neo-Hookean tables for the new order: Ds' = Ds P with
+                // P[k-1][m-1] = [nw[m] == k] - [nw[0] == k], so Dm'^-1 = P^-1 Dm^-1
+                if (nh) {
+                    const float* f = hm->tetrahedron_dm_inv + 9ll * t;
+                    double d[9], P[9], Pi[9], d2[9];
+                    for (int k = 0; k < 9; ++k) d[k] = f[k];
+                    for (int k = 1; k <= 3; ++k)
+                        for (int m = 1; m <= 3; ++m)
+                            P[3 * (k - 1) + (m - 1)] = (nw[m] == k ? 1.0 : 0.0) - (nw[0] == k ? 1.0 : 0.0);
+                    const double det = P[0] * (P[4] * P[8] - P[5] * P[7]) - P[1] * (P[3] * P[8] - P[5] * P[6]) +
+                                       P[2] * (P[3] * P[7] - P[4] * P[6]);
+                    Pi[0] = (P[4] * P[8] - P[5] * P[7]) / det; Pi[1] = (P[2] * P[7] - P[1] * P[8]) / det;
+                    Pi[2] = (P[1] * P[5] - P[2] * P[4]) / det; Pi[3] = (P[5] * P[6] - P[3] * P[8]) / det;
+                    Pi[4] = (P[0] * P[8] - P[2] * P[6]) / det; Pi[5] = (P[2] * P[3] - P[0] * P[5]) / det;
+                    Pi[6] = (P[3] * P[7] - P[4] * P[6]) / det; Pi[7] = (P[1] * P[6] - P[0] * P[7]) / det;
+                    Pi[8] = (P[0] * P[4] - P[1] * P[3]) / det;
+                    for (int i = 0; i < 3; ++i)
+                        for (int j = 0; j < 3; ++j)
+                            d2[3 * i + j] = Pi[3 * i] * d[j] + Pi[3 * i + 1] * d[3 + j] + Pi[3 * i + 2] * d[6 + j];
+                    auto mm = [&](int i, int j) {
+                        return d2[3 * i] * d2[3 * j] + d2[3 * i + 1] * d2[3 * j + 1] + d2[3 * i + 2] * d2[3 * j + 2];
+                    };
+                    const double dd = d2[0] * (d2[4] * d2[8] - d2[5] * d2[7]) - d2[1] * (d2[3] * d2[8] - d2[5] * d2[6]) +
+                                      d2[2] * (d2[3] * d2[7] - d2[4] * d2[6]);
+                    nh0[t] = make_float4((float)mm(0, 0), (float)mm(0, 1), (float)mm(0, 2), (float)mm(1, 1));
+                    nh1[t] = make_float4((float)mm(1, 2), (float)mm(2, 2), (float)dd, nh1[t].w);
+                }
+            }
+            r.e0 = ne_new0;
+            r.ne = (int)n_edge_idx.size() - ne_new0;
+        }
+        edge_idx.swap(n_edge_idx);
+        edge_la.swap(n_edge_la);
+    }
+
     // ---- order each env's constraint records by a greedy vertex colouring ----
-    std::vector<int> tet_orig(T), edge_orig(E);
+    std::vector<int> tet_orig(T), edge_orig(edge_idx.size());
     {
         std::vector<uint64_t> used;
         std::vector<int> col;
@@ -1006,7 +1196,9 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
             }
             std::vector<int> ord(r.nt);
             std::iota(ord.begin(), ord.end(), 0);
-            std::stable_sort(ord.begin(), ord.end(), [&](int a, int c2) { return col[a] < col[c2]; });
+            std::stable_sort(ord.begin(), ord.end(), [&](int a, int c2) {
+                return col[a] != col[c2] ? col[a] < col[c2] : tet_cls[r.t0 + a] < tet_cls[r.t0 + c2];
+            });
             for (int j = 0; j < r.nt; ++j) tet_orig[r.t0 + j] = r.t0 + ord[j];
             used.assign(r.nv, 0);
             for (int k = 0; k < r.ne; ++k) {
@@ -1028,7 +1220,7 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
             for (size_t i = 0; i < orig.size(); ++i) v[i] = c[orig[i]];
         };
         permute(tet_idx, tet_orig); permute(tet_va, tet_orig); permute(nh0, tet_orig); permute(nh1, tet_orig);
-        permute(tet_vs, tet_orig); permute(edge_idx, edge_orig); permute(edge_la, edge_orig);
+        permute(tet_vs, tet_orig); permute(tet_ed, tet_orig); permute(edge_idx, edge_orig); permute(edge_la, edge_orig);
     }
 
     // ---- share identical constraint tables: envs of one mesh read the same records ----
@@ -1050,12 +1242,12 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
             };
             return a.nv == c.nv && a.nt == c.nt && a.ne == c.ne && a.nf == c.nf &&
                    eq(tet_idx, a.t0, c.t0, a.nt) && eq(tet_va, a.t0, c.t0, a.nt) && eq(nh0, a.t0, c.t0, a.nt) &&
-                   eq(nh1, a.t0, c.t0, a.nt) && eq(tet_vs, a.t0, c.t0, a.nt) &&
+                   eq(nh1, a.t0, c.t0, a.nt) && eq(tet_vs, a.t0, c.t0, a.nt) && eq(tet_ed, a.t0, c.t0, a.nt) &&
                    eq(tet_orig, a.t0, c.t0, a.nt) && eq(edge_idx, a.e0, c.e0, a.ne) && eq(edge_la, a.e0, c.e0, a.ne) &&
                    eq(edge_orig, a.e0, c.e0, a.ne) && eq(tri_idx, a.f0, c.f0, a.nf);
         };
         std::vector<uint2> c_tet_idx; std::vector<float2> c_tet_va; std::vector<float4> c_nh0, c_nh1;
-        std::vector<float> c_tet_vs; std::vector<int> c_tet_orig, c_edge_orig;
+        std::vector<float> c_tet_vs; std::vector<float4> c_tet_ed; std::vector<int> c_tet_orig, c_edge_orig;
         std::vector<unsigned> c_edge_idx; std::vector<float2> c_edge_la; std::vector<uint2> c_tri_idx;
         std::unordered_map<uint64_t, std::vector<int>> seen;
         std::vector<EnvRec> out = env;
@@ -1078,14 +1270,14 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
             seen[h].push_back(e);
             out[e].t0 = (int)c_tet_idx.size(); out[e].e0 = (int)c_edge_idx.size(); out[e].f0 = (int)c_tri_idx.size();
             app(c_tet_idx, tet_idx, r.t0, r.nt); app(c_tet_va, tet_va, r.t0, r.nt); app(c_nh0, nh0, r.t0, r.nt);
-            app(c_nh1, nh1, r.t0, r.nt); app(c_tet_vs, tet_vs, r.t0, r.nt);
+            app(c_nh1, nh1, r.t0, r.nt); app(c_tet_vs, tet_vs, r.t0, r.nt); app(c_tet_ed, tet_ed, r.t0, r.nt);
             app(c_tet_orig, tet_orig, r.t0, r.nt); app(c_edge_idx, edge_idx, r.e0, r.ne);
             app(c_edge_la, edge_la, r.e0, r.ne); app(c_edge_orig, edge_orig, r.e0, r.ne);
             app(c_tri_idx, tri_idx, r.f0, r.nf);
         }
         env = out;
         tet_idx.swap(c_tet_idx); tet_va.swap(c_tet_va); nh0.swap(c_nh0); nh1.swap(c_nh1);
-        tet_vs.swap(c_tet_vs); tet_orig.swap(c_tet_orig); edge_idx.swap(c_edge_idx); edge_la.swap(c_edge_la);
+        tet_vs.swap(c_tet_vs); tet_ed.swap(c_tet_ed); tet_orig.swap(c_tet_orig); edge_idx.swap(c_edge_idx); edge_la.swap(c_edge_la);
         edge_orig.swap(c_edge_orig); tri_idx.swap(c_tri_idx);
     }
 
@@ -1152,6 +1344,7 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
         (st = dalloc(b, &b->d_nh0, nh0.size())) || (st = upload(b->d_nh0, nh0)) ||
         (st = dalloc(b, &b->d_nh1, nh1.size())) || (st = upload(b->d_nh1, nh1)) ||
         (st = dalloc(b, &b->d_tet_vs, tet_vs.size())) || (st = upload(b->d_tet_vs, tet_vs)) ||
+        (st = dalloc(b, &b->d_tet_ed, tet_ed.size())) || (st = upload(b->d_tet_ed, tet_ed)) ||
         (st = dalloc(b, &b->d_edge_idx, edge_idx.size())) || (st = upload(b->d_edge_idx, edge_idx)) ||
         (st = dalloc(b, &b->d_edge_la, edge_la.size())) || (st = upload(b->d_edge_la, edge_la)) ||
         (st = dalloc(b, &b->d_tri_idx, tri_idx.size())) || (st = upload(b->d_tri_idx, tri_idx)) ||
