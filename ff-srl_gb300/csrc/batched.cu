@@ -28,6 +28,7 @@
 // kernel (used for the precision report) sums in double.
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <climits>
 #include <vector>
 #include <algorithm>
 #include <numeric>
@@ -840,6 +841,54 @@ int32_t run(ffsrl_batch* b, int lane, const std::vector<int>& counts, const int*
     return FFSRL_OK;
 }
 
+// Regroups records (already ordered so that records of one colour, hence vertex-disjoint,
+// are contiguous) into the 32-record chunks a warp processes together, choosing for each
+// lane the candidate (within `window` records of the same key) whose vertices add the
+// fewest shared-memory bank collisions: the atomics on vertex v's accumulator words hit
+// bank (3v + component) mod 32, one per vertex per corner and warp; the 16-byte position
+// loads are served eight lanes at a time, colliding on v mod 8.  Only the order changes;
+// every record keeps its own data.
+template <class VertFn, class KeyFn>
+void bank_regroup(std::vector<int>& ord, int corners, VertFn vert, KeyFn key, int window = 64) {
+    const size_t n = ord.size();
+    std::vector<int> out;
+    out.reserve(n);
+    std::vector<char> taken(n, 0);  // by position in ord
+    size_t head = 0;
+    int aload[4][32], qload[4][8];
+    while (out.size() < n) {
+        std::memset(aload, 0, sizeof(aload));
+        for (int j = 0; j < 32 && out.size() < n; ++j) {
+            if ((j & 7) == 0) std::memset(qload, 0, sizeof(qload));
+            while (taken[head]) ++head;
+            const int k0 = key(ord[head]);
+            size_t best = head;
+            int best_cost = INT32_MAX, scanned = 0;
+            for (size_t i = head; i < n && scanned < window; ++i) {
+                if (taken[i]) continue;
+                const int r = ord[i];
+                if (key(r) != k0) break;
+                ++scanned;
+                int cost = 0;
+                for (int c = 0; c < corners; ++c) {
+                    const int v = vert(r, c);
+                    cost += 3 * aload[c][v & 31] + 4 * qload[c][v & 7];
+                }
+                if (cost < best_cost) { best_cost = cost; best = i; if (!cost) break; }
+            }
+            taken[best] = 1;
+            const int r = ord[best];
+            out.push_back(r);
+            for (int c = 0; c < corners; ++c) {
+                const int v = vert(r, c);
+                ++aload[c][v & 31];
+                ++qload[c][v & 7];
+            }
+        }
+    }
+    ord.swap(out);
+}
+
 // Block size of a class: the instantiation, its shared-memory allowance and the grid
 // from the runtime's occupancy calculator.
 constexpr int kLanes = 2;
@@ -985,6 +1034,40 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
         }
     }
 
+    // ---- envs with identical tables and masses: the folding and ordering below are
+    // computed once per distinct env and copied to its duplicates ----
+    std::vector<int> dup_of(N, -1);
+    {
+        auto fnv = [](uint64_t h, const void* p, size_t n) {
+            const unsigned char* c = static_cast<const unsigned char*>(p);
+            for (size_t i = 0; i < n; ++i) { h ^= c[i]; h *= 1099511628211ull; }
+            return h;
+        };
+        auto rng_eq = [](const auto& v, int o1, int o2, int n) {
+            return n == 0 || v.empty() || std::memcmp(&v[o1], &v[o2], sizeof(v[0]) * (size_t)n) == 0;
+        };
+        auto same = [&](const EnvRec& a, const EnvRec& c) {
+            return a.nv == c.nv && a.nt == c.nt && a.ne == c.ne && a.nf == c.nf &&
+                   std::memcmp(hm->inverse_mass + a.v0, hm->inverse_mass + c.v0, sizeof(float) * (size_t)a.nv) == 0 &&
+                   rng_eq(tet_idx, a.t0, c.t0, a.nt) && rng_eq(tet_va, a.t0, c.t0, a.nt) &&
+                   rng_eq(nh0, a.t0, c.t0, a.nt) && rng_eq(nh1, a.t0, c.t0, a.nt) && rng_eq(tet_vs, a.t0, c.t0, a.nt) &&
+                   rng_eq(edge_idx, a.e0, c.e0, a.ne) && rng_eq(edge_la, a.e0, c.e0, a.ne) &&
+                   rng_eq(tri_idx, a.f0, c.f0, a.nf);
+        };
+        std::unordered_map<uint64_t, std::vector<int>> first;
+        for (int e = 0; e < N; ++e) {
+            const EnvRec& r = env[e];
+            uint64_t h = fnv(1469598103934665603ull, &r.nv, sizeof(int));
+            h = fnv(h, &r.nt, sizeof(int));
+            h = fnv(h, &r.ne, sizeof(int));
+            if (r.nt) h = fnv(h, &tet_idx[r.t0], sizeof(uint2) * (size_t)std::min(r.nt, 256));
+            if (r.nv) h = fnv(h, hm->inverse_mass + r.v0, sizeof(float) * (size_t)std::min(r.nv, 256));
+            for (int c : first[h])
+                if (same(r, env[c])) { dup_of[e] = c; break; }
+            if (dup_of[e] < 0) first[h].push_back(e);
+        }
+    }
+
     // ---- static contribution counts (the runtime skips only on degenerate geometry) ----
     const float feps = (float)BEPS;
     std::vector<int> cnt0(V, 0), tri_deg(V, 0);
@@ -1043,6 +1126,26 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
         std::vector<int> owned_n(T, 0), owned(2 * T, -1);
         for (int e = 0; e < N; ++e) {
             EnvRec& r = env[e];
+            if (dup_of[e] >= 0) {
+                const EnvRec& src = env[dup_of[e]];
+                std::copy(tet_idx.begin() + src.t0, tet_idx.begin() + src.t0 + r.nt, tet_idx.begin() + r.t0);
+                std::copy(tet_ed.begin() + src.t0, tet_ed.begin() + src.t0 + r.nt, tet_ed.begin() + r.t0);
+                std::copy(tet_cls.begin() + src.t0, tet_cls.begin() + src.t0 + r.nt, tet_cls.begin() + r.t0);
+                if (nh) {
+                    std::copy(nh0.begin() + src.t0, nh0.begin() + src.t0 + r.nt, nh0.begin() + r.t0);
+                    std::copy(nh1.begin() + src.t0, nh1.begin() + src.t0 + r.nt, nh1.begin() + r.t0);
+                }
+                const int e0 = (int)n_edge_idx.size();
+                for (int k = 0; k < src.ne; ++k) {
+                    const unsigned ix = n_edge_idx[src.e0 + k];
+                    const float2 la = n_edge_la[src.e0 + k];
+                    n_edge_idx.push_back(ix);
+                    n_edge_la.push_back(la);
+                }
+                r.e0 = e0;
+                r.ne = src.ne;
+                continue;
+            }
             // vertex -> incident tets of this env
             adj_start.assign(r.nv + 1, 0);
             for (int t = r.t0; t < r.t0 + r.nt; ++t) {
@@ -1184,6 +1287,12 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
         std::vector<int> col;
         for (int e = 0; e < N; ++e) {
             const EnvRec& r = env[e];
+            if (dup_of[e] >= 0) {
+                const EnvRec& src = env[dup_of[e]];
+                for (int j = 0; j < r.nt; ++j) tet_orig[r.t0 + j] = r.t0 + (tet_orig[src.t0 + j] - src.t0);
+                for (int j = 0; j < r.ne; ++j) edge_orig[r.e0 + j] = r.e0 + (edge_orig[src.e0 + j] - src.e0);
+                continue;
+            }
             used.assign(r.nv, 0);
             col.resize(std::max(r.nt, r.ne));
             for (int t = 0; t < r.nt; ++t) {
@@ -1199,6 +1308,14 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
             std::stable_sort(ord.begin(), ord.end(), [&](int a, int c2) {
                 return col[a] != col[c2] ? col[a] < col[c2] : tet_cls[r.t0 + a] < tet_cls[r.t0 + c2];
             });
+            bank_regroup(
+                ord, 4,
+                [&](int t, int c) {
+                    const uint2 ix = tet_idx[r.t0 + t];
+                    const unsigned w = c < 2 ? ix.x : ix.y;
+                    return (int)((c & 1) ? (w >> 16) : (w & 0xffff));
+                },
+                [&](int t) { return col[t] * 4 + tet_cls[r.t0 + t]; });
             for (int j = 0; j < r.nt; ++j) tet_orig[r.t0 + j] = r.t0 + ord[j];
             used.assign(r.nv, 0);
             for (int k = 0; k < r.ne; ++k) {
@@ -1212,6 +1329,13 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
             ord.resize(r.ne);
             std::iota(ord.begin(), ord.end(), 0);
             std::stable_sort(ord.begin(), ord.end(), [&](int a, int c2) { return col[a] < col[c2]; });
+            bank_regroup(
+                ord, 2,
+                [&](int k, int c) {
+                    const unsigned ix = edge_idx[r.e0 + k];
+                    return (int)(c ? (ix >> 16) : (ix & 0xffff));
+                },
+                [&](int k) { return col[k]; });
             for (int j = 0; j < r.ne; ++j) edge_orig[r.e0 + j] = r.e0 + ord[j];
         }
         auto permute = [](auto& v, const std::vector<int>& orig) {
