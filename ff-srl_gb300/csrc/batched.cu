@@ -94,6 +94,10 @@ template <> struct Store<float> {
     // true when every |component| is below the per-term bound; the sum of magnitudes
     // also carries NaN and infinity into the test
     __device__ static bool in_range(float sum_abs, const Fixed& fx) { return sum_abs * fx.scale < fx.bound; }
+    // a term that merges `terms` constraint contributions may use that many term bounds
+    __device__ static bool in_range(float sum_abs, const Fixed& fx, float terms) {
+        return sum_abs * fx.scale < fx.bound * terms;
+    }
     __device__ static float get(A a, const Fixed& fx) { return __int2float_rn((int)a) * fx.inv; }
 };
 struct __align__(32) dpos { double x, y, z, w; };
@@ -104,6 +108,7 @@ template <> struct Store<double> {
     __device__ static P make(t3<double> v, double w) { P r; r.x = v.x; r.y = v.y; r.z = v.z; r.w = w; return r; }
     __device__ static void add(A* a, double v, const Fixed&) { atomicAdd(a, v); }
     __device__ static bool in_range(double sum_abs, const Fixed&) { return sum_abs < 1.0e300; }
+    __device__ static bool in_range(double sum_abs, const Fixed&, double) { return sum_abs < 1.0e300; }
     __device__ static double get(A a, const Fixed&) { return a; }
 };
 
@@ -124,10 +129,18 @@ template <class R> __device__ __forceinline__ void add3(typename Store<R>::A* ac
     Store<R>::add(acc + 3 * i + 1, d.y, fx);
     Store<R>::add(acc + 3 * i + 2, d.z, fx);
 }
+// The four corrections of one tet; each vertex's term merges at least `terms` of the
+// vertex's counted contributions (the tet's constraints), so it may use that many term
+// bounds and the per-vertex sum still stays within int32.
 template <class R> __device__ __forceinline__ void add3x4(typename Store<R>::A* acc, int ia, int ib, int ic, int id,
                                                           t3<R> dA, t3<R> dB, t3<R> dC, t3<R> dD, bool& bad,
-                                                          const Fixed& fx) {
-    if (!Store<R>::in_range(abs_sum(dA) + abs_sum(dB) + abs_sum(dC) + abs_sum(dD), fx)) { bad = true; return; }
+                                                          const Fixed& fx, R terms) {
+    typedef Store<R> S;
+    if (!(S::in_range(abs_sum(dA), fx, terms) && S::in_range(abs_sum(dB), fx, terms) &&
+          S::in_range(abs_sum(dC), fx, terms) && S::in_range(abs_sum(dD), fx, terms))) {
+        bad = true;
+        return;
+    }
     Store<R>::add(acc + 3 * ia, dA.x, fx); Store<R>::add(acc + 3 * ia + 1, dA.y, fx); Store<R>::add(acc + 3 * ia + 2, dA.z, fx);
     Store<R>::add(acc + 3 * ib, dB.x, fx); Store<R>::add(acc + 3 * ib + 1, dB.y, fx); Store<R>::add(acc + 3 * ib + 2, dB.z, fx);
     Store<R>::add(acc + 3 * ic, dC.x, fx); Store<R>::add(acc + 3 * ic + 1, dC.y, fx); Store<R>::add(acc + 3 * ic + 2, dC.z, fx);
@@ -467,6 +480,7 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
                                     }
                                 }
                             }
+                            const int ktet = k;  // tet constraints merged into each vertex's term
                             if (D.fold) {
                                 // distanceConstraints (integrator.py:65-109) of the edges this tet solves
                                 const float4 ed = __ldg(D.tet_ed + gt);
@@ -476,7 +490,7 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
                                     else k += fold_edge<R>(pa, pc, mA, mC, R(-ed.z), R(ed.w), dA, dC, ia, ic, cnt, it, R(D.ks_distance), &s_dyn_it);
                                 }
                             }
-                            if (k) add3x4<R>(acc, ia, ib, ic, id, dA, dB, dC, dD, bad, fx);
+                            if (k) add3x4<R>(acc, ia, ib, ic, id, dA, dB, dC, dD, bad, fx, R(ktet > 1 ? ktet : 1));
                             if (skip) {
                                 atomicSub(cnt + ia, skip); atomicSub(cnt + ib, skip);
                                 atomicSub(cnt + ic, skip); atomicSub(cnt + id, skip);

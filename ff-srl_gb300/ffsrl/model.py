@@ -400,17 +400,36 @@ class SimModelDO:
 
     def resetFixedModel(self, envNums):
         """Restore the listed envs' vertices and instrument, zero their velocity,
-        predicted positions and grasp (modelDO.py:1589-1622)."""
-        for e in envNums:
-            v0, v1 = int(self.envVertexStart[e]), int(self.envVertexStart[e + 1])
-            self.vertex[v0:v1] = self.initialVertex[v0:v1]
-            self.predictedVertex[v0:v1] = 0.0
-            self.velocity[v0:v1] = 0.0
-            self.activeDragConstraint[v0:v1] = 0.0
-            self.laparoscopeBase[4 * e:4 * e + 4] = self.laparoscopeInitialBase[4 * e:4 * e + 4]
-            self.laparoscopeTip[4 * e:4 * e + 4] = self.laparoscopeInitialTip[4 * e:4 * e + 4]
-            self.laparoscopeDragCutHeat[3 * e:3 * e + 3] = 0
-            self.laparoscopeDragCutHeatUpdate[3 * e:3 * e + 3] = 0
+        predicted positions and grasp (modelDO.py:1589-1622).  Whole-array copies when
+        every env is listed, masked copies otherwise."""
+        ids = sorted({int(e) for e in envNums})
+        if not ids:
+            return
+        if ids[0] < 0 or ids[-1] >= self.numEnvs:
+            raise ValueError("resetFixedModel: env id out of range")
+        if len(ids) == self.numEnvs:
+            self.vertex.copy_(self.initialVertex)
+            self.predictedVertex.zero_()
+            self.velocity.zero_()
+            self.activeDragConstraint.zero_()
+            self.laparoscopeBase.copy_(self.laparoscopeInitialBase)
+            self.laparoscopeTip.copy_(self.laparoscopeInitialTip)
+            self.laparoscopeDragCutHeat.zero_()
+            self.laparoscopeDragCutHeatUpdate.zero_()
+        else:
+            sel = torch.zeros(self.numEnvs, dtype=torch.bool, device=self.device)
+            sel[torch.as_tensor(ids, device=self.device)] = True
+            vm = sel[self.vertexToEnv.long()]
+            self.vertex[vm] = self.initialVertex[vm]
+            self.predictedVertex[vm] = 0.0
+            self.velocity[vm] = 0.0
+            self.activeDragConstraint[vm] = 0.0
+            lm = sel.repeat_interleave(4)
+            self.laparoscopeBase[lm] = self.laparoscopeInitialBase[lm]
+            self.laparoscopeTip[lm] = self.laparoscopeInitialTip[lm]
+            hm = sel.repeat_interleave(3)
+            self.laparoscopeDragCutHeat[hm] = 0
+            self.laparoscopeDragCutHeatUpdate[hm] = 0
         self.transformSimMeshData()
 
     def resetStochasticModel(self, *args, **kwargs):

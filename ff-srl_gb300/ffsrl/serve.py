@@ -70,6 +70,7 @@ class Request:
     disp: np.ndarray
     clamp: int
     t_arrival: float
+    reset: bool = False  # start a new episode: the env returns to its rest state first
     t_done: float = 0.0
     result: np.ndarray | None = None
 
@@ -178,18 +179,25 @@ class EnvServer:
                 for k, v in views.items():
                     v.copy_(snap[k], non_blocking=True)
             else:
-                v0, v1 = int(mm.envVertexStart[s]), int(mm.envVertexStart[s + 1])
-                views["vertex"].copy_(mm.initialVertex[v0:v1])
-                views["velocity"].zero_()
-                views["drag"].zero_()
-                views["base"].copy_(mm.laparoscopeInitialBase[4 * s:4 * s + 4])
-                views["tip"].copy_(mm.laparoscopeInitialTip[4 * s:4 * s + 4])
-                views["incol"].zero_()
-                self.actor_clamp[a] = 0
+                self._rest_state(s, a)
         self.actor_slot[a] = s
         self.slot_actor[s] = a
         self.admissions += 1
         return True
+
+    def _rest_state(self, s: int, a: int) -> None:
+        """Slot s holds actor a's env at rest, instrument at its initial pose, no grasp
+        (on the current stream)."""
+        mm = self.model
+        views = self._slot_views(s)
+        v0, v1 = int(mm.envVertexStart[s]), int(mm.envVertexStart[s + 1])
+        views["vertex"].copy_(mm.initialVertex[v0:v1])
+        views["velocity"].zero_()
+        views["drag"].zero_()
+        views["base"].copy_(mm.laparoscopeInitialBase[4 * s:4 * s + 4])
+        views["tip"].copy_(mm.laparoscopeInitialTip[4 * s:4 * s + 4])
+        views["incol"].zero_()
+        self.actor_clamp[a] = 0
 
     # ------------------------------------------------------------ ticks
     def submit(self, req: Request) -> None:
@@ -238,6 +246,11 @@ class EnvServer:
             return 0
         n = len(batch)
         ids = np.array([self.actor_slot[r.actor] for r in batch], dtype=np.int32)
+        resets = [r for r in batch if r.reset]
+        if resets:
+            with torch.cuda.stream(ln.stream):
+                for r in resets:
+                    self._rest_state(int(self.actor_slot[r.actor]), r.actor)
         acts = np.array([[*r.disp, r.clamp] for r in batch], dtype=np.float32)
         trans = [i for i, r in enumerate(batch) if r.clamp != self.actor_clamp[r.actor]]
         m = self.model
@@ -298,11 +311,13 @@ class EnvServer:
 
     # ------------------------------------------------------------ load generator
     def run_closed_loop(self, duration_s: float, think_hz: float = 60.0, seed: int = 0, warmup_s: float = 0.5,
-                        max_batch: int | None = None) -> dict:
+                        max_batch: int | None = None, episode: int = 16) -> dict:
         """Every actor sends its next request an exponential think time (mean 1/think_hz)
         after its previous result arrives; requests carry U[-0.1, 0.1] cm displacements
-        and a clamp flag that closes on the first request.  Returns latency percentiles
-        (arrival to result on the host) and served env-steps/s over ``duration_s``."""
+        and a clamp flag that closes on the first request of each episode; every
+        ``episode`` requests an actor starts a new episode from the rest state.  Returns
+        latency percentiles (arrival to result on the host) and served env-steps/s over
+        ``duration_s``."""
         rng = np.random.Generator(np.random.PCG64(seed))
         A = self.num_actors
         t0 = time.perf_counter()
@@ -311,13 +326,17 @@ class EnvServer:
         lat, served, t_meas = [], 0, t0 + warmup_s
         t_end = t_meas + duration_s
         ticks, batch_sizes = 0, []
+        sent = np.zeros(A, dtype=np.int64)
         while True:
             now = time.perf_counter()
             if now >= t_end:
                 break
             due = np.nonzero((~waiting) & (nxt <= now))[0]
             for a in due:
-                self.submit(Request(int(a), rng.uniform(-0.1, 0.1, size=3).astype(np.float32), 1, float(nxt[a])))
+                reset = bool(sent[a]) and episode > 0 and sent[a] % episode == 0
+                self.submit(Request(int(a), rng.uniform(-0.1, 0.1, size=3).astype(np.float32), 1, float(nxt[a]),
+                                    reset=reset))
+                sent[a] += 1
             waiting[due] = True
             for r in self.poll():
                 waiting[r.actor] = False
@@ -353,4 +372,5 @@ class EnvServer:
                 "served_env_steps_per_s": served / duration_s, "requests": served, "ticks": ticks,
                 "mean_batch": float(np.mean(batch_sizes)) if batch_sizes else 0.0, "actors": A,
                 "slots": self.num_slots, "evictions": self.evictions, "budget_bytes_used": self.budget_used,
+                "episode_requests": episode, "env_status_nonzero": int((self.plan.env_status() != 0).sum()),
                 **({"tick_profile": prof} if prof else {})}

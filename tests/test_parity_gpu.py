@@ -232,3 +232,19 @@ def test_precision_float32_vs_float64(gpu):
     assert rep["finite"]
     assert rep["max_pos_err_rel"] < POS_TOL
     assert rep["volume_err_f64"]["max"] < 0.5
+
+
+def test_reset_fixed_model_subset_and_all(gpu):
+    # resetFixedModel restores exactly the listed envs (masked path) or all of them
+    meshes, _ = sc.mixed_meshes(3, pool_size=3, seed=2, t_lo=200, t_hi=600)
+    m, _ = sc.liver_model("cuda:0", 3, meshes=meshes)
+    integ = SimIntegratorDO("cuda:0")
+    integ.stepModel(m, 2)
+    moved = m.vertex.clone()
+    m.resetFixedModel([1])
+    s0, s1 = m.envSlice(0), m.envSlice(1)
+    assert torch.equal(m.vertex[s1], m.initialVertex[s1])
+    assert torch.equal(m.vertex[s0], moved[s0])
+    assert float(m.velocity[s1].abs().max()) == 0.0
+    m.resetFixedModel(range(3))
+    assert torch.equal(m.vertex, m.initialVertex)

@@ -104,3 +104,23 @@ def test_closed_loop_reports_latency(gpu):
     assert st["requests"] > 8
     assert 0 < st["p50_ms"] <= st["p99_ms"]
     assert st["served_env_steps_per_s"] > 0
+
+
+@pytest.mark.gpu
+def test_episode_reset_restarts_from_rest(gpu):
+    # actor 3 steps three times, then starts a new episode with displacement d; actor 0
+    # (same mesh) takes d as its first request: both end in the same state
+    from ffsrl.serve import Request
+    actors = [0, 1, 2, 0]
+    srv = _serve(actors)
+    d = [0.04, -0.02, 0.01]
+    _run(srv, [[(3, [0.05, 0.0, 0.0], 1)], [(3, [0.0, 0.05, 0.0], 1)], [(3, [0.0, 0.0, 0.05], 1)]])
+    srv.submit(Request(3, np.asarray(d, dtype=np.float32), 1, 0.0, reset=True))
+    srv.submit(Request(0, np.asarray(d, dtype=np.float32), 1, 0.0))
+    done = []
+    while srv.pending or any(ln.batch for ln in srv.lanes):
+        srv.launch()
+        done += srv.poll()
+    res = {r.actor: r.result for r in done}
+    assert np.array_equal(res[3], res[0])
+    assert np.array_equal(_state(srv, 3), _state(srv, 0))
