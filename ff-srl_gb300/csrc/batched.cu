@@ -94,6 +94,13 @@ template <> struct Store<float> {
     // true when every |component| is below the per-term bound; the sum of magnitudes
     // also carries NaN and infinity into the test
     __device__ static bool in_range(float sum_abs, const Fixed& fx) { return sum_abs * fx.scale < fx.bound; }
+    // the tet path forms its corrections already multiplied by the power-of-two scale
+    // (exact), so only the conversion and the bound remain
+    __device__ static float prescale(const Fixed& fx) { return fx.scale; }
+    __device__ static void add_scaled(A* a, float v) { atomicAdd(a, (unsigned)__float2int_rn(v)); }
+    __device__ static bool in_range_scaled(float sum_abs, const Fixed& fx, float terms) {
+        return sum_abs < fx.bound * terms;
+    }
     // a term that merges `terms` constraint contributions may use that many term bounds
     __device__ static bool in_range(float sum_abs, const Fixed& fx, float terms) {
         return sum_abs * fx.scale < fx.bound * terms;
@@ -109,6 +116,9 @@ template <> struct Store<double> {
     __device__ static void add(A* a, double v, const Fixed&) { atomicAdd(a, v); }
     __device__ static bool in_range(double sum_abs, const Fixed&) { return sum_abs < 1.0e300; }
     __device__ static bool in_range(double sum_abs, const Fixed&, double) { return sum_abs < 1.0e300; }
+    __device__ static double prescale(const Fixed&) { return 1.0; }
+    __device__ static void add_scaled(A* a, double v) { atomicAdd(a, v); }
+    __device__ static bool in_range_scaled(double sum_abs, const Fixed&, double) { return sum_abs < 1.0e300; }
     __device__ static double get(A a, const Fixed&) { return a; }
 };
 
@@ -129,22 +139,23 @@ template <class R> __device__ __forceinline__ void add3(typename Store<R>::A* ac
     Store<R>::add(acc + 3 * i + 1, d.y, fx);
     Store<R>::add(acc + 3 * i + 2, d.z, fx);
 }
-// The four corrections of one tet; each vertex's term merges at least `terms` of the
+// The four corrections of one tet, already multiplied by the fixed-point scale; each
+// vertex's term merges at least `terms` of the
 // vertex's counted contributions (the tet's constraints), so it may use that many term
 // bounds and the per-vertex sum still stays within int32.
 template <class R> __device__ __forceinline__ void add3x4(typename Store<R>::A* acc, int ia, int ib, int ic, int id,
                                                           t3<R> dA, t3<R> dB, t3<R> dC, t3<R> dD, bool& bad,
                                                           const Fixed& fx, R terms) {
     typedef Store<R> S;
-    if (!(S::in_range(abs_sum(dA), fx, terms) && S::in_range(abs_sum(dB), fx, terms) &&
-          S::in_range(abs_sum(dC), fx, terms) && S::in_range(abs_sum(dD), fx, terms))) {
+    if (!(S::in_range_scaled(abs_sum(dA), fx, terms) && S::in_range_scaled(abs_sum(dB), fx, terms) &&
+          S::in_range_scaled(abs_sum(dC), fx, terms) && S::in_range_scaled(abs_sum(dD), fx, terms))) {
         bad = true;
         return;
     }
-    Store<R>::add(acc + 3 * ia, dA.x, fx); Store<R>::add(acc + 3 * ia + 1, dA.y, fx); Store<R>::add(acc + 3 * ia + 2, dA.z, fx);
-    Store<R>::add(acc + 3 * ib, dB.x, fx); Store<R>::add(acc + 3 * ib + 1, dB.y, fx); Store<R>::add(acc + 3 * ib + 2, dB.z, fx);
-    Store<R>::add(acc + 3 * ic, dC.x, fx); Store<R>::add(acc + 3 * ic + 1, dC.y, fx); Store<R>::add(acc + 3 * ic + 2, dC.z, fx);
-    Store<R>::add(acc + 3 * id, dD.x, fx); Store<R>::add(acc + 3 * id + 1, dD.y, fx); Store<R>::add(acc + 3 * id + 2, dD.z, fx);
+    S::add_scaled(acc + 3 * ia, dA.x); S::add_scaled(acc + 3 * ia + 1, dA.y); S::add_scaled(acc + 3 * ia + 2, dA.z);
+    S::add_scaled(acc + 3 * ib, dB.x); S::add_scaled(acc + 3 * ib + 1, dB.y); S::add_scaled(acc + 3 * ib + 2, dB.z);
+    S::add_scaled(acc + 3 * ic, dC.x); S::add_scaled(acc + 3 * ic + 1, dC.y); S::add_scaled(acc + 3 * ic + 2, dC.z);
+    S::add_scaled(acc + 3 * id, dD.x); S::add_scaled(acc + 3 * id + 1, dD.y); S::add_scaled(acc + 3 * id + 2, dD.z);
 }
 
 template <class R> struct Dev {
@@ -255,11 +266,11 @@ template <class R> __device__ __forceinline__ bool capsule_response(t3<R> tip, t
 }
 
 // One distance constraint between two of a tet's vertices, added to the tet's corrections
-// (u gets -d m_u, v gets +d m_v).  Returns 1 when it contributed.  A degenerate length
+// (u gets -d m_u, v gets +d m_v), multiplied by the fixed-point scale `sc`.  Returns 1 when it contributed.  A degenerate length
 // decrements the two static counts and records the iteration in *dyn_it.
 template <class R> __device__ __forceinline__ int fold_edge(t3<R> pu, t3<R> pv, R mu, R mv, R L0, R active,
                                                             t3<R>& du, t3<R>& dv, int iu, int iv, int* cnt,
-                                                            int it, R ks, int* dyn_it) {
+                                                            int it, R ks, int* dyn_it, R sc) {
     const R w = mu + mv;
     if (w < R(BEPS)) return 0;  // never counted
     const t3<R> dir = pv - pu;
@@ -271,7 +282,7 @@ template <class R> __device__ __forceinline__ int fold_edge(t3<R> pu, t3<R> pv, 
     }
     const R rl = rsqrt_(dd);
     const R C = dd * rl - L0;
-    const t3<R> d = dir * (-C * rl * ks * active * rcp(w));
+    const t3<R> d = dir * (-C * rl * ks * active * rcp(w) * sc);
     du = du - d * mu;
     dv = dv + d * mv;
     return 1;
@@ -307,6 +318,7 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
     const R dt = R(D.dt);
     const unsigned fl = D.flags;
     const Fixed fx = D.fx;
+    const R sc = S::prescale(fx);  // power of two: scaling a product by it is exact
     // Neo-Hookean constants, hoisted with the reference's association order:
     // C offset invDev/invVol, and compliance/dT/dT (the per-tet /V0 stays per tet)
     const R nh_off = (R(1) / R(D.dev_c)) / (R(1) / R(D.vol_c));
@@ -431,7 +443,7 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
                                     } else {
                                         if (fl & FFSRL_VOLUME) {
                                             R C = R(va.x) - fabs(s6) * R(1.0 / 6.0);
-                                            R dl = -R(D.ks_volume) * active * C * rcp(wq);
+                                            const R dl = -R(D.ks_volume) * active * C * rcp(wq) * sc;
                                             dA = q0 * dl * mA; dB = q1 * dl * mB; dC = q2 * dl * mC; dD = q3 * dl * mD;
                                             ++k;
                                         }
@@ -442,7 +454,8 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
                                             R C = s6 / R(6) - R(__ldg(D.tet_vs + gt));
                                             R dl = -(C + alpha * lam) / (wq + alpha);
                                             D.tet_lambda[ot] = float(lam + dl);
-                                            dA = dA + q0 * dl * mA; dB = dB + q1 * dl * mB; dC = dC + q2 * dl * mC; dD = dD + q3 * dl * mD;
+                                            const R dls = dl * sc;
+                                            dA = dA + q0 * dls * mA; dB = dB + q1 * dls * mB; dC = dC + q2 * dls * mC; dD = dD + q3 * dls * mD;
                                             ++k;
                                         }
                                     }
@@ -472,8 +485,8 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
                                     if (wD < R(BEPS)) {
                                         if (anym) ++skip;
                                     } else {
-                                        const R ce = -rs * rcp(wD + nh_uD * inv_rv) * rsi;
-                                        const R ch = dlH * detD;
+                                        const R ce = -rs * rcp(wD + nh_uD * inv_rv) * rsi * sc;
+                                        const R ch = dlH * detD * sc;
                                         dA = dA + (q0 * (ch * mA) + e0 * (ce * mA)); dB = dB + (q1 * (ch * mB) + e1 * (ce * mB));
                                         dC = dC + (q2 * (ch * mC) + e2 * (ce * mC)); dD = dD + (q3 * (ch * mD) + e3 * (ce * mD));
                                         ++k;
@@ -484,10 +497,10 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
                             if (D.fold) {
                                 // distanceConstraints (integrator.py:65-109) of the edges this tet solves
                                 const float4 ed = __ldg(D.tet_ed + gt);
-                                if (ed.y != 0.0f) k += fold_edge<R>(pa, pb, mA, mB, R(ed.x), R(ed.y), dA, dB, ia, ib, cnt, it, R(D.ks_distance), &s_dyn_it);
+                                if (ed.y != 0.0f) k += fold_edge<R>(pa, pb, mA, mB, R(ed.x), R(ed.y), dA, dB, ia, ib, cnt, it, R(D.ks_distance), &s_dyn_it, sc);
                                 if (ed.w != 0.0f) {
-                                    if (ed.z > 0.0f) k += fold_edge<R>(pc, pd, mC, mD, R(ed.z), R(ed.w), dC, dD, ic, id, cnt, it, R(D.ks_distance), &s_dyn_it);
-                                    else k += fold_edge<R>(pa, pc, mA, mC, R(-ed.z), R(ed.w), dA, dC, ia, ic, cnt, it, R(D.ks_distance), &s_dyn_it);
+                                    if (ed.z > 0.0f) k += fold_edge<R>(pc, pd, mC, mD, R(ed.z), R(ed.w), dC, dD, ic, id, cnt, it, R(D.ks_distance), &s_dyn_it, sc);
+                                    else k += fold_edge<R>(pa, pc, mA, mC, R(-ed.z), R(ed.w), dA, dC, ia, ic, cnt, it, R(D.ks_distance), &s_dyn_it, sc);
                                 }
                             }
                             if (k) add3x4<R>(acc, ia, ib, ic, id, dA, dB, dC, dD, bad, fx, R(ktet > 1 ? ktet : 1));
