@@ -40,9 +40,10 @@ __device__ __forceinline__ void refit_node(const ffsrl_bvh& b, const float* __re
             lo = vmin(pA, vmin(pB, vmin(pC, lo)));
             hi = vmax(pA, vmax(pB, vmax(pC, hi)));
             if (b.tri_pos) {
-                float* q = b.tri_pos + 9 * (fofs + first + k);
-                q[0] = pA.x; q[1] = pA.y; q[2] = pA.z; q[3] = pB.x; q[4] = pB.y; q[5] = pB.z;
-                q[6] = pC.x; q[7] = pC.y; q[8] = pC.z;
+                float4* q = reinterpret_cast<float4*>(b.tri_pos) + 3 * (fofs + first + k);
+                q[0] = make_float4(pA.x, pA.y, pA.z, pB.x);
+                q[1] = make_float4(pB.y, pB.z, pC.x, pC.y);
+                q[2] = make_float4(pC.z, 0.0f, 0.0f, 0.0f);
             }
         }
         if (b.node_box) {
@@ -170,16 +171,19 @@ __device__ __forceinline__ bool slab(v3 ro, v3 rd, v3 lo, v3 hi, float& tnear) {
 // Node test of the traversal: intersectAABB's hit && tmin < tMin (render.py:452-454).
 // The slab distances are first formed with the ray's reciprocal direction; when every
 // part of the decision is farther from its threshold than the rounding of that form can
-// move it (8 float ulps of the largest distance), the decision equals the reference's.
+// move it (8 float ulps of the summed distances), the decision equals the reference's.
 // Otherwise -- and for non-finite distances -- the reference's divisions decide.
 __device__ __forceinline__ bool node_hit(v3 ro, v3 rd, v3 inv, v3 lo, v3 hi, float tMin) {
     float t1 = (lo.x - ro.x) * inv.x, t2 = (hi.x - ro.x) * inv.x;
     float t3 = (lo.y - ro.y) * inv.y, t4 = (hi.y - ro.y) * inv.y;
     float t5 = (lo.z - ro.z) * inv.z, t6 = (hi.z - ro.z) * inv.z;
-    float m = fmaxf(fmaxf(fmaxf(fabsf(t1), fabsf(t2)), fmaxf(fabsf(t3), fabsf(t4))), fmaxf(fabsf(t5), fabsf(t6)));
+    // the sum of magnitudes bounds every distance and is infinite or NaN when any of them
+    // is, so the fast path only sees finite values, where fminf/fmaxf pick what the
+    // reference's comparisons pick (up to the sign of a zero, which no test below sees)
+    float m = ((fabsf(t1) + fabsf(t2)) + (fabsf(t3) + fabsf(t4))) + (fabsf(t5) + fabsf(t6));
     if (m < 3.0e37f) {
-        float tmin = fmax_ref(fmax_ref(fmin_ref(t1, t2), fmin_ref(t3, t4)), fmin_ref(t5, t6));
-        float tmax = fmin_ref(fmin_ref(fmax_ref(t1, t2), fmax_ref(t3, t4)), fmax_ref(t5, t6));
+        float tmin = fmaxf(fmaxf(fminf(t1, t2), fminf(t3, t4)), fminf(t5, t6));
+        float tmax = fminf(fminf(fmaxf(t1, t2), fmaxf(t3, t4)), fmaxf(t5, t6));
         float g = m * 4.76837158e-7f;  // 8 * 2^-24 * m
         // a certainly-false part decides a miss; all parts certainly true decide a hit
         if (tmax < -g || tmax - tmin < -2.0f * g || tmin > tMin + g) return false;
@@ -212,7 +216,7 @@ struct EnvView {
     const int* left; const int* first; const int* count; const int* tri;
     const float* amin; const float* amax;
     const float4* box;   // packed node boxes of the env (or null)
-    const float* tpos;   // leaf triangles of the env in tri-map order (or null)
+    const float4* tpos;  // leaf triangles of the env in tri-map order, 3 float4 each (or null)
     long long fofs;
     int nn;  // nodes in the topology
 };
@@ -228,7 +232,7 @@ __device__ __forceinline__ EnvView env_view(const ffsrl_bvh& b, int e) {
     v.fofs = b.env_face_offset[e];
     v.nn = b.topo_node_offset[topo + 1] - n0;
     v.box = b.node_box ? reinterpret_cast<const float4*>(b.node_box) + 2 * base : nullptr;
-    v.tpos = b.tri_pos ? b.tri_pos + 9 * v.fofs : nullptr;
+    v.tpos = b.tri_pos ? reinterpret_cast<const float4*>(b.tri_pos) + 3 * v.fofs : nullptr;
     return v;
 }
 
@@ -258,10 +262,11 @@ __device__ int query_packed(const EnvView& ev, v3 ro, v3 rd, float& t_hit, v3& p
                 int first = fc >> 8, cnt = fc & 255;
                 if (cnt == 255) cnt = ev.count[node];
                 for (int k = 0; k < cnt; ++k) {
-                    const float* q = ev.tpos + 9ll * (first + k);
-                    v3 A = mk(__ldg(q), __ldg(q + 1), __ldg(q + 2));
-                    v3 B = mk(__ldg(q + 3), __ldg(q + 4), __ldg(q + 5));
-                    v3 C = mk(__ldg(q + 6), __ldg(q + 7), __ldg(q + 8));
+                    const float4* q = ev.tpos + 3ll * (first + k);
+                    const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2);
+                    v3 A = mk(q0.x, q0.y, q0.z);
+                    v3 B = mk(q0.w, q1.x, q1.y);
+                    v3 C = mk(q1.z, q1.w, q2.x);
                     v3 p;
                     float t = moller_trumbore(A, B, C, ro, rd, p);
                     if (t < tMin && t > 0.0f) {
@@ -469,6 +474,10 @@ int32_t check_bvh(const ffsrl_bvh* b) {
         !b->topo_node_offset || !b->topo_tri_offset || !b->topo_max_level || !b->left_node || !b->first_tri_id ||
         !b->tri_count || !b->level || !b->tri_id || !b->aabb_min || !b->aabb_max || b->total_env_nodes <= 0)
         return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_bvh: missing arrays or empty");
+    if (!b->node_box != !b->tri_pos)
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_bvh: node_box and tri_pos go together");
+    if ((((uintptr_t)b->node_box) & 15) || (((uintptr_t)b->tri_pos) & 15))
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_bvh: node_box and tri_pos must be 16-byte aligned");
     return FFSRL_OK;
 }
 

@@ -148,7 +148,7 @@ class SimBVH:
         self.aabbMax = torch.as_tensor(amax, dtype=torch.float32, device=dev).clone()
         # traversal copies the refit writes: packed node boxes and leaf triangles in tri-map order
         self.nodeBox = torch.zeros((len(amin), 8), dtype=torch.float32, device=dev)
-        self.triPos = torch.zeros((m.numAllVisFaces, 9), dtype=torch.float32, device=dev)
+        self.triPos = torch.zeros((m.numAllVisFaces, 12), dtype=torch.float32, device=dev)
         self.numNodes = int(nn[0])
         self.numAllNodes = int(env_nodes.sum())
         self.maxLevel = int(max(t["max_level"] for t in topos))

@@ -140,10 +140,11 @@ typedef struct {
     const int32_t* topo_level_offset;/* [M+1] */
     /* optional traversal copies written by the refit (both or neither):
        node_box[2n] = (min.xyz, leftNode), node_box[2n+1] = (max.xyz, first*256 + min(count,255))
-       per env node; tri_pos[9k..9k+8] = the three vertices of the k-th triangle in
-       tri-map order (k = env_face_offset[e] + position in the env's topology map) */
+       per env node; tri_pos[12k..12k+8] = the three vertices of the k-th triangle in
+       tri-map order (k = env_face_offset[e] + position in the env's topology map),
+       12k+9..12k+11 padding, so each triangle is three 16-byte loads; 16-byte aligned */
     float* node_box;                 /* [8 * total_env_nodes] */
-    float* tri_pos;                  /* [9 * total env faces] */
+    float* tri_pos;                  /* [12 * total env faces] */
 } ffsrl_bvh;
 
 /* ---- ray-cast renderer (render.py:826-1196) ------------------------------------ */
