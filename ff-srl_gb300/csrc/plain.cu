@@ -408,6 +408,27 @@ __global__ void k_move_tool_envs(float* base, float* tip, const float* __restric
     st3(tip, slot, ld3(tip, slot) + d);
 }
 
+// one block per listed env: rest positions, zero velocity and grasp, initial instrument
+__global__ void k_reset_envs(float* vertex, float* velocity, float* drag, const float* __restrict__ init,
+                             float* base, float* tip, const float* __restrict__ init_base,
+                             const float* __restrict__ init_tip, int* in_collision, const int* __restrict__ vstart,
+                             const int* __restrict__ ids, int num_envs) {
+    const int e = ids[blockIdx.x];
+    if (e < 0 || e >= num_envs) return;
+    const long long v0 = vstart[e], v1 = vstart[e + 1];
+    for (long long i = 3 * v0 + threadIdx.x; i < 3 * v1; i += blockDim.x) {
+        vertex[i] = init[i];
+        velocity[i] = 0.0f;
+    }
+    for (long long v = v0 + threadIdx.x; v < v1; v += blockDim.x) drag[v] = 0.0f;
+    if (threadIdx.x < 12) {
+        const long long k = 12ll * e + threadIdx.x;
+        base[k] = init_base[k];
+        tip[k] = init_tip[k];
+    }
+    if (threadIdx.x == 0) in_collision[e] = 0;
+}
+
 __global__ void k_move_tool(float* base, float* tip, const float* __restrict__ disp, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;  // one thread per (env, entry)
     if (i >= 4 * n) return;
@@ -586,6 +607,22 @@ extern "C" int32_t ffsrl_move_tool_envs(float* laparoscope_base, float* laparosc
     k_move_tool_envs<<<grid_for(4ll * n, kBlock), kBlock, 0, (cudaStream_t)stream>>>(laparoscope_base, laparoscope_tip,
                                                                                     disp, env_ids, n, num_envs);
     FFSRL_LAUNCH_CHECK("ffsrl_move_tool_envs");
+    return FFSRL_OK;
+}
+
+extern "C" int32_t ffsrl_reset_envs(float* vertex, float* velocity, float* active_drag, const float* initial_vertex,
+                                    float* laparoscope_base, float* laparoscope_tip, const float* initial_base,
+                                    const float* initial_tip, int32_t* in_collision, const int32_t* env_vertex_start,
+                                    const int32_t* env_ids, int32_t n, int32_t num_envs, void* stream) {
+    if (n < 0 || num_envs < 0 ||
+        (n > 0 && (!vertex || !velocity || !active_drag || !initial_vertex || !laparoscope_base || !laparoscope_tip ||
+                   !initial_base || !initial_tip || !in_collision || !env_vertex_start || !env_ids)))
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_reset_envs");
+    if (n == 0) return FFSRL_OK;
+    k_reset_envs<<<n, 256, 0, (cudaStream_t)stream>>>(vertex, velocity, active_drag, initial_vertex, laparoscope_base,
+                                                       laparoscope_tip, initial_base, initial_tip, in_collision,
+                                                       env_vertex_start, env_ids, num_envs);
+    FFSRL_LAUNCH_CHECK("ffsrl_reset_envs");
     return FFSRL_OK;
 }
 

@@ -417,19 +417,19 @@ class SimModelDO:
             self.laparoscopeDragCutHeat.zero_()
             self.laparoscopeDragCutHeatUpdate.zero_()
         else:
+            self.require_cuda()
+            idt = torch.as_tensor(ids, dtype=torch.int32, device=self.device)
+            check(lib().ffsrl_reset_envs(ptr(self.vertex), ptr(self.velocity), ptr(self.activeDragConstraint),
+                                         ptr(self.initialVertex), ptr(self.laparoscopeBase), ptr(self.laparoscopeTip),
+                                         ptr(self.laparoscopeInitialBase), ptr(self.laparoscopeInitialTip),
+                                         ptr(self.laparoscopeInCollision), ptr(self.envVertexStartT), ptr(idt),
+                                         len(ids), self.numEnvs, _lib.stream_handle(None)))
             sel = torch.zeros(self.numEnvs, dtype=torch.bool, device=self.device)
-            sel[torch.as_tensor(ids, device=self.device)] = True
-            vm = sel[self.vertexToEnv.long()]
-            self.vertex[vm] = self.initialVertex[vm]
-            self.predictedVertex[vm] = 0.0
-            self.velocity[vm] = 0.0
-            self.activeDragConstraint[vm] = 0.0
-            lm = sel.repeat_interleave(4)
-            self.laparoscopeBase[lm] = self.laparoscopeInitialBase[lm]
-            self.laparoscopeTip[lm] = self.laparoscopeInitialTip[lm]
+            sel[idt.long()] = True
+            self.predictedVertex.masked_fill_(sel[self.vertexToEnv.long()].unsqueeze(1), 0.0)
             hm = sel.repeat_interleave(3)
-            self.laparoscopeDragCutHeat[hm] = 0
-            self.laparoscopeDragCutHeatUpdate[hm] = 0
+            self.laparoscopeDragCutHeat.masked_fill_(hm, 0)
+            self.laparoscopeDragCutHeatUpdate.masked_fill_(hm, 0)
         self.transformSimMeshData()
 
     def resetStochasticModel(self, *args, **kwargs):

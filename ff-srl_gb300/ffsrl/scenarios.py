@@ -67,12 +67,12 @@ def place_instruments(model: SimModelDO, meshes: list, dip: float = 0.1) -> np.n
     return pts
 
 
-def beam_model(device, num_envs=1, neo=False, xpbd=False, **kw) -> tuple[SimModelDO, list]:
+def beam_model(device, num_envs=1, neo=False, xpbd=False, mesh=None, **kw) -> tuple[SimModelDO, list]:
     """Config 0: 10x4x4 beam of 1 cm cubes, 275 vertices, 800 tets, x=0 face fixed,
     1 g/cm^3, dt 1/60, 8 substeps x 10 iterations.  Plain form: the reference DO step with
     kS = 1; the compliant form (xpbd=True) runs XPBD distance (alpha 1e-6) and volume
     (alpha 0)."""
-    mesh = mg.beam()
+    mesh = mg.beam() if mesh is None else mesh
     flags = L.REFERENCE_STEP
     if xpbd:
         flags = (flags & ~(L.DISTANCE | L.VOLUME)) | L.DISTANCE_XPBD | L.VOLUME_XPBD

@@ -86,6 +86,10 @@ class _Lane:
     res_d: torch.Tensor
     gids_d: torch.Tensor
     gclamp_d: torch.Tensor
+    rst_h: torch.Tensor
+    rst_d: torch.Tensor
+    gids_h: torch.Tensor
+    gclamp_h: torch.Tensor
     event: torch.cuda.Event
     batch: list = field(default_factory=list)
 
@@ -136,6 +140,10 @@ class EnvServer:
                             res_d=torch.empty((n, 4), dtype=torch.float32, device=self.device),
                             gids_d=torch.empty(n, dtype=torch.int32, device=self.device),
                             gclamp_d=torch.empty(n, dtype=torch.int32, device=self.device),
+                            rst_h=torch.empty(n, dtype=torch.int32, **pin),
+                            rst_d=torch.empty(n, dtype=torch.int32, device=self.device),
+                            gids_h=torch.empty(n, dtype=torch.int32, **pin),
+                            gclamp_h=torch.empty(n, dtype=torch.int32, **pin),
                             event=torch.cuda.Event())
                       for _ in range(lanes)]
         self.pending: list[Request] = []
@@ -246,11 +254,10 @@ class EnvServer:
             return 0
         n = len(batch)
         ids = np.array([self.actor_slot[r.actor] for r in batch], dtype=np.int32)
-        resets = [r for r in batch if r.reset]
-        if resets:
-            with torch.cuda.stream(ln.stream):
-                for r in resets:
-                    self._rest_state(int(self.actor_slot[r.actor]), r.actor)
+        resets = [int(self.actor_slot[r.actor]) for r in batch if r.reset]
+        for r in batch:
+            if r.reset:
+                self.actor_clamp[r.actor] = 0  # the grasp closes again below
         acts = np.array([[*r.disp, r.clamp] for r in batch], dtype=np.float32)
         trans = [i for i, r in enumerate(batch) if r.clamp != self.actor_clamp[r.actor]]
         m = self.model
@@ -264,15 +271,25 @@ class EnvServer:
             ln.act_h[:n].copy_(torch.from_numpy(acts))
             ln.ids_d[:n].copy_(ln.ids_h[:n], non_blocking=True)
             ln.act_d[:n].copy_(ln.act_h[:n], non_blocking=True)
+            if resets:
+                nr = len(resets)
+                ln.rst_h[:nr].copy_(torch.as_tensor(resets, dtype=torch.int32))
+                ln.rst_d[:nr].copy_(ln.rst_h[:nr], non_blocking=True)
+                check(lib().ffsrl_reset_envs(ptr(m.vertex), ptr(m.velocity), ptr(m.activeDragConstraint),
+                                             ptr(m.initialVertex), ptr(m.laparoscopeBase), ptr(m.laparoscopeTip),
+                                             ptr(m.laparoscopeInitialBase), ptr(m.laparoscopeInitialTip),
+                                             ptr(m.laparoscopeInCollision), ptr(m.envVertexStartT), ptr(ln.rst_d), nr,
+                                             m.numEnvs, s))
             disp = ln.act_d[:n, :3].contiguous()
             check(lib().ffsrl_move_tool_envs(ptr(m.laparoscopeBase), ptr(m.laparoscopeTip), ptr(disp),
                                              ptr(ln.ids_d), n, m.numEnvs, s))
             if trans:
-                t = torch.tensor(trans, dtype=torch.long)
-                gids = torch.from_numpy(ids)[t]
-                gcl = torch.tensor([batch[i].clamp for i in trans], dtype=torch.int32)
-                ln.gids_d[:len(trans)].copy_(gids)
-                ln.gclamp_d[:len(trans)].copy_(gcl)
+                # pinned staging: a copy from pageable memory would wait for the stream
+                nt = len(trans)
+                ln.gids_h[:nt].copy_(torch.from_numpy(ids[np.asarray(trans)]))
+                ln.gclamp_h[:nt].copy_(torch.tensor([batch[i].clamp for i in trans], dtype=torch.int32))
+                ln.gids_d[:nt].copy_(ln.gids_h[:nt], non_blocking=True)
+                ln.gclamp_d[:nt].copy_(ln.gclamp_h[:nt], non_blocking=True)
                 check(lib().ffsrl_grasp_nearest_envs(ptr(m.vertex), ptr(m.graspCandStartT), ptr(m.graspCand),
                                                      ptr(m.laparoscopeTip), ptr(ln.gclamp_d), m.globalLaparoscopeDragLookupRadius,
                                                      ptr(m.activeDragConstraint), ptr(ln.gids_d), len(trans), m.numEnvs, s))

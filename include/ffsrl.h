@@ -230,6 +230,15 @@ int32_t ffsrl_grasp_nearest_envs(const float* positions, const int32_t* cand_sta
    [0, num_envs) are skipped. */
 int32_t ffsrl_move_tool_envs(float* laparoscope_base, float* laparoscope_tip, const float* disp,
                              const int32_t* env_ids, int32_t n, int32_t num_envs, void* stream);
+/* Return the listed envs to their rest state (resetFixedModel, modelDO.py:1589-1622, for
+   an env list): vertex = initial_vertex and velocity = 0 over each env's vertex range
+   [env_vertex_start[e], env_vertex_start[e+1]), grasp flags 0, instrument base/tip =
+   their initial values, contact count 0.  Device arrays; ids outside [0, num_envs) are
+   skipped.  One launch for any number of envs. */
+int32_t ffsrl_reset_envs(float* vertex, float* velocity, float* active_drag, const float* initial_vertex,
+                         float* laparoscope_base, float* laparoscope_tip, const float* initial_base,
+                         const float* initial_tip, int32_t* in_collision, const int32_t* env_vertex_start,
+                         const int32_t* env_ids, int32_t n, int32_t num_envs, void* stream);
 /* Rigidly translate each env's instrument (4 bases + 4 tips) by disp[3e..3e+2]. */
 int32_t ffsrl_move_tool(float* laparoscope_base, float* laparoscope_tip, const float* disp, int32_t num_envs,
                         void* stream);
