@@ -411,7 +411,8 @@ __global__ void k_move_tool_envs(float* base, float* tip, const float* __restric
 // one block per listed env: rest positions, zero velocity and grasp, initial instrument
 __global__ void k_reset_envs(float* vertex, float* velocity, float* drag, const float* __restrict__ init,
                              float* base, float* tip, const float* __restrict__ init_base,
-                             const float* __restrict__ init_tip, int* in_collision, const int* __restrict__ vstart,
+                             const float* __restrict__ init_tip, int* in_collision, float* xform,
+                             const float* __restrict__ init_xform, const int* __restrict__ vstart,
                              const int* __restrict__ ids, int num_envs) {
     const int e = ids[blockIdx.x];
     if (e < 0 || e >= num_envs) return;
@@ -427,6 +428,7 @@ __global__ void k_reset_envs(float* vertex, float* velocity, float* drag, const 
         tip[k] = init_tip[k];
     }
     if (threadIdx.x == 0) in_collision[e] = 0;
+    if (xform && threadIdx.x < 112) xform[112ll * e + threadIdx.x] = init_xform[112ll * e + threadIdx.x];
 }
 
 __global__ void k_move_tool(float* base, float* tip, const float* __restrict__ disp, int n) {
@@ -612,16 +614,18 @@ extern "C" int32_t ffsrl_move_tool_envs(float* laparoscope_base, float* laparosc
 
 extern "C" int32_t ffsrl_reset_envs(float* vertex, float* velocity, float* active_drag, const float* initial_vertex,
                                     float* laparoscope_base, float* laparoscope_tip, const float* initial_base,
-                                    const float* initial_tip, int32_t* in_collision, const int32_t* env_vertex_start,
+                                    const float* initial_tip, int32_t* in_collision, float* xform,
+                                    const float* initial_xform, const int32_t* env_vertex_start,
                                     const int32_t* env_ids, int32_t n, int32_t num_envs, void* stream) {
     if (n < 0 || num_envs < 0 ||
         (n > 0 && (!vertex || !velocity || !active_drag || !initial_vertex || !laparoscope_base || !laparoscope_tip ||
-                   !initial_base || !initial_tip || !in_collision || !env_vertex_start || !env_ids)))
+                   !initial_base || !initial_tip || !in_collision || !env_vertex_start || !env_ids ||
+                   (xform && !initial_xform))))
         return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_reset_envs");
     if (n == 0) return FFSRL_OK;
     k_reset_envs<<<n, 256, 0, (cudaStream_t)stream>>>(vertex, velocity, active_drag, initial_vertex, laparoscope_base,
-                                                       laparoscope_tip, initial_base, initial_tip, in_collision,
-                                                       env_vertex_start, env_ids, num_envs);
+                                                       laparoscope_tip, initial_base, initial_tip, in_collision, xform,
+                                                       initial_xform, env_vertex_start, env_ids, num_envs);
     FFSRL_LAUNCH_CHECK("ffsrl_reset_envs");
     return FFSRL_OK;
 }

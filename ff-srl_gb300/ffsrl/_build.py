@@ -29,6 +29,7 @@ UNITS = {
     "plain.cu": ["-fmad=false"],
     "batched.cu": ["-prec-div=false", "-prec-sqrt=false"],
     "render.cu": ["-fmad=false"],
+    "instrument.cu": ["-fmad=false"],
     "bvh_build.cpp": [],
 }
 

@@ -127,7 +127,12 @@ def lib() -> C.CDLL:
         "ffsrl_grasp_nearest": ([P, P, P, P, P, F32, P, I32, P], I32),
         "ffsrl_move_tool": ([P, P, P, I32, P], I32),
         "ffsrl_move_tool_envs": ([P, P, P, P, I32, I32, P], I32),
-        "ffsrl_reset_envs": ([P, P, P, P, P, P, P, P, P, P, P, I32, I32, P], I32),
+        "ffsrl_reset_envs": ([P, P, P, P, P, P, P, P, P, P, P, P, P, I32, I32, P], I32),
+        "ffsrl_instrument_update": ([P, P, P, P, I32, P], I32),
+        "ffsrl_instrument_apply_actions": ([P, P, P, P, P, P, P, I32, P], I32),
+        "ffsrl_instrument_cartesian": ([P, P, P, P, P, P, P, I32, P], I32),
+        "ffsrl_instrument_cartesian_envs": ([P, P, P, P, P, P, P, P, I32, I32, P], I32),
+        "ffsrl_instrument_set_rotation_center": ([P, P, P, P, P, P, I32, P], I32),
         "ffsrl_grasp_nearest_envs": ([P, P, P, P, P, F32, P, P, I32, I32, P], I32),
         "ffsrl_bvh_refit_fused_envs": ([pb, P, P, P, I32, P], I32),
         "ffsrl_render_fused_envs": ([pr, pb, P, I32, P], I32),

@@ -13,6 +13,8 @@ list of ``numEnvs`` mesh dicts for environments with different meshes.
 
 from __future__ import annotations
 
+import contextlib
+
 import numpy as np
 import torch
 
@@ -233,6 +235,13 @@ class SimModelDO:
         self.laparoscopeInCollision = torch.zeros(self.numEnvs, **i32)
         self.laparoscopeDragCutHeat = torch.zeros(3 * self.numEnvs, **i32)
         self.laparoscopeDragCutHeatUpdate = torch.zeros(3 * self.numEnvs, **i32)
+        # instrument kinematics (setInstrument): 7 transforms per env in the reference's
+        # storage (row-major transposes), capsule heights, workspace violation flags
+        self.laparoscopeXForm = torch.zeros(112 * self.numEnvs, **f32)
+        self.laparoscopeInitialXForm = torch.zeros(112 * self.numEnvs, **f32)
+        self.laparoscopeHeight = torch.zeros(4 * self.numEnvs, **f32)
+        self.laparoscopeWorkspaceViolation = torch.zeros(self.numEnvs, **i32)
+        self.hasInstrumentKinematics = False
         self.envStatus = torch.zeros(self.numEnvs, **i32)
         self.envVertexStartT = T(self.envVertexStart, **i32)
         self.envTetStartT = T(self.envTetStart, **i32)
@@ -381,11 +390,96 @@ class SimModelDO:
                                         self.numEnvs, _lib.stream_handle(stream)))
 
     def moveTool(self, disp, stream=None):
-        """Translate every env's instrument by ``disp`` [N, 3] (device tensor)."""
+        """Translate every env's instrument by ``disp`` [N, 3] (device tensor): the capsule
+        ends, and the kinematic transforms when the model has them."""
         self.require_cuda()
         disp = disp.contiguous()
         check(lib().ffsrl_move_tool(ptr(self.laparoscopeBase), ptr(self.laparoscopeTip), ptr(disp), self.numEnvs,
                                     _lib.stream_handle(stream)))
+        if self.hasInstrumentKinematics:
+            with torch.cuda.stream(stream) if stream is not None else contextlib.nullcontext():
+                # the translation of a stored transpose is its bottom row
+                self.laparoscopeXForm.view(self.numEnvs, 7, 16)[:, :, 12:15] += disp.view(self.numEnvs, 1, 3)
+
+    # ------------------------------------------------- instrument kinematics
+    def setInstrument(self, xform, heights):
+        """Kinematic instrument (laparoscope.py:370-383): 7 transforms per env, [N, 112] in
+        the reference's storage (row-major transposes of column-vector transforms; slots 0
+        rod capsule, 1/2 clamps, 3 rotation centre, 4/5 clamp pivots, 6 rod), and capsule
+        heights [N, 4].  The capsule ends stay as set by ``setTool`` until an action
+        recomputes them from the transforms."""
+        self.laparoscopeXForm.copy_(torch.as_tensor(np.asarray(xform, dtype=np.float32).reshape(-1)))
+        self.laparoscopeInitialXForm.copy_(self.laparoscopeXForm)
+        self.laparoscopeHeight.copy_(torch.as_tensor(np.asarray(heights, dtype=np.float32).reshape(-1)))
+        self.hasInstrumentKinematics = True
+
+    def _require_kinematics(self):
+        self.require_cuda()
+        if not self.hasInstrumentKinematics:
+            raise _lib.FFSRLError(_lib.ERR_INVALID_ARGUMENT, "the model has no instrument transforms (setInstrument)")
+
+    def _flat(self, a, n):
+        a = torch.as_tensor(a, dtype=torch.float32, device=self.device).reshape(-1).contiguous()
+        if a.numel() != n:
+            raise ValueError(f"expected {n} values, got {a.numel()}")
+        return a
+
+    def applyActions(self, actions, stream=None):
+        """applyActions (modelDO.py:1331-1362): per env, rod forward, rod roll, rotation-
+        centre x and y rotation, clamp opening ([N, 5]); then the clamps' grasp update
+        (updateClampsDragKernel) and the visual points."""
+        self._require_kinematics()
+        a = self._flat(actions, 5 * self.numEnvs)
+        check(lib().ffsrl_instrument_apply_actions(ptr(self.laparoscopeXForm), ptr(a), ptr(self.laparoscopeDragCutHeat),
+                                                   ptr(self.laparoscopeDragCutHeatUpdate), ptr(self.laparoscopeBase),
+                                                   ptr(self.laparoscopeTip), ptr(self.laparoscopeHeight), self.numEnvs,
+                                                   _lib.stream_handle(stream)))
+        self.updateClampsDrag(self.laparoscopeDragCutHeat, self.laparoscopeDragCutHeatUpdate)
+        self.transformSimMeshData(stream)
+
+    def applyCartesianActions(self, cartesianActions, stream=None):
+        """applyCartesianActions (modelDO.py:1364-1383): move each effector by [N, 3]."""
+        self._require_kinematics()
+        a = self._flat(cartesianActions, 3 * self.numEnvs)
+        check(lib().ffsrl_instrument_cartesian(ptr(self.laparoscopeXForm), ptr(a), None, None,
+                                               ptr(self.laparoscopeBase), ptr(self.laparoscopeTip),
+                                               ptr(self.laparoscopeHeight), self.numEnvs, _lib.stream_handle(stream)))
+        self.transformSimMeshData(stream)
+
+    def applyCartesianActionsInWorkspace(self, cartesianActions, stream=None):
+        """applyCartesianActionsInWorkspace (modelDO.py:1385-1404): components that would take
+        the effector out of [workspaceLow, workspaceHigh] are dropped;
+        ``laparoscopeWorkspaceViolation`` flags those envs."""
+        self._require_kinematics()
+        a = self._flat(cartesianActions, 3 * self.numEnvs)
+        ws = np.asarray(list(self.workspaceLow) + list(self.workspaceHigh), dtype=np.float32)
+        check(lib().ffsrl_instrument_cartesian(ptr(self.laparoscopeXForm), ptr(a), ws.ctypes.data,
+                                               ptr(self.laparoscopeWorkspaceViolation), ptr(self.laparoscopeBase),
+                                               ptr(self.laparoscopeTip), ptr(self.laparoscopeHeight), self.numEnvs,
+                                               _lib.stream_handle(stream)))
+
+    def setRotationCenter(self, translation, rotation, stream=None):
+        """setRotationCenter (modelDO.py:1570-1587): the rotation centre of env e takes the
+        pose T(translation[e]) Rx Ry Rz(rotation[e]) and carries the instrument with it."""
+        self._require_kinematics()
+        t = self._flat(translation, 3 * self.numEnvs)
+        r = self._flat(rotation, 3 * self.numEnvs)
+        check(lib().ffsrl_instrument_set_rotation_center(ptr(self.laparoscopeXForm), ptr(t), ptr(r),
+                                                         ptr(self.laparoscopeBase), ptr(self.laparoscopeTip),
+                                                         ptr(self.laparoscopeHeight), self.numEnvs,
+                                                         _lib.stream_handle(stream)))
+
+    def forceLaparoscopeClamp(self, envs):
+        """forceLaparoscopeClamp (modelDO.py:1524-1531): a closing clamp action (-1 rad) for
+        the envs where ``envs`` is nonzero."""
+        e = torch.clamp(torch.as_tensor(envs, dtype=torch.float32, device=self.device), 0.0, 1.0)
+        actions = torch.zeros((self.numEnvs, 5), dtype=torch.float32, device=self.device)
+        actions[:, 4] = -e
+        self.applyActions(actions)
+
+    def getLaparoscopePositionsTensor(self):
+        """Each env's effector (drag point) [N, 3], a view of the capsule-end array."""
+        return self.laparoscopeTip.view(self.numEnvs, 4, 3)[:, 3]
 
     def setTool(self, base, tip, radius=None):
         """Set the instrument's capsule ends [4N, 3] (and radii [4N])."""
@@ -397,6 +491,7 @@ class SimModelDO:
     def setEffectorInitialPosition(self):
         self.laparoscopeInitialBase.copy_(self.laparoscopeBase)
         self.laparoscopeInitialTip.copy_(self.laparoscopeTip)
+        self.laparoscopeInitialXForm.copy_(self.laparoscopeXForm)
 
     def resetFixedModel(self, envNums):
         """Restore the listed envs' vertices and instrument, zero their velocity,
@@ -414,6 +509,7 @@ class SimModelDO:
             self.activeDragConstraint.zero_()
             self.laparoscopeBase.copy_(self.laparoscopeInitialBase)
             self.laparoscopeTip.copy_(self.laparoscopeInitialTip)
+            self.laparoscopeXForm.copy_(self.laparoscopeInitialXForm)
             self.laparoscopeDragCutHeat.zero_()
             self.laparoscopeDragCutHeatUpdate.zero_()
         else:
@@ -422,7 +518,8 @@ class SimModelDO:
             check(lib().ffsrl_reset_envs(ptr(self.vertex), ptr(self.velocity), ptr(self.activeDragConstraint),
                                          ptr(self.initialVertex), ptr(self.laparoscopeBase), ptr(self.laparoscopeTip),
                                          ptr(self.laparoscopeInitialBase), ptr(self.laparoscopeInitialTip),
-                                         ptr(self.laparoscopeInCollision), ptr(self.envVertexStartT), ptr(idt),
+                                         ptr(self.laparoscopeInCollision), ptr(self.laparoscopeXForm),
+                                         ptr(self.laparoscopeInitialXForm), ptr(self.envVertexStartT), ptr(idt),
                                          len(ids), self.numEnvs, _lib.stream_handle(None)))
             sel = torch.zeros(self.numEnvs, dtype=torch.bool, device=self.device)
             sel[idt.long()] = True
@@ -437,6 +534,7 @@ class SimModelDO:
         self.vertex.copy_(self.initialVertex)
         self.laparoscopeBase.copy_(self.laparoscopeInitialBase)
         self.laparoscopeTip.copy_(self.laparoscopeInitialTip)
+        self.laparoscopeXForm.copy_(self.laparoscopeInitialXForm)
         self.laparoscopeDragCutHeat.zero_()
         self.laparoscopeDragCutHeatUpdate.zero_()
         self.transformSimMeshData()

@@ -278,7 +278,8 @@ class EnvServer:
                 check(lib().ffsrl_reset_envs(ptr(m.vertex), ptr(m.velocity), ptr(m.activeDragConstraint),
                                              ptr(m.initialVertex), ptr(m.laparoscopeBase), ptr(m.laparoscopeTip),
                                              ptr(m.laparoscopeInitialBase), ptr(m.laparoscopeInitialTip),
-                                             ptr(m.laparoscopeInCollision), ptr(m.envVertexStartT), ptr(ln.rst_d), nr,
+                                             ptr(m.laparoscopeInCollision), ptr(m.laparoscopeXForm),
+                                             ptr(m.laparoscopeInitialXForm), ptr(m.envVertexStartT), ptr(ln.rst_d), nr,
                                              m.numEnvs, s))
             disp = ln.act_d[:n, :3].contiguous()
             check(lib().ffsrl_move_tool_envs(ptr(m.laparoscopeBase), ptr(m.laparoscopeTip), ptr(disp),

@@ -233,12 +233,45 @@ int32_t ffsrl_move_tool_envs(float* laparoscope_base, float* laparoscope_tip, co
 /* Return the listed envs to their rest state (resetFixedModel, modelDO.py:1589-1622, for
    an env list): vertex = initial_vertex and velocity = 0 over each env's vertex range
    [env_vertex_start[e], env_vertex_start[e+1]), grasp flags 0, instrument base/tip =
-   their initial values, contact count 0.  Device arrays; ids outside [0, num_envs) are
-   skipped.  One launch for any number of envs. */
+   their initial values, contact count 0, and -- when xform is not NULL -- the 7 instrument
+   transforms (112 floats per env) their initial values.  Device arrays; ids outside
+   [0, num_envs) are skipped.  One launch for any number of envs. */
 int32_t ffsrl_reset_envs(float* vertex, float* velocity, float* active_drag, const float* initial_vertex,
                          float* laparoscope_base, float* laparoscope_tip, const float* initial_base,
-                         const float* initial_tip, int32_t* in_collision, const int32_t* env_vertex_start,
-                         const int32_t* env_ids, int32_t n, int32_t num_envs, void* stream);
+                         const float* initial_tip, int32_t* in_collision, float* xform, const float* initial_xform,
+                         const int32_t* env_vertex_start, const int32_t* env_ids, int32_t n, int32_t num_envs,
+                         void* stream);
+/* ---- instrument kinematics (modelDO.py:26-416, 1331-1419, 1552-1587) -------------
+   xform: 7 transforms per env, [112 * num_envs] floats, each a row-major 4x4 holding the
+   transpose of the column-vector transform, as the reference stores them (slots: 0 rod
+   capsule, 1 left clamp, 2 right clamp, 3 rotation centre, 4 and 5 clamp pivots, 6 rod).
+   height: [4 * num_envs] capsule heights (rod, left clamp, right clamp, unused).  Every
+   call ends by writing the 4 capsule ends per env into base/tip [4 * num_envs * 3]
+   (updateLaparoscopeKernel, modelDO.py:222-245); entry 3's tip is the drag point.
+   All arrays are device arrays unless stated. */
+int32_t ffsrl_instrument_update(float* xform, float* base, float* tip, const float* height, int32_t num_envs,
+                                void* stream);
+/* applyActions (modelDO.py:1331-1362, applyActionsKernel :161-190): actions [5 * num_envs]
+   = rod forward, rod roll, rotation-centre x, rotation-centre y, clamp opening (rad);
+   drag_cut_heat / drag_cut_heat_update [3 * num_envs] carry the clamp's grasp state. */
+int32_t ffsrl_instrument_apply_actions(float* xform, const float* actions, int32_t* drag_cut_heat,
+                                       int32_t* drag_cut_heat_update, float* base, float* tip, const float* height,
+                                       int32_t num_envs, void* stream);
+/* applyCartesianActions[InWorkspace] (modelDO.py:1364-1404): actions [3 * num_envs] move
+   each effector; workspace = HOST array {low x, y, z, high x, y, z} or NULL for none;
+   violation [num_envs] (may be NULL) flags envs whose action was clipped. */
+int32_t ffsrl_instrument_cartesian(float* xform, const float* actions, const float* workspace, int32_t* violation,
+                                   float* base, float* tip, const float* height, int32_t num_envs, void* stream);
+/* ffsrl_instrument_cartesian for the listed envs: actions[3i..3i+2] move env env_ids[i];
+   ids outside [0, num_envs) are skipped. */
+int32_t ffsrl_instrument_cartesian_envs(float* xform, const float* actions, const float* workspace, int32_t* violation,
+                                        float* base, float* tip, const float* height, const int32_t* env_ids,
+                                        int32_t n, int32_t num_envs, void* stream);
+/* setRotationCenter (modelDO.py:1570-1587): the rotation centre takes the pose
+   T(translation) Rx Ry Rz(rotation), [3 * num_envs] each, carrying the instrument. */
+int32_t ffsrl_instrument_set_rotation_center(float* xform, const float* translation, const float* rotation,
+                                             float* base, float* tip, const float* height, int32_t num_envs,
+                                             void* stream);
 /* Rigidly translate each env's instrument (4 bases + 4 tips) by disp[3e..3e+2]. */
 int32_t ffsrl_move_tool(float* laparoscope_base, float* laparoscope_tip, const float* disp, int32_t num_envs,
                         void* stream);
