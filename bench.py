@@ -2,7 +2,8 @@
 
 Workload (one "step"): every environment of a 4096-env batch drawn from a pool of
 mixed-size ellipsoids (tet counts log-uniform in [500, 20000]) takes one RL step --
-instrument displacement (0.5 mm random walk), 8 substeps x 10 Jacobi iterations of
+an effector displacement through the instrument's kinematic chain (0.5 mm random walk,
+applyCartesianActionsInWorkspace), 8 substeps x 10 Jacobi iterations of
 Neo-Hookean + volume + distance constraints with grasp and instrument contact, BVH refit,
 and a 128x128 (2x2 supersampled) depth + colour ray-cast per environment.
 
@@ -37,6 +38,7 @@ METRIC = "env-steps/s at 4096 envs"
 NUM_ENVS = 4096
 RES = 128
 POOL = 64
+GRASP_RADIUS = 0.5  # cm: grasp the nearest surface vertex within this distance of the drag point
 EPISODE = 16  # RL episode length: every env returns to its rest state after this many steps
 
 
@@ -144,7 +146,7 @@ def build_workload(device, envs, seed):
                               horizontalAperture=ap, lightPos=(0.3, 1.0, 0.5), lightIntensity=0.8)
     pos, rot = sc.env_cameras(meshes, seed=seed + 1)
     r.setCameras(pos, rot)
-    m.graspNearest(torch.ones(envs, dtype=torch.int32, device=device), radius=0.3)
+    m.graspNearest(torch.ones(envs, dtype=torch.int32, device=device), radius=GRASP_RADIUS)
     return m, meshes, bvh, r
 
 
@@ -227,18 +229,18 @@ def main():
         # restart from the rest state (reset + grasp), inside the timed region
         if episode["steps"] and episode["steps"] % EPISODE == 0:
             m.resetFixedModel(all_envs)
-            m.graspNearest(grasp_all, radius=0.3)
+            m.graspNearest(grasp_all, radius=GRASP_RADIUS)
             episode["resets"] += 1
         episode["steps"] += 1
 
     def new_episode():
         m.resetFixedModel(all_envs)
-        m.graspNearest(grasp_all, radius=0.3)
+        m.graspNearest(grasp_all, radius=GRASP_RADIUS)
         episode["steps"] = 1
 
     def step(k):
         episode_tick()
-        m.moveTool(walk[k])
+        m.applyCartesianActionsInWorkspace(walk[k])
         integ.stepModel(m, 1)
         bvh.refitBVH()
         r.renderNew(bvh, m)
@@ -304,7 +306,7 @@ def main():
         act_h[:, :3] = walk_h[k % len(walk_h)]
         act_h[:, 3] = 1.0
         act_d.copy_(act_h, non_blocking=True)
-        m.moveTool(act_d[:, :3].contiguous())
+        m.applyCartesianActionsInWorkspace(act_d[:, :3].contiguous())
         integ.stepModel(m, 1)
         bvh.refitBVH()
         r.renderNew(bvh, m)
@@ -333,7 +335,7 @@ def main():
         pk = 2
         pe[0].record(stream)
         for k in range(pk):
-            m.moveTool(walk[k])
+            m.applyCartesianActionsInWorkspace(walk[k])
             pint.stepModel(m, 1)
             bvh.refitBVH(fused=False)
             r.fused = False
@@ -355,7 +357,7 @@ def main():
         srv = EnvServer(pool_s, [ids[id(mm)] for mm in meshes_s], device, hbm_budget_bytes=60e9, resolution=RES,
                         autotune=True)
         serving = srv.run_closed_loop(args.serve_seconds, think_hz=60.0, seed=rank, warmup_s=1.0)
-        serving["what"] = ("closed-loop actors, Poisson think time at 60 Hz, each request = tool move + 8x10 step "
+        serving["what"] = ("closed-loop actors, Poisson think time at 60 Hz, each request = effector move + 8x10 step "
                            "+ refit + 128x128 ray-cast of its env; latency from arrival to result on the host")
         del srv
     if rank == 0:
@@ -366,7 +368,7 @@ def main():
             cpu = {"value": v, "unit": "env-steps/s", "cores": threads, "kind": "port",
                    "sample": f"32 envs of the same pool, 1 full env-step (8x10 solve, refit, {RES}x{RES} ray-cast), "
                              "oracle restatement, OpenMP over envs"}
-        # per step: move_tool, one launch per size class, remap, fused refit, normal gather, rays;
+        # per step: instrument kinematics, one launch per size class, remap, fused refit, normal gather, rays;
         # per episode reset: remap and grasp
         launches = K * (n_cls + 5) + 2 * resets_timed
         line = {"metric": METRIC, "value": value, "unit": "env-steps/s", "n_gpus": world, "steps": K,

@@ -28,7 +28,7 @@ from . import scenarios as sc
 def step_mixed(envs: int = 512, device: str = "cuda:0") -> None:
     meshes, _ = sc.mixed_meshes(envs, pool_size=64, seed=0)
     m, _ = sc.liver_model(device, envs, meshes=meshes)
-    m.graspNearest(torch.ones(envs, dtype=torch.int32, device=device), radius=0.3)
+    m.graspNearest(torch.ones(envs, dtype=torch.int32, device=device), radius=0.5)
     integ = SimIntegratorDO(device, autotune=True)
     p = integ.plan(m)
     print(p.info(), integ.tuning)
@@ -39,7 +39,7 @@ def step_mixed(envs: int = 512, device: str = "cuda:0") -> None:
 def step_big(device: str = "cuda:0") -> None:
     meshes, _ = sc.mixed_meshes(304, pool_size=8, seed=3, t_lo=12000, t_hi=20000)
     m, _ = sc.liver_model(device, 304, meshes=meshes)
-    m.graspNearest(torch.ones(304, dtype=torch.int32, device=device), radius=0.3)
+    m.graspNearest(torch.ones(304, dtype=torch.int32, device=device), radius=0.5)
     p = SimIntegratorDO(device).plan(m)
     print(p.info())
     p.step(1)

@@ -50,6 +50,70 @@ def instrument_arrays(points, up=(0.0, 1.0, 0.0), radii=(0.3, 0.1, 0.1), rod=12.
     return base.reshape(-1, 3).astype(np.float32), tip.reshape(-1, 3).astype(np.float32), rad.astype(np.float32)
 
 
+def _frame(z) -> np.ndarray:
+    """Rotation whose third column is the unit vector z."""
+    z = np.asarray(z, dtype=np.float64)
+    z = z / np.linalg.norm(z)
+    ref = np.array([1.0, 0.0, 0.0]) if abs(z[0]) < 0.9 else np.array([0.0, 1.0, 0.0])
+    x = np.cross(ref, z)
+    x /= np.linalg.norm(x)
+    return np.stack([x, np.cross(z, x), z], axis=1)
+
+
+def _rt(R, t) -> np.ndarray:
+    M = np.eye(4)
+    M[:3, :3], M[:3, 3] = R, t
+    return M
+
+
+def _rx(a) -> np.ndarray:
+    c, s = np.cos(a), np.sin(a)
+    return np.array([[1.0, 0.0, 0.0], [0.0, c, -s], [0.0, s, c]])
+
+
+def instrument_xforms(points, down=(0.0, -1.0, 0.0), radii=(0.3, 0.1, 0.1), rod=12.0, clamp=1.2,
+                      clamp_angle=40.0, pivot_depth=None):
+    """Kinematic laparoscopes whose drag point (effector) sits at ``points``.
+
+    The instrument's local z runs along ``down`` toward the tissue.  Returns, per env, the
+    7 transforms in the library's layout ([N, 112], row-major transposes of column-vector
+    transforms; slots 0 rod capsule, 1/2 left/right clamp, 3 rotation centre, 4/5 clamp
+    pivots, 6 rod), capsule heights [N, 4] (rod, clamp, clamp, 0), and the initial capsule
+    ends base/tip [4N, 3] with radii [4N], computed on the host in float64 as the update
+    kernel computes them from the transforms.  The rotation centre (the trocar) sits
+    ``pivot_depth`` (default: the rod height) up the axis from the effector; the clamps
+    stand at ``clamp_angle`` degrees about their pivots' x axes (40 = closed).
+    """
+    p = np.asarray(points, dtype=np.float64).reshape(-1, 3)
+    N = len(p)
+    R = _frame(down)
+    z = R[:, 2]
+    depth = rod if pivot_depth is None else float(pivot_depth)
+    th = np.radians(clamp_angle)
+    xf = np.zeros((N, 7, 4, 4))
+    ends_b = np.zeros((N, 4, 3))
+    ends_t = np.zeros((N, 4, 3))
+    for e in range(N):
+        c0 = p[e] - z * (0.5 * rod + clamp)         # rod capsule centre
+        X0 = _rt(R, c0)
+        X3 = _rt(R, p[e] - z * depth)                 # rotation centre
+        X4 = _rt(R @ _rx(-th), c0 + z * (0.5 * rod))  # clamp pivots at the rod's end
+        X5 = _rt(R @ _rx(th), c0 + z * (0.5 * rod))
+        X1 = X4 @ _rt(np.eye(3), np.array([0.0, 0.0, 0.5 * clamp]))
+        X2 = X5 @ _rt(np.eye(3), np.array([0.0, 0.0, 0.5 * clamp]))
+        for k, M in enumerate((X0, X1, X2, X3, X4, X5, X0)):
+            xf[e, k] = M.T  # stored as the transpose, as the reference stores them
+        for k, (M, h) in enumerate(((X0, rod), (X1, clamp), (X2, clamp))):
+            ends_b[e, k] = (M @ np.array([0.0, 0.0, -h / 1.85, 1.0]))[:3]
+            ends_t[e, k] = (M @ np.array([0.0, 0.0, h / 1.85, 1.0]))[:3]
+        ends_b[e, 3] = (X0 @ np.array([0.0, 0.0, -0.5 * rod - clamp, 1.0]))[:3]
+        ends_t[e, 3] = (X0 @ np.array([0.0, 0.0, 0.5 * rod + clamp, 1.0]))[:3]
+    heights = np.tile(np.array([rod, clamp, clamp, 0.0], dtype=np.float32), (N, 1))
+    rad = np.tile(np.array([radii[0], radii[1], radii[2], 0.0]), N).astype(np.float32)
+    return (xf.reshape(N, 112).astype(np.float32), heights, ends_b.reshape(-1, 3).astype(np.float32),
+            ends_t.reshape(-1, 3).astype(np.float32), rad)
+
+
 def top_surface_point(mesh) -> np.ndarray:
     """The highest surface vertex of a mesh (the default grasp site)."""
     surf = mesh["point_to_vertex"][:, 1]
@@ -57,12 +121,15 @@ def top_surface_point(mesh) -> np.ndarray:
     return v[np.argmax(v[:, 1])].astype(np.float64)
 
 
-def place_instruments(model: SimModelDO, meshes: list, dip: float = 0.1) -> np.ndarray:
-    """Effector of env e just below mesh e's highest surface point; returns the points."""
+def place_instruments(model: SimModelDO, meshes: list, dip: float = 0.35) -> np.ndarray:
+    """Kinematic instrument of env e with its effector ``dip`` cm below mesh e's highest
+    surface point, pointing down, clamps closed (their tips then touch the surface);
+    returns the effector points."""
     pts = np.stack([top_surface_point(m) - np.array([0.0, dip, 0.0]) for m in meshes])
-    b, t, r = instrument_arrays(pts)
+    xf, heights, b, t, r = instrument_xforms(pts)
     model.setTool(b, t, r)
-    model.toolHost = {"base": b, "tip": t, "radius": r}
+    model.setInstrument(xf, heights)
+    model.toolHost = {"base": b, "tip": t, "radius": r, "xform": xf, "height": heights}
     model.setEffectorInitialPosition()
     return pts
 
@@ -94,7 +161,7 @@ def liver_model(device, num_envs, meshes=None, E=NH_E, nu=NH_NU, substeps=8, ite
     kw.setdefault("environmentGravity", mg.gravity_force(meshes[0]))
     m = SimModelDO(meshes, num_envs, device, simSubsteps=substeps, simFrameRate=60, simConstraintsSteps=iterations,
                    environmentGroundLevel=-100.0, constraints=flags, globalVolumeCompliance=1.0 / lam,
-                   globalDeviatoricCompliance=1.0 / mu, globalLaparoscopeDragLookupRadius=0.3, **kw)
+                   globalDeviatoricCompliance=1.0 / mu, globalLaparoscopeDragLookupRadius=0.5, **kw)
     place_instruments(m, meshes)
     return m, meshes
 

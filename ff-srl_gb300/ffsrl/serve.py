@@ -282,8 +282,13 @@ class EnvServer:
                                              ptr(m.laparoscopeInitialXForm), ptr(m.envVertexStartT), ptr(ln.rst_d), nr,
                                              m.numEnvs, s))
             disp = ln.act_d[:n, :3].contiguous()
-            check(lib().ffsrl_move_tool_envs(ptr(m.laparoscopeBase), ptr(m.laparoscopeTip), ptr(disp),
-                                             ptr(ln.ids_d), n, m.numEnvs, s))
+            if m.hasInstrumentKinematics:  # the effector moves through the instrument's kinematic chain
+                check(lib().ffsrl_instrument_cartesian_envs(ptr(m.laparoscopeXForm), ptr(disp), None, None,
+                                                            ptr(m.laparoscopeBase), ptr(m.laparoscopeTip),
+                                                            ptr(m.laparoscopeHeight), ptr(ln.ids_d), n, m.numEnvs, s))
+            else:
+                check(lib().ffsrl_move_tool_envs(ptr(m.laparoscopeBase), ptr(m.laparoscopeTip), ptr(disp),
+                                                 ptr(ln.ids_d), n, m.numEnvs, s))
             if trans:
                 # pinned staging: a copy from pageable memory would wait for the stream
                 nt = len(trans)

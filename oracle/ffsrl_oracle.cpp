@@ -750,6 +750,170 @@ int render_env(const ffsrl_render* r, const ffsrl_bvh* b, int stack_cap, int e, 
     return 0;
 }
 
+// ---------------------------------------------------------------------------------
+// Instrument kinematics (modelDO.py:26-416): 7 transforms per env stored as the
+// reference stores them (row-major transpose of the column-vector transform); children
+// follow their parent: 0 -> 1 2 4 5 6, 3 -> 0 1 2 4 5 6, 4 -> 1, 5 -> 2.  Per env the rod,
+// rotation-centre and clamp actions apply in that order.  Warp's mat44(pos, quat, scale),
+// inverse and quat_from_axis_angle are restated from their mathematics.
+struct Mat4 { float m[4][4]; };
+struct P3 { float x, y, z; };
+inline P3 p3(float x, float y, float z) { return P3{x, y, z}; }
+inline float pdot(P3 a, P3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline float plen(P3 a) { return std::sqrt(pdot(a, a)); }
+
+Mat4 kload(const float* X, int s) {
+    Mat4 c;
+    for (int r = 0; r < 4; ++r)
+        for (int k = 0; k < 4; ++k) c.m[r][k] = X[16 * s + 4 * k + r];
+    return c;
+}
+void kstore(float* X, int s, const Mat4& c) {
+    for (int r = 0; r < 4; ++r)
+        for (int k = 0; k < 4; ++k) X[16 * s + 4 * k + r] = c.m[r][k];
+}
+Mat4 kmul(const Mat4& a, const Mat4& b) {
+    Mat4 c;
+    for (int r = 0; r < 4; ++r)
+        for (int k = 0; k < 4; ++k)
+            c.m[r][k] = ((a.m[r][0] * b.m[0][k] + a.m[r][1] * b.m[1][k]) + a.m[r][2] * b.m[2][k]) + a.m[r][3] * b.m[3][k];
+    return c;
+}
+// adjugate / determinant with the 2x2 minors of the row pairs (0,1) and (2,3)
+Mat4 kinv(const Mat4& a) {
+    const float(*m)[4] = a.m;
+    float s0 = m[0][0] * m[1][1] - m[1][0] * m[0][1], s1 = m[0][0] * m[1][2] - m[1][0] * m[0][2];
+    float s2 = m[0][0] * m[1][3] - m[1][0] * m[0][3], s3 = m[0][1] * m[1][2] - m[1][1] * m[0][2];
+    float s4 = m[0][1] * m[1][3] - m[1][1] * m[0][3], s5 = m[0][2] * m[1][3] - m[1][2] * m[0][3];
+    float c5 = m[2][2] * m[3][3] - m[3][2] * m[2][3], c4 = m[2][1] * m[3][3] - m[3][1] * m[2][3];
+    float c3 = m[2][1] * m[3][2] - m[3][1] * m[2][2], c2 = m[2][0] * m[3][3] - m[3][0] * m[2][3];
+    float c1 = m[2][0] * m[3][2] - m[3][0] * m[2][2], c0 = m[2][0] * m[3][1] - m[3][0] * m[2][1];
+    float det = s0 * c5 - s1 * c4 + s2 * c3 + s3 * c2 - s4 * c1 + s5 * c0;
+    float inv = 1.0f / det;
+    Mat4 b;
+    b.m[0][0] = (m[1][1] * c5 - m[1][2] * c4 + m[1][3] * c3) * inv;
+    b.m[0][1] = (-m[0][1] * c5 + m[0][2] * c4 - m[0][3] * c3) * inv;
+    b.m[0][2] = (m[3][1] * s5 - m[3][2] * s4 + m[3][3] * s3) * inv;
+    b.m[0][3] = (-m[2][1] * s5 + m[2][2] * s4 - m[2][3] * s3) * inv;
+    b.m[1][0] = (-m[1][0] * c5 + m[1][2] * c2 - m[1][3] * c1) * inv;
+    b.m[1][1] = (m[0][0] * c5 - m[0][2] * c2 + m[0][3] * c1) * inv;
+    b.m[1][2] = (-m[3][0] * s5 + m[3][2] * s2 - m[3][3] * s1) * inv;
+    b.m[1][3] = (m[2][0] * s5 - m[2][2] * s2 + m[2][3] * s1) * inv;
+    b.m[2][0] = (m[1][0] * c4 - m[1][1] * c2 + m[1][3] * c0) * inv;
+    b.m[2][1] = (-m[0][0] * c4 + m[0][1] * c2 - m[0][3] * c0) * inv;
+    b.m[2][2] = (m[3][0] * s4 - m[3][1] * s2 + m[3][3] * s0) * inv;
+    b.m[2][3] = (-m[2][0] * s4 + m[2][1] * s2 - m[2][3] * s0) * inv;
+    b.m[3][0] = (-m[1][0] * c3 + m[1][1] * c1 - m[1][2] * c0) * inv;
+    b.m[3][1] = (m[0][0] * c3 - m[0][1] * c1 + m[0][2] * c0) * inv;
+    b.m[3][2] = (-m[3][0] * s3 + m[3][1] * s1 - m[3][2] * s0) * inv;
+    b.m[3][3] = (m[2][0] * s3 - m[2][1] * s1 + m[2][2] * s0) * inv;
+    return b;
+}
+P3 kpoint(const Mat4& c, P3 p) {
+    return p3(((c.m[0][0] * p.x + c.m[0][1] * p.y) + c.m[0][2] * p.z) + c.m[0][3],
+              ((c.m[1][0] * p.x + c.m[1][1] * p.y) + c.m[1][2] * p.z) + c.m[1][3],
+              ((c.m[2][0] * p.x + c.m[2][1] * p.y) + c.m[2][2] * p.z) + c.m[2][3]);
+}
+// wp.mat44(t, quat_from_axis_angle(axis, angle), 1)
+Mat4 krigid(P3 t, P3 axis, float angle) {
+    float h = 0.5f * angle;
+    float s = std::sin(h), w = std::cos(h);
+    float x = axis.x * s, y = axis.y * s, z = axis.z * s;
+    Mat4 c;
+    c.m[0][0] = 1.0f - 2.0f * (y * y + z * z); c.m[0][1] = 2.0f * (x * y - z * w); c.m[0][2] = 2.0f * (x * z + y * w);
+    c.m[1][0] = 2.0f * (x * y + z * w); c.m[1][1] = 1.0f - 2.0f * (x * x + z * z); c.m[1][2] = 2.0f * (y * z - x * w);
+    c.m[2][0] = 2.0f * (x * z - y * w); c.m[2][1] = 2.0f * (y * z + x * w); c.m[2][2] = 1.0f - 2.0f * (x * x + y * y);
+    c.m[0][3] = t.x; c.m[1][3] = t.y; c.m[2][3] = t.z;
+    c.m[3][0] = 0.0f; c.m[3][1] = 0.0f; c.m[3][2] = 0.0f; c.m[3][3] = 1.0f;
+    return c;
+}
+// getTransformationMatrix (modelDO.py:396-414)
+Mat4 kshift_rotate(float sx, float sy, float sz, float ax, float ay, float az) {
+    const P3 zero = p3(0.0f, 0.0f, 0.0f);
+    Mat4 T = krigid(p3(sx, sy, sz), zero, 0.0f);
+    Mat4 X = krigid(zero, p3(1.0f, 0.0f, 0.0f), ax);
+    Mat4 Y = krigid(zero, p3(0.0f, 1.0f, 0.0f), ay);
+    Mat4 Z = krigid(zero, p3(0.0f, 0.0f, 1.0f), az);
+    return kmul(T, kmul(X, kmul(Y, Z)));
+}
+// applyTransformationToChild (modelDO.py:386-394)
+void kchild(float* X, const Mat4& M, int parent, int child) {
+    Mat4 P = kload(X, parent);
+    Mat4 C = kload(X, child);
+    kstore(X, child, kmul(P, kmul(M, kmul(kinv(P), C))));
+}
+// applyTransformationToChildren (modelDO.py:366-384)
+void kchildren(float* X, const Mat4& M, int parent) {
+    if (parent == 4) kchild(X, M, 4, 1);
+    if (parent == 5) kchild(X, M, 5, 2);
+    if (parent == 3)
+        for (int i = 0; i < 7; ++i)
+            if (i != 3) kchild(X, M, 3, i);
+    if (parent == 0)
+        for (int i = 1; i < 7; ++i)
+            if (i != 3) kchild(X, M, 0, i);
+}
+// transformFunc (modelDO.py:291-298)
+void kslot(float* X, int slot, const Mat4& cur, const Mat4& M) {
+    kchildren(X, M, slot);
+    kstore(X, slot, kmul(cur, M));
+}
+// rotateClampsFunc (modelDO.py:300-364), angles in degrees
+void kclamps(float* X, int* dch, int* dchu, float action) {
+    const float pi = 3.14159265358979323846f;
+    float diff = action * 180.0f / pi;
+    if (diff == 0.0f) return;
+    Mat4 rod = kload(X, 0), left = kload(X, 4), right = kload(X, 5);
+    Mat4 local = kmul(kinv(rod), right);
+    float cur = std::asin(local.m[2][1]) * 180.0f / pi;
+    bool apply = false;
+    if (dch[0] == 1 && dchu[0] == 1) dchu[0] = 0;
+    if (action > 0.0f) {
+        if (cur < 85.0f) {
+            if (cur + diff > 85.0f) diff = 85.0f - cur;
+            apply = true;
+        }
+        if (cur > 3.0f + 40.0f && dch[0] == 1) { dch[0] = 0; dchu[0] = 1; }
+    } else {
+        if (cur > 40.0f) {
+            if (cur + diff < 40.0f) diff = 40.0f - cur;
+            apply = true;
+        }
+        if (cur < 3.0f + 40.0f && dch[0] == 0) { dch[0] = 1; dchu[0] = 1; }
+    }
+    if (apply) {
+        float rad = diff * pi / 180.0f;
+        Mat4 R = kshift_rotate(0.0f, 0.0f, 0.0f, rad, 0.0f, 0.0f);
+        Mat4 Ri = kshift_rotate(0.0f, 0.0f, 0.0f, -rad, 0.0f, 0.0f);
+        kstore(X, 4, kmul(left, Ri));
+        kchildren(X, Ri, 4);
+        kstore(X, 5, kmul(right, R));
+        kchildren(X, R, 5);
+    }
+}
+// updateLaparoscopeKernel (modelDO.py:222-245)
+void kends(const float* X, const float* height, float* base, float* tip, int e) {
+    for (int k = 0; k < 4; ++k) {
+        Mat4 c;
+        P3 bl, tl;
+        if (k < 3) {
+            c = kload(X, k);
+            float h = height[4 * e + k];
+            bl = p3(0.0f, 0.0f, 0.0f - h / 1.85f);
+            tl = p3(0.0f, 0.0f, 0.0f + h / 1.85f);
+        } else {
+            c = kload(X, 0);
+            float rh = height[4 * e], ch = height[4 * e + 2];
+            bl = p3(0.0f, 0.0f, 0.0f - rh * 0.5f - ch * 1.0f);
+            tl = p3(0.0f, 0.0f, 0.0f + rh * 0.5f + ch * 1.0f);
+        }
+        P3 b = kpoint(c, bl), t = kpoint(c, tl);
+        int64_t o = 3ll * (4 * e + k);
+        base[o] = b.x; base[o + 1] = b.y; base[o + 2] = b.z;
+        tip[o] = t.x; tip[o + 1] = t.y; tip[o + 2] = t.z;
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -786,6 +950,71 @@ int oracle_render_mt(const ffsrl_render* r, const ffsrl_bvh* b, int stack_cap, i
 void oracle_refit_mt(const ffsrl_bvh* b, const float* pts, const int32_t* faces, int threads) {
 #pragma omp parallel for schedule(dynamic, 4) num_threads(threads)
     for (int e = 0; e < b->num_envs; ++e) refit_env(b, pts, faces, e);
+}
+
+
+// Instrument kinematics entry points (host arrays; same layouts as the library's)
+void oracle_instrument_update(const float* xform, float* base, float* tip, const float* height, int num_envs) {
+    for (int e = 0; e < num_envs; ++e) kends(xform + 112ll * e, height, base, tip, e);
+}
+
+void oracle_instrument_apply_actions(float* xform, const float* actions, int* dch, int* dchu, float* base, float* tip,
+                                     const float* height, int num_envs) {
+    for (int e = 0; e < num_envs; ++e) {  // applyActionsKernel (modelDO.py:161-190)
+        float* X = xform + 112ll * e;
+        const float* a = actions + 5ll * e;
+        Mat4 rod0 = kload(X, 0), rc0 = kload(X, 3);
+        kslot(X, 0, rod0, kshift_rotate(0.0f, 0.0f, a[0], 0.0f, 0.0f, a[1]));
+        kslot(X, 3, rc0, kshift_rotate(0.0f, 0.0f, 0.0f, a[2], a[3], 0.0f));
+        kclamps(X, dch + 3ll * e, dchu + 3ll * e, a[4]);
+        kends(X, height, base, tip, e);
+    }
+}
+
+void oracle_instrument_cartesian(float* xform, const float* actions, const float* ws, int* violation, float* base,
+                                 float* tip, const float* height, int num_envs) {
+    for (int e = 0; e < num_envs; ++e) {  // transfromCartesianActionsKernel[InWorkspace] (modelDO.py:56-153)
+        const float* a = actions + 3ll * e;
+        if (a[0] == 0.0f && a[1] == 0.0f && a[2] == 0.0f) continue;
+        float* X = xform + 112ll * e;
+        int64_t d = 3ll * (4 * e + 3);
+        P3 cur = p3(tip[d], tip[d + 1], tip[d + 2]);
+        P3 act = p3(a[0], a[1], a[2]);
+        if (ws) {
+            if (violation) violation[e] = 0;
+            P3 nw = p3(cur.x + act.x, cur.y + act.y, cur.z + act.z);
+            if (nw.x < ws[0] || nw.x > ws[3]) { act.x = 0.0f; if (violation) violation[e] = 1; }
+            if (nw.y < ws[1] || nw.y > ws[4]) { act.y = 0.0f; if (violation) violation[e] = 1; }
+            if (nw.z < ws[2] || nw.z > ws[5]) { act.z = 0.0f; if (violation) violation[e] = 1; }
+        }
+        Mat4 rod = kload(X, 0), rc = kload(X, 3);
+        P3 rel = kpoint(kinv(rc), cur);
+        P3 delta = p3(((rc.m[0][0] * act.x + rc.m[1][0] * act.y) + rc.m[2][0] * act.z) + rc.m[3][0],
+                      ((rc.m[0][1] * act.x + rc.m[1][1] * act.y) + rc.m[2][1] * act.z) + rc.m[3][1],
+                      ((rc.m[0][2] * act.x + rc.m[1][2] * act.y) + rc.m[2][2] * act.z) + rc.m[3][2]);
+        P3 nrel = p3(rel.x + delta.x, rel.y + delta.y, rel.z + delta.z);
+        float rcur = plen(rel), rnew = plen(nrel);
+        P3 cr = p3(rel.y * nrel.z - rel.z * nrel.y, rel.z * nrel.x - rel.x * nrel.z, rel.x * nrel.y - rel.y * nrel.x);
+        float sin_t = plen(cr) / (plen(rel) * plen(nrel));
+        float lc = plen(cr);
+        P3 axis = lc > 0.0f ? p3(cr.x / lc, cr.y / lc, cr.z / lc) : p3(0.0f, 0.0f, 0.0f);
+        float angle = std::asin(sin_t);
+        kslot(X, 0, rod, kshift_rotate(0.0f, 0.0f, rnew - rcur, 0.0f, 0.0f, 0.0f));
+        kslot(X, 3, rc, krigid(p3(0.0f, 0.0f, 0.0f), axis, angle));
+        kends(X, height, base, tip, e);
+    }
+}
+
+void oracle_instrument_set_rotation_center(float* xform, const float* t, const float* r, float* base, float* tip,
+                                           const float* height, int num_envs) {
+    for (int e = 0; e < num_envs; ++e) {  // setRotationCenterTransformKernel (modelDO.py:155-171)
+        float* X = xform + 112ll * e;
+        Mat4 rc = kload(X, 3);
+        int64_t o = 3ll * e;
+        Mat4 G = kshift_rotate(t[o], t[o + 1], t[o + 2], r[o], r[o + 1], r[o + 2]);
+        kslot(X, 3, rc, kmul(kinv(rc), G));
+        kends(X, height, base, tip, e);
+    }
 }
 
 }  // extern "C"

@@ -218,3 +218,50 @@ class OracleScene:
         rc = lib_.oracle_render_mt(C.byref(self.r), C.byref(self.bvh), int(self.stack_cap), int(threads))
         if rc:
             raise RuntimeError(f"oracle render failed: {rc}")
+
+
+# ---------------------------------------------------------------- instrument kinematics
+def _kin_lib():
+    lb = lib()
+    if not getattr(lb, "_kin_ready", False):
+        P = C.c_void_p
+        lb.oracle_instrument_update.argtypes = [P, P, P, P, C.c_int]
+        lb.oracle_instrument_apply_actions.argtypes = [P, P, P, P, P, P, P, C.c_int]
+        lb.oracle_instrument_cartesian.argtypes = [P, P, P, P, P, P, P, C.c_int]
+        lb.oracle_instrument_set_rotation_center.argtypes = [P, P, P, P, P, P, C.c_int]
+        lb._kin_ready = True
+    return lb
+
+
+class OracleInstrument:
+    """Host copy of a model's kinematic instrument (transforms, heights, capsule ends,
+    clamp state) advanced by the C++ restatement."""
+
+    def __init__(self, xform, height, base, tip, dch=None, dchu=None):
+        f = lambda a: np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(-1)).copy()
+        self.xform, self.height, self.base, self.tip = f(xform), f(height), f(base), f(tip)
+        self.n = len(self.height) // 4
+        i = lambda a: np.ascontiguousarray(np.zeros(3 * self.n, np.int32) if a is None else
+                                           np.asarray(a, dtype=np.int32).reshape(-1)).copy()
+        self.dch, self.dchu = i(dch), i(dchu)
+        self.violation = np.zeros(self.n, dtype=np.int32)
+
+    def update(self):
+        _kin_lib().oracle_instrument_update(_p(self.xform), _p(self.base), _p(self.tip), _p(self.height), self.n)
+
+    def apply_actions(self, actions):
+        a = np.ascontiguousarray(np.asarray(actions, dtype=np.float32).reshape(-1))
+        _kin_lib().oracle_instrument_apply_actions(_p(self.xform), _p(a), _p(self.dch), _p(self.dchu), _p(self.base),
+                                                   _p(self.tip), _p(self.height), self.n)
+
+    def cartesian(self, actions, workspace=None):
+        a = np.ascontiguousarray(np.asarray(actions, dtype=np.float32).reshape(-1))
+        ws = None if workspace is None else np.ascontiguousarray(np.asarray(workspace, dtype=np.float32).reshape(6))
+        _kin_lib().oracle_instrument_cartesian(_p(self.xform), _p(a), None if ws is None else _p(ws),
+                                               _p(self.violation), _p(self.base), _p(self.tip), _p(self.height), self.n)
+
+    def set_rotation_center(self, translation, rotation):
+        t = np.ascontiguousarray(np.asarray(translation, dtype=np.float32).reshape(-1))
+        r = np.ascontiguousarray(np.asarray(rotation, dtype=np.float32).reshape(-1))
+        _kin_lib().oracle_instrument_set_rotation_center(_p(self.xform), _p(t), _p(r), _p(self.base), _p(self.tip),
+                                                         _p(self.height), self.n)

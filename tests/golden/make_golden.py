@@ -39,7 +39,7 @@ MESH_KEYS = ("vertex", "rest_vertex", "inverse_mass", "tetrahedron", "tetrahedro
 BEAM_STEPS = 25
 LIVER_STEPS = 5
 RES = 16
-GRASP_RADIUS = 0.3
+GRASP_RADIUS = 0.5
 
 
 def pack_meshes(meshes) -> dict:

@@ -62,7 +62,7 @@ def test_beam_xpbd_variant(gpu, oracle_lib, batched):
 def test_neohookean_grasp_contact(gpu, oracle_lib, batched):
     mesh = mg.ellipsoid_for_tets(1500, seed=2)
     m, meshes = sc.liver_model("cuda:0", 2, meshes=[mesh, mesh])
-    m.graspNearest(torch.ones(2, dtype=torch.int32, device="cuda:0"), radius=0.3)
+    m.graspNearest(torch.ones(2, dtype=torch.int32, device="cuda:0"), radius=0.5)
     torch.cuda.synchronize()
     assert int((m.activeDragConstraint != 0).sum()) == 2
     disp = torch.tensor([[0.05, 0.05, 0.0], [-0.05, 0.05, 0.0]], device="cuda:0")
@@ -173,7 +173,7 @@ def test_grasp_nearest_matches_numpy(gpu):
     t = m.laparoscopeTip.cpu().numpy()
     t[4 * 3 + 3] = tip[3]
     m.laparoscopeTip.copy_(torch.as_tensor(t))
-    m.graspNearest(clamp, radius=0.3)
+    m.graspNearest(clamp, radius=0.5)
     got = m.activeDragConstraint.cpu().numpy()
     x = m.vertex.cpu().numpy()
     for e in range(4):
@@ -208,7 +208,7 @@ def test_liver_config1_mesh_global_accumulators(gpu, oracle_lib):
     # whole: positions stay in shared memory, sums go to global scratch (mode 1)
     m, meshes = sc.liver_model("cuda:0", 2)
     assert m.numVertices == 2 * 11102
-    m.graspNearest(torch.ones(2, dtype=torch.int32, device="cuda:0"), radius=0.3)
+    m.graspNearest(torch.ones(2, dtype=torch.int32, device="cuda:0"), radius=0.5)
     integ = SimIntegratorDO("cuda:0")
     info = integ.plan(m).info()
     o = oracle_for(m)
