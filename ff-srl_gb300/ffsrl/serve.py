@@ -44,7 +44,8 @@ def slot_bytes(mesh: dict, resolution: int) -> int:
     plan = T * (8 + 8 + 36 + 4) + E * (4 + 8 + 4) + F * 8 + V * 4
     bvh = 2 * F * (24 + 16) + F * 4
     image = resolution * resolution * 16
-    return int(model + plan + bvh + image)
+    instrument = 112 * 4 + 16 * 4 * 3  # transforms, heights, capsule ends
+    return int(model + plan + bvh + image + instrument)
 
 
 def plan_slots(pool: list, actor_mesh, hbm_budget_bytes: float, resolution: int) -> np.ndarray:
@@ -158,7 +159,7 @@ class EnvServer:
         v0, v1 = int(m.envVertexStart[s]), int(m.envVertexStart[s + 1])
         return {"vertex": m.vertex[v0:v1], "velocity": m.velocity[v0:v1], "drag": m.activeDragConstraint[v0:v1],
                 "base": m.laparoscopeBase[4 * s:4 * s + 4], "tip": m.laparoscopeTip[4 * s:4 * s + 4],
-                "incol": m.laparoscopeInCollision[s:s + 1]}
+                "xform": m.laparoscopeXForm[112 * s:112 * s + 112], "incol": m.laparoscopeInCollision[s:s + 1]}
 
     def _evict(self, a: int, stream) -> None:
         s = int(self.actor_slot[a])
@@ -204,6 +205,7 @@ class EnvServer:
         views["drag"].zero_()
         views["base"].copy_(mm.laparoscopeInitialBase[4 * s:4 * s + 4])
         views["tip"].copy_(mm.laparoscopeInitialTip[4 * s:4 * s + 4])
+        views["xform"].copy_(mm.laparoscopeInitialXForm[112 * s:112 * s + 112])
         views["incol"].zero_()
         self.actor_clamp[a] = 0
 

@@ -82,9 +82,13 @@ def test_neohookean_grasp_contact(gpu, oracle_lib, batched):
 
 
 def test_mixed_pool_batched(gpu, oracle_lib):
+    # mixed sizes in one batch; contact is off here: with the closed clamps pressed into
+    # these meshes a contact decision sits on its threshold within a few steps, and the
+    # reference-shaped path (float atomics) flips it from run to run as well, so contact
+    # parity is checked in the Neo-Hookean + grasp + contact and golden tests instead
     pool = [mg.ellipsoid_for_tets(t, seed=i) for i, t in enumerate([300, 1200, 4000])]
     meshes = [pool[i % 3] for i in range(7)]
-    m, _ = sc.liver_model("cuda:0", 7, meshes=meshes)
+    m, _ = sc.liver_model("cuda:0", 7, meshes=meshes, collide=False)
     x, o = run_pair(m, 5, batched=True)
     assert rel_err(x, o.a["vertex"], "mixed pool") < POS_TOL
 
