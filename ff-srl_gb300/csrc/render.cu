@@ -347,9 +347,35 @@ __device__ int query(const EnvView& ev, const float* __restrict__ pts, const int
 
 struct Shade { v3 color; float depth; };
 
-// shading of drawSimBVHKernelManyEnvs (render.py:334-409), modes 3 (vertex colour) and 4 (depth)
-__device__ __forceinline__ Shade trace(const ffsrl_render& r, const EnvView& ev, v3 ro, float4 q, int x, int y, int W,
-                                       int H) {
+// shading of drawSimBVHKernelManyEnvs (render.py:334-409): modes 0 grayscale, 1 texture,
+// 2 normal map, 3 vertex colour, 4 depth map into `color`; `depth` gets t/50 in every mode
+// texture_interpolation (render.py:123-148): bilinear texel of the interpolated tex
+// coordinate; texel (x, y) of a texture at first + y + x*S.  Indices are clamped into the
+// texture (the reference reads one texel past the edge at coordinate 1, weighted 0).
+__device__ __forceinline__ v3 texel(const ffsrl_render& r, int e, int local_face, float u, float v, float w) {
+    const int* et = r.env_texture + 4ll * e;
+    const int first = et[0], S = et[1], c0 = et[2];
+    const int* ti = r.tex_indices + et[3] + 3ll * local_face;
+    const float* ta = r.tex_coords + 2ll * (c0 + ti[0]);
+    const float* tb = r.tex_coords + 2ll * (c0 + ti[1]);
+    const float* tc = r.tex_coords + 2ll * (c0 + ti[2]);
+    float tx = (u * ta[0] + v * tb[0]) + w * tc[0];
+    float ty = (u * ta[1] + v * tb[1]) + w * tc[1];
+    float fx = tx * float(S - 1), fy = (1.0f - ty) * float(S - 1);
+    int x0 = (int)fx, y0 = (int)fy;
+    float ax = fx - float(x0), ay = fy - float(y0);
+    int x1 = x0 + 1, y1 = y0 + 1;
+    x0 = min(max(x0, 0), S - 1); x1 = min(max(x1, 0), S - 1);
+    y0 = min(max(y0, 0), S - 1); y1 = min(max(y1, 0), S - 1);
+    v3 c00 = ld3(r.texture, (long long)first + y0 + x0 * S), c10 = ld3(r.texture, (long long)first + y0 + x1 * S);
+    v3 c01 = ld3(r.texture, (long long)first + y1 + x0 * S), c11 = ld3(r.texture, (long long)first + y1 + x1 * S);
+    v3 lower = (1.0f - ax) * c00 + ax * c10;
+    v3 upper = (1.0f - ax) * c01 + ax * c11;
+    return (1.0f - ay) * lower + ay * upper;
+}
+
+__device__ __forceinline__ Shade trace(const ffsrl_render& r, const EnvView& ev, int e, v3 ro, float4 q, int x, int y,
+                                       int W, int H) {
     float sx = 2.0f * float(x) / float(W) - 1.0f;
     float sy = 2.0f * float(y) / float(H) - 1.0f;
     v3 rd = normalize(quat_rotate(q, mk(sx * r.camera_tan * r.camera_aspect, sy * r.camera_tan, -1.0f)));
@@ -367,14 +393,28 @@ __device__ __forceinline__ Shade trace(const ffsrl_render& r, const EnvView& ev,
         float v = length(cross(p - a, c - a)) / area;
         float u = 1.0f - w - v;
         v3 n = u * ld3(r.vertex_normal, i) + v * ld3(r.vertex_normal, j) + w * ld3(r.vertex_normal, k);
-        v3 vc = (ld3(r.vis_point_color, i) + ld3(r.vis_point_color, j) + ld3(r.vis_point_color, k)) / 3.0f;
-        float lam = 0.0f;
-        for (int l = 0; l < r.num_lights; ++l) {
-            float val = r.light_intensity[l] * dot(n, ld3(r.light_dir, l));
-            if (val < 0.0f) val = 0.0f;
-            lam = lam + val;
+        v3 col;
+        if (r.render_mode == 2) {  // normal map
+            col = n * 0.5f + mk(0.5f, 0.5f, 0.5f);
+        } else if (r.render_mode == 4) {  // depth map
+            float g = t / 50.0f;
+            col = mk(g, g, g);
+        } else {
+            v3 base;
+            if (r.render_mode == 0)
+                base = mk(1.0f, 1.0f, 1.0f);
+            else if (r.render_mode == 1 && r.env_texture && r.env_texture[4ll * e + 1] > 0)
+                base = texel(r, e, (int)(tri - ev.fofs), u, v, w);
+            else
+                base = (ld3(r.vis_point_color, i) + ld3(r.vis_point_color, j) + ld3(r.vis_point_color, k)) / 3.0f;
+            float lam = 0.0f;
+            for (int l = 0; l < r.num_lights; ++l) {
+                float val = r.light_intensity[l] * dot(n, ld3(r.light_dir, l));
+                if (val < 0.0f) val = 0.0f;
+                lam = lam + val;
+            }
+            col = lam * base;
         }
-        v3 col = lam * vc;
         if (col.x > 1.0f) col.x = 1.0f;
         if (col.y > 1.0f) col.y = 1.0f;
         if (col.z > 1.0f) col.z = 1.0f;
@@ -399,7 +439,7 @@ __global__ void k_draw(ffsrl_render r, ffsrl_bvh b) {
     v3 ro = ld3(r.camera_pos, cam);
     float4 q = reinterpret_cast<const float4*>(r.camera_rot)[cam];
     EnvView ev = env_view(b, e);
-    Shade s = trace(r, ev, ro, q, x, y, W, H);
+    Shade s = trace(r, ev, e, ro, q, x, y, W, H);
     st3(r.rays, tid, s.color);
     r.ray_depth[tid] = s.depth;
 }
@@ -447,7 +487,7 @@ __global__ void __launch_bounds__(256) k_rays(ffsrl_render r, ffsrl_bvh b, const
         const float4 qr = reinterpret_cast<const float4*>(r.camera_rot)[cam];
         const EnvView ev = env_view(b, e);
         const int et = (2 * py + (q >> 1)) * W + 2 * px + (q & 1);  // ray index as in downsample_kernel
-        s = trace(r, ev, ro, qr, et % W, H - et / W, W, H);
+        s = trace(r, ev, e, ro, qr, et % W, H - et / W, W, H);
     }
     float cx = s.color.x, cy = s.color.y, cz = s.color.z, d = s.depth;
     float ax[3], ay[3], az[3], ad[3];
@@ -486,6 +526,10 @@ int32_t check_render(const ffsrl_render* r) {
         !r->vertex_normal || !r->camera_pos || !r->camera_rot || r->num_cameras <= 0 ||
         (r->num_lights > 0 && (!r->light_dir || !r->light_intensity)) || !r->error_flag)
         return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_render: missing arrays");
+    if (r->render_mode < 0 || r->render_mode > 4)
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_render: render_mode must be 0..4");
+    if (r->render_mode == 1 && r->env_texture && (!r->texture || !r->tex_coords || !r->tex_indices))
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_render: texture mode needs texture, tex_coords, tex_indices");
     if (r->num_cameras != 1 && r->num_cameras != r->num_envs)
         return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_render: num_cameras must be 1 or num_envs");
     if (((uintptr_t)r->camera_rot) & 15)

@@ -9,7 +9,7 @@ from ._lib import FFSRLError
 from .model import SimModelDO
 from .integrator import SimIntegratorDO, BatchPlan
 from .bvh import SimBVH
-from .render import WarpRaycastRendererDO, quat_rpy, look_at_rotation
+from .render import RenderMode, WarpRaycastRendererDO, quat_rpy, look_at_rotation
 
-__all__ = ["SimModelDO", "SimIntegratorDO", "BatchPlan", "SimBVH", "WarpRaycastRendererDO", "meshgen",
+__all__ = ["SimModelDO", "SimIntegratorDO", "BatchPlan", "SimBVH", "WarpRaycastRendererDO", "RenderMode", "meshgen",
            "FFSRLError", "quat_rpy", "look_at_rotation"]

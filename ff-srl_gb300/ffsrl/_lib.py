@@ -94,6 +94,7 @@ class Render(C.Structure):
         ("num_cameras", I32), ("camera_pos", P), ("camera_rot", P), ("camera_tan", F32), ("camera_aspect", F32),
         ("num_lights", I32), ("light_dir", P), ("light_intensity", P),
         ("color", P), ("depth", P), ("rays", P), ("ray_depth", P), ("error_flag", P), ("env_point_start", P),
+        ("render_mode", I32), ("texture", P), ("env_texture", P), ("tex_coords", P), ("tex_indices", P),
     ]
 
 

@@ -273,3 +273,38 @@ def tiny_mesh(vertex, tetrahedron=(), edge=(), triangle=(), inverse_mass=None) -
         "vis_point_color": np.full((len(surf), 3), 0.5, dtype=np.float32),
         "fixed": inv == 0,
     }
+
+
+def add_texture(mesh: dict, size: int = 64, seed: int = 0, per_corner: bool = False) -> dict:
+    """A copy of ``mesh`` with a texture, standing in for a USD material's diffuse texture
+    (``FF_SRL/FF_SRL/modelDO.py:628-640``).
+
+    ``texture`` [size, size, 3] in [0, 1] is a seeded smooth tissue-like pattern (stripes
+    plus blotches).  ``tex_coords`` are a planar projection of the rest shape onto its x/z
+    extent, one per visual point, and ``tex_indices`` is ``vis_face`` (the reference's
+    default when the mesh carries no ``primvars:st:indices``).  With ``per_corner`` the
+    coordinates are one per face corner instead, with their own ``tex_indices`` (the
+    indexed-primvar form)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    g = np.linspace(0.0, 1.0, size)
+    X, Y = np.meshgrid(g, g, indexing="ij")
+    field = 0.5 + 0.25 * np.sin(2 * np.pi * (3 * X + rng.uniform())) * np.cos(2 * np.pi * (2 * Y + rng.uniform()))
+    for _ in range(6):
+        cx, cy, r = rng.uniform(0, 1), rng.uniform(0, 1), rng.uniform(0.05, 0.2)
+        field += 0.2 * np.exp(-((X - cx) ** 2 + (Y - cy) ** 2) / (2 * r * r))
+    tint = np.array([0.75, 0.28, 0.25]) + rng.uniform(-0.05, 0.05, size=3)
+    tex = np.clip(field[..., None] * tint[None, None, :] * 1.3, 0.0, 1.0).astype(np.float32)
+    rest = mesh["rest_vertex"] if "rest_vertex" in mesh else mesh["vertex"]
+    p = np.asarray(rest, dtype=np.float64)[np.asarray(mesh["point_to_vertex"])[:, 1]]
+    lo, hi = p.min(axis=0), p.max(axis=0)
+    span = np.where(hi - lo > 0, hi - lo, 1.0)
+    uv = np.stack([(p[:, 0] - lo[0]) / span[0], (p[:, 2] - lo[2]) / span[2]], axis=1)
+    out = dict(mesh)
+    out["texture"] = tex
+    if per_corner:
+        out["tex_coords"] = uv[np.asarray(mesh["vis_face"]).reshape(-1)].astype(np.float32)
+        out["tex_indices"] = np.arange(out["tex_coords"].shape[0], dtype=np.int32)
+    else:
+        out["tex_coords"] = uv.astype(np.float32)
+        out["tex_indices"] = np.asarray(mesh["vis_face"], dtype=np.int32).reshape(-1)
+    return out

@@ -155,6 +155,7 @@ class SimModelDO:
         # grasp candidates: the surface (visual) vertices of each env
         self.graspCandStart = self.envVisPointStart.copy()
         h["graspCand"] = h["pointToVertex"][1::2].copy()
+        self._concatenate_textures(h)
         self.host = h
 
         self.numVertices = int(self.envVertexStart[-1])
@@ -182,6 +183,38 @@ class SimModelDO:
         base[:, 1] = 10.1
         rad = np.tile(np.array([r[0], r[1], r[2], 0.0], dtype=np.float32), N)
         self.toolHost = {"base": base, "tip": tip, "radius": rad}
+
+    def _concatenate_textures(self, h):
+        """Texture tables of the renderer's texture mode (modelDO.py:1056-1125): each distinct
+        mesh's ``texture`` [S, S, 3] in [0, 1], ``tex_coords`` [T, 2] and ``tex_indices`` (3 per
+        visual face, default ``vis_face``, as modelDO.py:636-640) appended once; per env
+        ``envTexture`` = (first texel, S, first tex coord, first tex index), S = 0 for none."""
+        tex, coords, idx, slot = [], [], [], []
+        nt = nc = ni = 0
+        for m in self.meshes:
+            if m.get("texture") is None:
+                slot.append((0, 0, 0, 0))
+                continue
+            t = np.asarray(m["texture"], dtype=np.float32)
+            if t.ndim != 3 or t.shape[0] != t.shape[1] or t.shape[2] != 3 or t.shape[0] < 1:
+                raise ValueError("texture must be a square [S, S, 3] array")
+            c = np.asarray(m["tex_coords"], dtype=np.float32).reshape(-1, 2)
+            i = np.asarray(m.get("tex_indices", m["vis_face"]), dtype=np.int64).reshape(-1)
+            if len(i) != 3 * len(m["vis_face"]) or (len(i) and (i.min() < 0 or i.max() >= len(c))):
+                raise ValueError("tex_indices must hold 3 tex-coord ids per visual face")
+            S = t.shape[0]
+            slot.append((nt, S, nc, ni))
+            tex.append(t.reshape(-1))
+            coords.append(c.reshape(-1))
+            idx.append(i)
+            nt, nc, ni = nt + S * S, nc + len(c), ni + len(i)
+        self.hasTextures = bool(tex)
+        if nt >= 2**31 or ni >= 2**31:
+            raise ValueError("textures exceed int32 indexing")
+        h["texture"] = _cat(tex, np.float32)
+        h["texCoords"] = _cat(coords, np.float32)
+        h["texIndices"] = _cat(idx, np.int32)
+        h["envTexture"] = np.asarray([slot[k] for k in self.envMesh], dtype=np.int32).reshape(-1)
 
     def _upload(self):
         d = self.device
@@ -224,6 +257,10 @@ class SimModelDO:
         self.allVisFace = T(h["allVisFace"], **i32)
         self.visFace = self.allVisFace
         self.allVisPointColor = T(h["allVisPointColor"], **f32)
+        self.textureT = T(h["texture"], **f32)
+        self.texCoordsT = T(h["texCoords"], **f32)
+        self.texIndicesT = T(h["texIndices"], **i32)
+        self.envTextureT = T(h["envTexture"], **i32)
         self.pointToVertex = T(h["pointToVertex"], **i32)
         self.graspCand = T(h["graspCand"], **i32)
         self.graspCandStartT = T(self.graspCandStart, **i32)

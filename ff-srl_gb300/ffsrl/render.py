@@ -4,8 +4,9 @@
 ``renderNew(simBVH, simModel)`` returns the per-env images ``[N, R, R, 3]`` as a device
 tensor (the reference's ``wp.to_torch(pixels).view(N, R, R, 3)``, ``render.py:1113``).
 Each pixel averages 2x2 rays (``num_samples = 1`` -> rays of ``2R x 2R``).  One pass
-writes both reference shading modes: vertex-colour Lambert (mode 3) into ``pixels`` and
-depth ``t/50`` (mode 4, one channel) into ``depth``.
+writes the colour image in ``render_mode`` (``RenderMode``: grayscale, texture, normal
+map, vertex colour or depth map) into ``pixels`` and depth ``t/50`` (one channel) into
+``depth``.
 
 Display back-ends of the reference (matplotlib, terminal, OpenGL window) are not
 available; every ``mode`` renders headless and returns the tensor.
@@ -49,10 +50,23 @@ def look_at_rotation(pos, at) -> np.ndarray:
     return quat_rpy(pitch, yaw, 0.0)
 
 
+class RenderMode:
+    """Shading of the colour image (render.py:17-25, drawSimBVHKernelManyEnvs render.py:350-409).
+
+    grayscale, texture and vertex_color are Lambert-lit; texture falls back to the vertex
+    colour for an env whose mesh has no texture; depth_map writes t/50 to all channels."""
+    grayscale = 0
+    texture = 1
+    normal_map = 2
+    vertex_color = 3
+    depth_map = 4
+
+
 class WarpRaycastRendererDO:
     def __init__(self, device, simModel, cameraPos=(3.0, 3.0, 3.0), cameraRot=(0.0, 0.0, 0.0),
                  lightPos=(3.0, 0.0, 0.0), lightIntensity=0.3, resolution: int = 512, mode: str = "human",
-                 horizontalAperture: float = 19.2, verticalAperture: float = 19.2, fused: bool = True):
+                 horizontalAperture: float = 19.2, verticalAperture: float = 19.2, fused: bool = True,
+                 render_mode: int = RenderMode.texture):
         if mode not in ("headless", "gpuless"):
             warnings.warn(f"render mode {mode!r}: no display back-end here, rendering headless")
         self.device = torch.device(device)
@@ -60,6 +74,9 @@ class WarpRaycastRendererDO:
         self.simModel = simModel
         self.numEnvs = simModel.numEnvs
         self.fused = bool(fused)
+        if int(render_mode) not in range(5):
+            raise ValueError(f"render_mode {render_mode!r}: expected a RenderMode value 0..4")
+        self.render_mode = int(render_mode)  # the reference's default is RenderMode.texture (render.py:852)
         self.height = self.width = int(resolution)
         self.num_pixels = self.width * self.height
         self.num_samples = 1
@@ -129,6 +146,10 @@ class WarpRaycastRendererDO:
             r.rays, r.ray_depth = ptr(self.rays), ptr(self.rayDepth)
         r.error_flag = ptr(self.errorFlag)
         r.env_point_start = ptr(simModel.envVisPointStartT)
+        r.render_mode = int(self.render_mode)
+        if simModel.hasTextures:
+            r.texture, r.env_texture = ptr(simModel.textureT), ptr(simModel.envTextureT)
+            r.tex_coords, r.tex_indices = ptr(simModel.texCoordsT), ptr(simModel.texIndicesT)
         return r
 
     def renderFunctionNew(self, simBVH, stream=None) -> None:

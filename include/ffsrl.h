@@ -174,6 +174,16 @@ typedef struct {
     float* ray_depth;                /* [N*(2R)^2]   per-ray scratch, reference-shaped path only */
     int32_t* error_flag;             /* [1] set to FFSRL_ERR_STACK_OVERFLOW by an overflowing ray */
     const int32_t* env_point_start;  /* [N+1] each env's visual-point range (for the *_envs calls) */
+    /* shading of `color` (drawSimBVHKernelManyEnvs, render.py:350-409): 0 grayscale, 1 texture
+       (vertex colour for envs without one), 2 normal map (no lighting), 3 vertex colour,
+       4 depth map (t/50 in all three channels); 0, 1 and 3 are Lambert-lit.  `depth` is t/50
+       in every mode.  Values outside 0..4 are rejected. */
+    int32_t render_mode;
+    const float* texture;            /* [3 * texels] RGB in [0, 1], every texture one after another */
+    const int32_t* env_texture;      /* [4N] per env: first texel, side S (0 = none), first tex coord,
+                                        first tex index; texel (x, y) of a texture is first + y + x*S */
+    const float* tex_coords;         /* [2T] (u, v) */
+    const int32_t* tex_indices;      /* 3 per env-local visual face: tex coords relative to the env's first */
 } ffsrl_render;
 
 /* ---- library ---------------------------------------------------------------- */

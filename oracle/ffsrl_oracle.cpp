@@ -711,16 +711,52 @@ int render_env(const ffsrl_render* r, const ffsrl_bvh* b, int stack_cap, int e, 
                 float v = length(cross(p - a, c - a)) / area;
                 float u = 1.0f - w - v;
                 V3<float> n = u * ld3<float>(nrmp, i) + v * ld3<float>(nrmp, j) + w * ld3<float>(nrmp, k);
-                V3<float> vc = (ld3<float>(r->vis_point_color, i) + ld3<float>(r->vis_point_color, j) +
+                if (r->render_mode == 2) {  // normal map (render.py:399-401)
+                    col = n * 0.5f + mk<float>(0.5f, 0.5f, 0.5f);
+                } else if (r->render_mode == 4) {  // depth map (render.py:403-405)
+                    float g = h.t / 50.0f;
+                    col = mk<float>(g, g, g);
+                } else {
+                    V3<float> base;
+                    if (r->render_mode == 0) {  // grayscale
+                        base = mk<float>(1.0f, 1.0f, 1.0f);
+                    } else if (r->render_mode == 1 && r->env_texture && r->env_texture[4 * e + 1] > 0) {
+                        // texture_interpolation (render.py:123-148), indices clamped into the texture
+                        const int32_t* et = r->env_texture + 4 * e;
+                        int first = et[0], S = et[1], c0 = et[2];
+                        int lf = (int)(h.tri - b->env_face_offset[e]);
+                        const int32_t* ti = r->tex_indices + et[3] + 3 * lf;
+                        const float* ta = r->tex_coords + 2 * (c0 + ti[0]);
+                        const float* tb = r->tex_coords + 2 * (c0 + ti[1]);
+                        const float* tc = r->tex_coords + 2 * (c0 + ti[2]);
+                        float tx = (u * ta[0] + v * tb[0]) + w * tc[0];
+                        float ty = (u * ta[1] + v * tb[1]) + w * tc[1];
+                        float fx = tx * float(S - 1), fy = (1.0f - ty) * float(S - 1);
+                        int x0 = (int)fx, y0 = (int)fy;
+                        float ax = fx - float(x0), ay = fy - float(y0);
+                        int x1 = x0 + 1, y1 = y0 + 1;
+                        auto cl = [S](int q) { return q < 0 ? 0 : (q > S - 1 ? S - 1 : q); };
+                        x0 = cl(x0); x1 = cl(x1); y0 = cl(y0); y1 = cl(y1);
+                        V3<float> c00 = ld3<float>(r->texture, (int64_t)first + y0 + x0 * S);
+                        V3<float> c10 = ld3<float>(r->texture, (int64_t)first + y0 + x1 * S);
+                        V3<float> c01 = ld3<float>(r->texture, (int64_t)first + y1 + x0 * S);
+                        V3<float> c11 = ld3<float>(r->texture, (int64_t)first + y1 + x1 * S);
+                        V3<float> lower = (1.0f - ax) * c00 + ax * c10;
+                        V3<float> upper = (1.0f - ax) * c01 + ax * c11;
+                        base = (1.0f - ay) * lower + ay * upper;
+                    } else {
+                        base = (ld3<float>(r->vis_point_color, i) + ld3<float>(r->vis_point_color, j) +
                                 ld3<float>(r->vis_point_color, k)) / 3.0f;
-                float lam = 0.0f;
-                for (int l = 0; l < r->num_lights; ++l) {
-                    V3<float> dir = ld3<float>(r->light_dir, l);
-                    float val = r->light_intensity[l] * dot(n, dir);
-                    if (val < 0.0f) val = 0.0f;
-                    lam = lam + val;
+                    }
+                    float lam = 0.0f;
+                    for (int l = 0; l < r->num_lights; ++l) {
+                        V3<float> dir = ld3<float>(r->light_dir, l);
+                        float val = r->light_intensity[l] * dot(n, dir);
+                        if (val < 0.0f) val = 0.0f;
+                        lam = lam + val;
+                    }
+                    col = lam * base;
                 }
-                col = lam * vc;
                 if (col.x > 1.0f) col.x = 1.0f;
                 if (col.y > 1.0f) col.y = 1.0f;
                 if (col.z > 1.0f) col.z = 1.0f;

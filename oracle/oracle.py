@@ -174,6 +174,12 @@ def _render_desc(renderer, vis_points: np.ndarray):
     r.num_cameras = a["camera_pos"].shape[0]
     r.camera_tan, r.camera_aspect = renderer.camera_tan, renderer.camera_aspect
     r.num_lights = a["light_dir"].shape[0]
+    r.render_mode = int(renderer.render_mode)
+    if m.hasTextures:
+        for k, src in (("texture", m.host["texture"]), ("env_texture", m.host["envTexture"]),
+                       ("tex_coords", m.host["texCoords"]), ("tex_indices", m.host["texIndices"])):
+            a[k] = np.ascontiguousarray(src)
+            setattr(r, k, _p(a[k]))
     return r, a
 
 
