@@ -168,8 +168,11 @@ def test_render_modes_gpu_match_oracle(gpu, oracle_lib, fused):
         seen[mode] = g_col
     # the texture changes the textured envs only
     tex_env = m.host["envTexture"].reshape(-1, 4)[:, 1] > 0
-    assert not np.array_equal(seen[1][tex_env], seen[3][tex_env])
-    assert np.array_equal(seen[1][~tex_env], seen[3][~tex_env])
+    assert not np.allclose(seen[1][tex_env], seen[3][tex_env], atol=1e-3)
+    if fused:
+        assert np.array_equal(seen[1][~tex_env], seen[3][~tex_env])
+    else:  # each render sums the normals again with float atomics
+        assert np.abs(seen[1][~tex_env] - seen[3][~tex_env]).max() < 1e-5
     print(f"[render modes] fused={fused}: modes 0-4 match the oracle, textured envs {int(tex_env.sum())}")
 
 
