@@ -287,6 +287,28 @@ __global__ void k_update_ends(Kin k) {
     update_ends(k.xform + 112ll * e, k.height, k.base, k.tip, e);
 }
 
+// updateLaparoscopeMeshKernel (modelDO.py:202-216) as transformSimLaparoscopeMeshData runs
+// it (modelDO.py:1446-1473): one block per env stages the env's 7 transforms in shared
+// memory; each thread carries local points (one instrument shape shared by every env)
+// by the transform of their slot into the env's visual points
+__global__ void k_visual(const float* __restrict__ xform, const float* __restrict__ local,
+                         const int* __restrict__ slot, int num_points, float* __restrict__ vis,
+                         const int* __restrict__ first, const int* __restrict__ ids, int num_envs) {
+    const int e = ids ? ids[blockIdx.x] : blockIdx.x;
+    if (e < 0 || e >= num_envs) return;
+    __shared__ float X[112];
+    for (int k = threadIdx.x; k < 112; k += blockDim.x) X[k] = xform[112ll * e + k];
+    __syncthreads();
+    const long long o = first[e];
+    for (int i = threadIdx.x; i < num_points; i += blockDim.x) {
+        const int s = slot[i];
+        if (s < 0 || s > 6) continue;
+        F3 p = xform_point(load(X, s), f3(local[3 * i], local[3 * i + 1], local[3 * i + 2]));
+        float* q = vis + 3 * (o + i);
+        q[0] = p.x; q[1] = p.y; q[2] = p.z;
+    }
+}
+
 int32_t check_kin(const Kin& k, const char* what) {
     if (k.num_envs < 0 || (k.num_envs > 0 && (!k.xform || !k.base || !k.tip || !k.height)))
         return fail(FFSRL_ERR_INVALID_ARGUMENT, std::string(what) + ": null array or negative env count");
@@ -363,5 +385,20 @@ extern "C" int32_t ffsrl_instrument_set_rotation_center(float* xform, const floa
     if (num_envs == 0) return FFSRL_OK;
     k_set_center<<<grid_for(num_envs, 128), 128, 0, (cudaStream_t)stream>>>(k, translation, rotation);
     FFSRL_LAUNCH_CHECK("ffsrl_instrument_set_rotation_center");
+    return FFSRL_OK;
+}
+
+extern "C" int32_t ffsrl_instrument_visual_update(const float* xform, const float* local_point,
+                                                  const int32_t* point_slot, int32_t num_points, float* vis_point,
+                                                  const int32_t* env_first_point, const int32_t* env_ids, int32_t n,
+                                                  int32_t num_envs, void* stream) {
+    if (n < 0 || num_points < 0 || num_envs < 0 || (!env_ids && n != num_envs))
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_instrument_visual_update: bad counts");
+    if (n == 0 || num_points == 0) return FFSRL_OK;
+    if (!xform || !local_point || !point_slot || !vis_point || !env_first_point)
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_instrument_visual_update: null array");
+    k_visual<<<n, 128, 0, (cudaStream_t)stream>>>(xform, local_point, point_slot, num_points, vis_point,
+                                                  env_first_point, env_ids, num_envs);
+    FFSRL_LAUNCH_CHECK("ffsrl_instrument_visual_update");
     return FFSRL_OK;
 }

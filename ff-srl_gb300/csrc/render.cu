@@ -36,9 +36,13 @@ __device__ __forceinline__ void refit_node(const ffsrl_bvh& b, const float* __re
         long long fofs = b.env_face_offset[e];
         for (int k = 0; k < cnt; ++k) {
             long long f = fofs + b.tri_id[t0 + first + k];
-            v3 pA = ld3(pts, faces[3 * f]), pB = ld3(pts, faces[3 * f + 1]), pC = ld3(pts, faces[3 * f + 2]);
+            // the reference's refit may box another face than the one it traverses
+            // (bvh.py:66-74 against render.py:462-470); refit_source holds that face
+            const long long fb = b.refit_source ? (long long)b.refit_source[f] : f;
+            v3 pA = ld3(pts, faces[3 * fb]), pB = ld3(pts, faces[3 * fb + 1]), pC = ld3(pts, faces[3 * fb + 2]);
             lo = vmin(pA, vmin(pB, vmin(pC, lo)));
             hi = vmax(pA, vmax(pB, vmax(pC, hi)));
+            if (fb != f) pA = ld3(pts, faces[3 * f]), pB = ld3(pts, faces[3 * f + 1]), pC = ld3(pts, faces[3 * f + 2]);
             if (b.tri_pos) {
                 float4* q = reinterpret_cast<float4*>(b.tri_pos) + 3 * (fofs + first + k);
                 q[0] = make_float4(pA.x, pA.y, pA.z, pB.x);
@@ -349,13 +353,24 @@ struct Shade { v3 color; float depth; };
 
 // shading of drawSimBVHKernelManyEnvs (render.py:334-409): modes 0 grayscale, 1 texture,
 // 2 normal map, 3 vertex colour, 4 depth map into `color`; `depth` gets t/50 in every mode
+// The object of env e that holds env-local face lf (render.py:360-366: visFaceToObjectId,
+// objectUsesTexture, objectNumVisFaceCummulative): its 5-int entry in object_texture.
+__device__ __forceinline__ const int* face_object(const ffsrl_render& r, int e, int lf) {
+    const int o0 = r.env_objects[2ll * e], no = r.env_objects[2ll * e + 1];
+    const int* ob = r.object_texture + 5ll * o0;
+    for (int k = 1; k < no; ++k) {
+        if (r.object_texture[5ll * (o0 + k)] > lf) break;
+        ob = r.object_texture + 5ll * (o0 + k);
+    }
+    return ob;
+}
+
 // texture_interpolation (render.py:123-148): bilinear texel of the interpolated tex
 // coordinate; texel (x, y) of a texture at first + y + x*S.  Indices are clamped into the
 // texture (the reference reads one texel past the edge at coordinate 1, weighted 0).
-__device__ __forceinline__ v3 texel(const ffsrl_render& r, int e, int local_face, float u, float v, float w) {
-    const int* et = r.env_texture + 4ll * e;
-    const int first = et[0], S = et[1], c0 = et[2];
-    const int* ti = r.tex_indices + et[3] + 3ll * local_face;
+__device__ __forceinline__ v3 texel(const ffsrl_render& r, const int* ob, int lf, float u, float v, float w) {
+    const int first = ob[1], S = ob[2], c0 = ob[3];
+    const int* ti = r.tex_indices + ob[4] + 3ll * (lf - ob[0]);
     const float* ta = r.tex_coords + 2ll * (c0 + ti[0]);
     const float* tb = r.tex_coords + 2ll * (c0 + ti[1]);
     const float* tc = r.tex_coords + 2ll * (c0 + ti[2]);
@@ -403,10 +418,14 @@ __device__ __forceinline__ Shade trace(const ffsrl_render& r, const EnvView& ev,
             v3 base;
             if (r.render_mode == 0)
                 base = mk(1.0f, 1.0f, 1.0f);
-            else if (r.render_mode == 1 && r.env_texture && r.env_texture[4ll * e + 1] > 0)
-                base = texel(r, e, (int)(tri - ev.fofs), u, v, w);
-            else
-                base = (ld3(r.vis_point_color, i) + ld3(r.vis_point_color, j) + ld3(r.vis_point_color, k)) / 3.0f;
+            else {
+                const int lf = (int)(tri - ev.fofs);
+                const int* ob = (r.render_mode == 1 && r.env_objects) ? face_object(r, e, lf) : nullptr;
+                if (ob && ob[2] > 0)
+                    base = texel(r, ob, lf, u, v, w);
+                else
+                    base = (ld3(r.vis_point_color, i) + ld3(r.vis_point_color, j) + ld3(r.vis_point_color, k)) / 3.0f;
+            }
             float lam = 0.0f;
             for (int l = 0; l < r.num_lights; ++l) {
                 float val = r.light_intensity[l] * dot(n, ld3(r.light_dir, l));
@@ -528,8 +547,9 @@ int32_t check_render(const ffsrl_render* r) {
         return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_render: missing arrays");
     if (r->render_mode < 0 || r->render_mode > 4)
         return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_render: render_mode must be 0..4");
-    if (r->render_mode == 1 && r->env_texture && (!r->texture || !r->tex_coords || !r->tex_indices))
-        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_render: texture mode needs texture, tex_coords, tex_indices");
+    if (r->env_objects && (!r->object_texture || !r->texture || !r->tex_coords || !r->tex_indices))
+        return fail(FFSRL_ERR_INVALID_ARGUMENT,
+                    "ffsrl_render: env_objects needs object_texture, texture, tex_coords and tex_indices");
     if (r->num_cameras != 1 && r->num_cameras != r->num_envs)
         return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_render: num_cameras must be 1 or num_envs");
     if (((uintptr_t)r->camera_rot) & 15)

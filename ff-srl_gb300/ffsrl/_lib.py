@@ -83,6 +83,7 @@ class Bvh(C.Structure):
         ("aabb_min", P), ("aabb_max", P),
         ("total_env_nodes", I32), ("total_topology_nodes", I32), ("max_level", I32),
         ("level_node", P), ("level_start", P), ("topo_level_offset", P), ("node_box", P), ("tri_pos", P),
+        ("refit_source", P),
     ]
 
 
@@ -94,7 +95,8 @@ class Render(C.Structure):
         ("num_cameras", I32), ("camera_pos", P), ("camera_rot", P), ("camera_tan", F32), ("camera_aspect", F32),
         ("num_lights", I32), ("light_dir", P), ("light_intensity", P),
         ("color", P), ("depth", P), ("rays", P), ("ray_depth", P), ("error_flag", P), ("env_point_start", P),
-        ("render_mode", I32), ("texture", P), ("env_texture", P), ("tex_coords", P), ("tex_indices", P),
+        ("render_mode", I32), ("texture", P), ("env_objects", P), ("object_texture", P), ("tex_coords", P),
+        ("tex_indices", P),
     ]
 
 
@@ -134,6 +136,7 @@ def lib() -> C.CDLL:
         "ffsrl_instrument_cartesian": ([P, P, P, P, P, P, P, I32, P], I32),
         "ffsrl_instrument_cartesian_envs": ([P, P, P, P, P, P, P, P, I32, I32, P], I32),
         "ffsrl_instrument_set_rotation_center": ([P, P, P, P, P, P, I32, P], I32),
+        "ffsrl_instrument_visual_update": ([P, P, P, I32, P, P, P, I32, I32, P], I32),
         "ffsrl_grasp_nearest_envs": ([P, P, P, P, P, F32, P, P, I32, I32, P], I32),
         "ffsrl_bvh_refit_fused_envs": ([pb, P, P, P, I32, P], I32),
         "ffsrl_render_fused_envs": ([pr, pb, P, I32, P], I32),

@@ -45,11 +45,41 @@ def build_topology(points: np.ndarray, faces: np.ndarray, bins: int = 8) -> dict
     return out
 
 
+def reference_refit_source(simModel) -> np.ndarray | None:
+    """The face whose box the reference's refit takes for each visual face, or None where
+    it takes the face itself everywhere.
+
+    The reference orders the visual faces object by object over all envs (soft meshes,
+    then rigid meshes, then instruments; M, Rg and Lf faces per env) and its refit shifts
+    an env-local face id to that order testing ``>`` (``bvh.py:66-74``) where the traversal
+    tests ``>=`` (``render.py:462-470``).  So env e's local face M (its first rigid or
+    instrument face) is boxed from env e+1's face 0, and with both rigids and an
+    instrument its local face M + Rg from env e+1's face M; the last env wraps to env 0's
+    faces M and M + Rg.  Defined when every env has the same object face counts (the
+    reference's only layout) and more than one env."""
+    m = simModel
+    N, M = m.numEnvs, m.numEnvMeshesVisFaces
+    Rg, Lf = m.numEnvRigidsVisFaces, m.numEnvLaparoscopeVisFaces
+    if Rg + Lf == 0 or N < 2 or not m.uniformVisLayout:
+        return None
+    efo = m.envVisFaceStart[:-1].astype(np.int64)
+    src = np.arange(int(m.envVisFaceStart[-1]), dtype=np.int64)
+    last = np.arange(N) == N - 1
+    nxt = np.roll(efo, -1)
+    src[efo + M] = np.where(last, efo[0] + M, nxt)
+    if Rg > 0 and Lf > 0:
+        src[efo + M + Rg] = np.where(last, efo[0] + M + Rg, nxt + M)
+    return src.astype(np.int32)
+
+
 class SimBVH:
     def __init__(self, device, simModel, binsNumber: int = 8, save: bool = False, load: bool = False,
-                 path: str = "bvh.npz") -> None:
+                 path: str = "bvh.npz", referenceRefitShift: bool = True) -> None:
+        """``referenceRefitShift``: box the leaves as the reference's refit does at the
+        object boundaries (``reference_refit_source``); False boxes every face itself."""
         self.device = torch.device(device)
         self.simModel = simModel
+        self.referenceRefitShift = bool(referenceRefitShift)
         self.binsNumber = int(binsNumber)
         self.numEnvs = simModel.numEnvs
         self.refitGraph = None
@@ -167,6 +197,9 @@ class SimBVH:
         d.total_env_nodes = self.numAllNodes
         d.total_topology_nodes = int(nn.sum())
         d.max_level = self.maxLevel
+        src = reference_refit_source(m) if self.referenceRefitShift else None
+        self.refitSource = None if src is None else T(src)
+        d.refit_source = None if src is None else ptr(self.refitSource)
 
     # ------------------------------------------------------------- npz files
     def saveBVH(self, path: str) -> None:

@@ -308,3 +308,90 @@ def add_texture(mesh: dict, size: int = 64, seed: int = 0, per_corner: bool = Fa
         out["tex_coords"] = uv.astype(np.float32)
         out["tex_indices"] = np.asarray(mesh["vis_face"], dtype=np.int32).reshape(-1)
     return out
+
+
+def _outward(points: np.ndarray, faces: np.ndarray, centre) -> np.ndarray:
+    """Flip the faces of a star-shaped surface (about ``centre``) whose normals point inward."""
+    p = points[faces]
+    n = np.cross(p[:, 1] - p[:, 0], p[:, 2] - p[:, 0])
+    inward = np.einsum("ij,ij->i", n, p.mean(axis=1) - np.asarray(centre)) < 0
+    faces = faces.copy()
+    faces[inward] = faces[inward][:, [0, 2, 1]]
+    return faces
+
+
+def capsule(radius: float = 1.0, height: float = 1.0, sections=(10, 10)) -> tuple[np.ndarray, np.ndarray]:
+    """Triangle mesh of a capsule along z, centred at the origin: a cylinder of ``height``
+    between two hemispheres of ``radius``.  ``sections`` = (latitude rings over both caps,
+    segments around).  The reference generates its instrument capsules with
+    ``trimesh.creation.capsule`` (``utils.py:105-107``, not available here); this is a
+    tessellation of the same solid, with poles, ``sections[0] // 2`` rings per cap and
+    outward faces."""
+    nlat, nlon = max(1, int(sections[0]) // 2), max(3, int(sections[1]))
+    rings = []
+    for k in range(1, nlat + 1):          # bottom cap, from below the equator up to it
+        a = -0.5 * np.pi + 0.5 * np.pi * k / nlat
+        rings.append((-0.5 * height + radius * np.sin(a), radius * np.cos(a)))
+    for k in range(0, nlat):              # top cap, from the equator up
+        a = 0.5 * np.pi * k / nlat
+        rings.append((0.5 * height + radius * np.sin(a), radius * np.cos(a)))
+    phi = 2.0 * np.pi * np.arange(nlon) / nlon
+    pts = [[0.0, 0.0, -0.5 * height - radius]]
+    for zr, rr in rings:
+        pts += [[rr * np.cos(f), rr * np.sin(f), zr] for f in phi]
+    pts.append([0.0, 0.0, 0.5 * height + radius])
+    pts = np.asarray(pts, dtype=np.float64)
+    top = len(pts) - 1
+    ring = lambda i, j: 1 + i * nlon + (j % nlon)
+    faces = [[0, ring(0, j + 1), ring(0, j)] for j in range(nlon)]
+    for i in range(len(rings) - 1):
+        for j in range(nlon):
+            a, b, c, d = ring(i, j), ring(i, j + 1), ring(i + 1, j + 1), ring(i + 1, j)
+            faces += [[a, b, c], [a, c, d]]
+    faces += [[top, ring(len(rings) - 1, j), ring(len(rings) - 1, j + 1)] for j in range(nlon)]
+    return pts, _outward(pts, np.asarray(faces, dtype=np.int64), (0.0, 0.0, 0.0))
+
+
+def instrument_mesh(rod: float = 12.0, clamp: float = 1.2, radii=(0.15, 0.05, 0.05), sections=(10, 10),
+                    colors=((0.55, 0.55, 0.6), (0.75, 0.75, 0.8), (0.75, 0.75, 0.8)),
+                    offsets=(0.0, 0.5, 0.5)) -> dict:
+    """Visual mesh of a laparoscope: rod, left clamp and right clamp capsules
+    (``laparoscope.py:388-422``), each in the frame of its transform slot -- 6 (rod), 4 and
+    5 (clamp pivots), as ``modelDO.py:1031-1033`` assigns them -- and shifted along its z
+    by ``offsets`` x its height.  The reference shifts its generated capsules by -h/2 to
+    suit its USD frames (``laparoscope.py:402``); for the synthetic instrument of
+    ``scenarios.instrument_xforms`` the rod frame is the capsule's centre (shift 0) and
+    each clamp starts at its pivot (shift +h/2), so the visual mesh covers the contact
+    capsules.  Visual radii are half the contact radii (the reference doubles them for
+    contact, ``laparoscope.py:378``)."""
+    pts, faces, slot, col = [], [], [], []
+    n0 = 0
+    for h, r, s, off, c in zip((rod, clamp, clamp), radii, (6, 4, 5), offsets, colors):
+        p, f = capsule(r, h, sections)
+        p = p + np.array([0.0, 0.0, off * h])
+        pts.append(p)
+        faces.append(f + n0)
+        slot.append(np.full(len(p), s, dtype=np.int32))
+        col.append(np.tile(np.asarray(c, dtype=np.float32), (len(p), 1)))
+        n0 += len(p)
+    return {"points": np.concatenate(pts).astype(np.float32), "faces": np.concatenate(faces).astype(np.int32),
+            "slot": np.concatenate(slot), "color": np.concatenate(col)}
+
+
+def rigid_box(lo, hi, color=(0.45, 0.35, 0.3)) -> dict:
+    """A static axis-aligned box (12 outward triangles) as a rigid visual object, e.g. the
+    table or the abdominal wall under an organ (the reference's ``SimRigidDO``)."""
+    lo, hi = np.asarray(lo, dtype=np.float64), np.asarray(hi, dtype=np.float64)
+    c = np.array([[(hi if (k >> d) & 1 else lo)[d] for d in range(3)] for k in range(8)])
+    quads = [(0, 2, 3, 1), (4, 5, 7, 6), (0, 1, 5, 4), (2, 6, 7, 3), (0, 4, 6, 2), (1, 3, 7, 5)]
+    f = np.array([[q[0], q[1], q[2]] for q in quads] + [[q[0], q[2], q[3]] for q in quads], dtype=np.int64)
+    f = _outward(c, f, 0.5 * (lo + hi))
+    return {"vertex": c.astype(np.float32), "triangle": f.astype(np.int32),
+            "color": np.tile(np.asarray(color, dtype=np.float32), (8, 1))}
+
+
+def with_rigids(mesh: dict, rigids) -> dict:
+    """A copy of ``mesh`` carrying static rigid visual objects (``rigid_box`` dicts)."""
+    out = dict(mesh)
+    out["rigids"] = list(rigids)
+    return out

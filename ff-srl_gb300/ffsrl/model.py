@@ -41,7 +41,17 @@ class SimModelDO:
       the reference DO step's volume, distance, drag, connectors and contact);
     * ``distanceCompliance`` / ``volumeComplianceXPBD``: XPBD alphas for the compliant
       variants (``integrator.py:191-240, 507-576``);
-    * ``toolRadius``: capsule radii of the synthetic instrument (rod, clamps).
+    * ``toolRadius``: capsule radii of the synthetic instrument (rod, clamps);
+    * ``instrumentMesh``: the instrument's visual mesh, shared by every env (the reference
+      reads it from USD or generates capsules, ``laparoscope.py:388-496``): ``points`` [Lp, 3]
+      in the frames of their transform slots, ``faces`` [Lf, 3], ``slot`` [Lp] (6 rod, 4/5
+      clamp pivots, ``modelDO.py:1031-1033``) and ``color`` [Lp, 3]
+      (``meshgen.instrument_mesh`` builds one).  Its points follow the transforms
+      (``transformSimLaparoscopeMeshData``) and it is rendered with the env.
+
+    A mesh dict may list static rigid meshes under ``"rigids"`` (``vertex`` [Q, 3],
+    ``triangle`` [G, 3], optional ``color`` and texture keys): visual-only objects of the
+    env, as the reference's ``SimRigidDO`` (``modelDO.py:642-770, 996-1008``).
     """
 
     def __init__(self, stage, numEnvs, device="cuda:0",
@@ -56,7 +66,7 @@ class SimModelDO:
                  workspaceLow=(-1e5, -1e5, -1e5), workspaceHigh=(1e5, 1e5, 1e5),
                  startingBoxLow=(-1e5, -1e5, -1e5), startingBoxHigh=(1e5, 1e5, 1e5),
                  constraints=None, distanceCompliance=0.0, volumeComplianceXPBD=0.0,
-                 toolRadius=(0.004, 0.002, 0.002)):
+                 toolRadius=(0.004, 0.002, 0.002), instrumentMesh=None):
         if hasattr(stage, "GetPrimAtPath"):
             raise _lib.FFSRLError(_lib.ERR_UNSUPPORTED,
                                   "USD stages are not supported; pass ffsrl.meshgen mesh dicts (array scene)")
@@ -96,6 +106,8 @@ class SimModelDO:
         self.volumeComplianceXPBD = float(volumeComplianceXPBD)
         self.reduce = False
 
+        self.instrumentMesh = self._check_instrument_mesh(instrumentMesh)
+
         # distinct meshes (topologies) and the env -> mesh map
         uniq, self.envMesh = [], []
         for m in meshes:
@@ -112,7 +124,31 @@ class SimModelDO:
         self._batch = None
 
     # ------------------------------------------------------------------ build
+    @staticmethod
+    def _check_instrument_mesh(im):
+        if im is None:
+            return None
+        out = dict(im)
+        out["points"] = np.ascontiguousarray(np.asarray(im["points"], dtype=np.float32).reshape(-1, 3))
+        out["faces"] = np.ascontiguousarray(np.asarray(im["faces"], dtype=np.int32).reshape(-1, 3))
+        out["slot"] = np.ascontiguousarray(np.asarray(im["slot"], dtype=np.int32).reshape(-1))
+        Lp = len(out["points"])
+        out["color"] = np.ascontiguousarray(np.asarray(im.get("color", np.full((Lp, 3), 0.6)),
+                                                       dtype=np.float32).reshape(-1, 3))
+        if len(out["slot"]) != Lp or len(out["color"]) != Lp:
+            raise ValueError("instrumentMesh: slot and color need one entry per point")
+        if Lp and (out["slot"].min() < 0 or out["slot"].max() > 6):
+            raise ValueError("instrumentMesh: slots are 0..6")
+        if len(out["faces"]) and (out["faces"].min() < 0 or out["faces"].max() >= Lp):
+            raise ValueError("instrumentMesh: face index out of range")
+        return out
+
     def _concatenate(self, meshes, toolRadius):
+        """Concatenate the envs' arrays.  Each env's visual points and faces are its objects'
+        one after another -- the soft mesh's (``vis_face`` over its surface points), the
+        static rigid meshes' (``mesh["rigids"]``) and the instrument's visual mesh
+        (``instrumentMesh``) -- so an env's local face ids are the reference's
+        (``modelDO.py:1231-1246, 1279-1326``); envs follow one another (env-major)."""
         N = self.numEnvs
         nv = np.array([len(m["vertex"]) for m in meshes], dtype=np.int64)
         nt = np.array([len(m["tetrahedron"]) for m in meshes], dtype=np.int64)
@@ -120,16 +156,33 @@ class SimModelDO:
         nf = np.array([len(m["triangle"]) for m in meshes], dtype=np.int64)
         npnt = np.array([len(m["point_to_vertex"]) for m in meshes], dtype=np.int64)
         nvf = np.array([len(m["vis_face"]) for m in meshes], dtype=np.int64)
+        rigids = [list(m.get("rigids", ())) for m in meshes]
+        for rs in rigids:
+            for r in rs:
+                q = np.asarray(r["vertex"]).reshape(-1, 3)
+                g = np.asarray(r["triangle"]).reshape(-1, 3)
+                if len(g) and (g.min() < 0 or g.max() >= len(q)):
+                    raise ValueError("rigid mesh: triangle index out of range")
+        nq = np.array([sum(len(np.asarray(r["vertex"]).reshape(-1, 3)) for r in rs) for rs in rigids], dtype=np.int64)
+        ng = np.array([sum(len(np.asarray(r["triangle"]).reshape(-1, 3)) for r in rs) for rs in rigids],
+                      dtype=np.int64)
+        inst = self.instrumentMesh
+        Lp = len(inst["points"]) if inst is not None else 0
+        Lf = len(inst["faces"]) if inst is not None else 0
         z = np.zeros(1, dtype=np.int64)
-        if int(nv.sum()) >= 2**31 or 4 * int(nt.sum()) >= 2**31 or 3 * int(nf.sum()) >= 2**31:
+        if int(nv.sum()) >= 2**31 or 4 * int(nt.sum()) >= 2**31 or 3 * int(nf.sum()) >= 2**31 or \
+                3 * int((nvf + ng).sum() + N * Lf) >= 2**31:
             raise ValueError("model exceeds int32 indexing")
         self.envVertexStart = np.concatenate([z, np.cumsum(nv)]).astype(np.int32)
         self.envTetStart = np.concatenate([z, np.cumsum(nt)]).astype(np.int32)
         self.envEdgeStart = np.concatenate([z, np.cumsum(ne)]).astype(np.int32)
         self.envTriStart = np.concatenate([z, np.cumsum(nf)]).astype(np.int32)
-        self.envVisPointStart = np.concatenate([z, np.cumsum(npnt)]).astype(np.int32)
-        self.envVisFaceStart = np.concatenate([z, np.cumsum(nvf)]).astype(np.int32)
+        self.envVisPointStart = np.concatenate([z, np.cumsum(npnt + nq + Lp)]).astype(np.int32)
+        self.envVisFaceStart = np.concatenate([z, np.cumsum(nvf + ng + Lf)]).astype(np.int32)
+        # remap pairs: the soft mesh's points only, env after env
+        self.envMapStart = np.concatenate([z, np.cumsum(npnt)]).astype(np.int32)
         vo, po = self.envVertexStart[:-1].astype(np.int64), self.envVisPointStart[:-1].astype(np.int64)
+        self.envInstrumentPointStart = (po + npnt + nq).astype(np.int32)
         h = {}
         h["vertex"] = _cat([m["vertex"] for m in meshes], np.float32).reshape(-1, 3)
         h["inverseMass"] = _cat([m["inverse_mass"] for m in meshes], np.float32)
@@ -143,8 +196,24 @@ class SimModelDO:
         h["triangle"] = _cat([m["triangle"].reshape(-1) + vo[e] for e, m in enumerate(meshes)], np.int32)
         h["triToEnv"] = np.repeat(np.arange(N, dtype=np.int32), nf)
         h["vertexToEnv"] = np.repeat(np.arange(N, dtype=np.int32), nv)
-        h["allVisFace"] = _cat([m["vis_face"].reshape(-1) + po[e] for e, m in enumerate(meshes)], np.int32)
-        h["allVisPointColor"] = _cat([m["vis_point_color"] for m in meshes], np.float32).reshape(-1, 3)
+        faces, colors, static = [], [], []
+        grey = np.array([0.6, 0.6, 0.6], dtype=np.float32)
+        for e, m in enumerate(meshes):
+            faces.append(np.asarray(m["vis_face"]).reshape(-1) + po[e])
+            colors.append(np.asarray(m["vis_point_color"], dtype=np.float32).reshape(-1, 3))
+            off = po[e] + npnt[e]
+            for r in rigids[e]:
+                q = np.asarray(r["vertex"], dtype=np.float32).reshape(-1, 3)
+                faces.append(np.asarray(r["triangle"]).reshape(-1) + off)
+                colors.append(np.asarray(r.get("color", np.broadcast_to(grey, q.shape)), dtype=np.float32).reshape(-1, 3))
+                static.append((off, q))
+                off += len(q)
+            if inst is not None:
+                faces.append(np.asarray(inst["faces"]).reshape(-1) + off)
+                colors.append(np.asarray(inst["color"], dtype=np.float32).reshape(-1, 3))
+        h["allVisFace"] = _cat(faces, np.int32)
+        h["allVisPointColor"] = _cat(colors, np.float32).reshape(-1, 3)
+        self._staticVisPoints = static
         ptv = []
         for e, m in enumerate(meshes):
             pv = m["point_to_vertex"].astype(np.int64).copy()
@@ -152,28 +221,35 @@ class SimModelDO:
             pv[:, 1] += vo[e]
             ptv.append(pv.reshape(-1))
         h["pointToVertex"] = _cat(ptv, np.int32)
-        # grasp candidates: the surface (visual) vertices of each env
-        self.graspCandStart = self.envVisPointStart.copy()
+        # grasp candidates: the surface (visual) vertices of each env's soft mesh
+        self.graspCandStart = self.envMapStart.copy()
         h["graspCand"] = h["pointToVertex"][1::2].copy()
-        self._concatenate_textures(h)
+        self._concatenate_textures(h, rigids, nvf, ng, Lf)
         self.host = h
 
         self.numVertices = int(self.envVertexStart[-1])
         self.numTetrahedrons = int(self.envTetStart[-1])
         self.numEdges = int(self.envEdgeStart[-1])
         self.numTriangles = int(self.envTriStart[-1])
-        self.numVisPoints = int(self.envVisPointStart[-1])
-        self.numAllVisPoints = self.numVisPoints
-        self.numVisFaces = int(self.envVisFaceStart[-1])
-        self.numAllVisFaces = self.numVisFaces
+        self.numVisPoints = int(self.envMapStart[-1])         # soft-mesh visual points (remapped)
+        self.numAllVisPoints = int(self.envVisPointStart[-1])
+        self.numVisFaces = int(nvf.sum())
+        self.numAllVisFaces = int(self.envVisFaceStart[-1])
+        self.numRigidVisPoints, self.numRigidVisFaces = int(nq.sum()), int(ng.sum())
+        self.numLaparoscopeVisPoints, self.numLaparoscopeVisFaces = N * Lp, N * Lf
         self.simConnectors = 0
         # per-env sizes (the reference assumes identical envs; these hold env 0's)
         self.environmentNumVertices = int(nv[0])
         self.numEnvAllVertices = int(nv[0])
         self.numEnvMeshesVisPoints = int(npnt[0])
         self.numEnvMeshesVisFaces = int(nvf[0])
-        self.numEnvRigidsVisFaces = 0
-        self.numEnvLaparoscopeVisFaces = 0
+        self.numEnvRigidsVisPoints = int(nq[0])
+        self.numEnvRigidsVisFaces = int(ng[0])
+        self.numEnvLaparoscopeVisPoints = Lp
+        self.numEnvLaparoscopeVisFaces = Lf
+        self.numEnvAllVisFaces = int(nvf[0] + ng[0] + Lf)
+        # all envs alike in their object face counts: the reference's layout assumption
+        self.uniformVisLayout = bool(np.all(nvf == nvf[0]) and np.all(ng == ng[0]))
 
         # synthetic instrument: 3 capsules + drag point per env, parked far above
         r = np.asarray(toolRadius, dtype=np.float32)
@@ -184,37 +260,67 @@ class SimModelDO:
         rad = np.tile(np.array([r[0], r[1], r[2], 0.0], dtype=np.float32), N)
         self.toolHost = {"base": base, "tip": tip, "radius": rad}
 
-    def _concatenate_textures(self, h):
-        """Texture tables of the renderer's texture mode (modelDO.py:1056-1125): each distinct
-        mesh's ``texture`` [S, S, 3] in [0, 1], ``tex_coords`` [T, 2] and ``tex_indices`` (3 per
-        visual face, default ``vis_face``, as modelDO.py:636-640) appended once; per env
-        ``envTexture`` = (first texel, S, first tex coord, first tex index), S = 0 for none."""
-        tex, coords, idx, slot = [], [], [], []
-        nt = nc = ni = 0
-        for m in self.meshes:
-            if m.get("texture") is None:
-                slot.append((0, 0, 0, 0))
-                continue
-            t = np.asarray(m["texture"], dtype=np.float32)
-            if t.ndim != 3 or t.shape[0] != t.shape[1] or t.shape[2] != 3 or t.shape[0] < 1:
-                raise ValueError("texture must be a square [S, S, 3] array")
-            c = np.asarray(m["tex_coords"], dtype=np.float32).reshape(-1, 2)
-            i = np.asarray(m.get("tex_indices", m["vis_face"]), dtype=np.int64).reshape(-1)
-            if len(i) != 3 * len(m["vis_face"]) or (len(i) and (i.min() < 0 or i.max() >= len(c))):
-                raise ValueError("tex_indices must hold 3 tex-coord ids per visual face")
-            S = t.shape[0]
-            slot.append((nt, S, nc, ni))
-            tex.append(t.reshape(-1))
-            coords.append(c.reshape(-1))
-            idx.append(i)
-            nt, nc, ni = nt + S * S, nc + len(c), ni + len(i)
-        self.hasTextures = bool(tex)
-        if nt >= 2**31 or ni >= 2**31:
+    @staticmethod
+    def _texture_entry(obj, num_faces, tables):
+        """Append one object's texture (modelDO.py:1056-1125) to ``tables`` once (objects are
+        deduplicated by identity) and return (first texel, S, first tex coord, first tex
+        index), or zeros for an object without ``texture``."""
+        if obj is None or obj.get("texture") is None:
+            return (0, 0, 0, 0)
+        for o, ent in tables["seen"]:
+            if o is obj:
+                return ent
+        t = np.asarray(obj["texture"], dtype=np.float32)
+        if t.ndim != 3 or t.shape[0] != t.shape[1] or t.shape[2] != 3 or t.shape[0] < 1:
+            raise ValueError("texture must be a square [S, S, 3] array")
+        c = np.asarray(obj["tex_coords"], dtype=np.float32).reshape(-1, 2)
+        default = obj.get("vis_face", obj.get("triangle", obj.get("faces")))
+        i = np.asarray(obj.get("tex_indices", default), dtype=np.int64).reshape(-1)
+        if len(i) != 3 * num_faces or (len(i) and (i.min() < 0 or i.max() >= len(c))):
+            raise ValueError("tex_indices must hold 3 tex-coord ids per visual face")
+        S = t.shape[0]
+        ent = (tables["nt"], S, tables["nc"], tables["ni"])
+        tables["tex"].append(t.reshape(-1))
+        tables["coords"].append(c.reshape(-1))
+        tables["idx"].append(i)
+        tables["nt"] += S * S
+        tables["nc"] += len(c)
+        tables["ni"] += len(i)
+        tables["seen"].append((obj, ent))
+        return ent
+
+    def _concatenate_textures(self, h, rigids, nvf, ng, Lf):
+        """Object and texture tables of the renderer's texture mode.  Per env, its objects
+        in face order -- soft mesh, rigids, instrument -- each as (first env-local face, first
+        texel, S, first tex coord, first tex index); S = 0 for an object without a texture
+        (rendered with its vertex colours).  A texture is ``texture`` [S, S, 3] in [0, 1],
+        ``tex_coords`` [T, 2] and ``tex_indices`` (3 per face, default the faces themselves,
+        as modelDO.py:636-640)."""
+        tables = {"tex": [], "coords": [], "idx": [], "nt": 0, "nc": 0, "ni": 0, "seen": []}
+        objects, env_objects, per_mesh = [], [], {}
+        inst = self.instrumentMesh
+        for e, k in enumerate(self.envMesh):
+            if k not in per_mesh:
+                m = self.meshes[k]
+                ents = [(0,) + self._texture_entry(m, len(m["vis_face"]), tables)]
+                f0 = int(nvf[e])
+                for r in rigids[e]:
+                    g = len(np.asarray(r["triangle"]).reshape(-1, 3))
+                    ents.append((f0,) + self._texture_entry(r, g, tables))
+                    f0 += g
+                if inst is not None:
+                    ents.append((f0,) + self._texture_entry(inst, Lf, tables))
+                per_mesh[k] = (len(objects), len(ents))
+                objects += ents
+            env_objects.append(per_mesh[k])
+        self.hasTextures = bool(tables["tex"])
+        if tables["nt"] >= 2**31 or tables["ni"] >= 2**31:
             raise ValueError("textures exceed int32 indexing")
-        h["texture"] = _cat(tex, np.float32)
-        h["texCoords"] = _cat(coords, np.float32)
-        h["texIndices"] = _cat(idx, np.int32)
-        h["envTexture"] = np.asarray([slot[k] for k in self.envMesh], dtype=np.int32).reshape(-1)
+        h["texture"] = _cat(tables["tex"], np.float32)
+        h["texCoords"] = _cat(tables["coords"], np.float32)
+        h["texIndices"] = _cat(tables["idx"], np.int32)
+        h["objectTexture"] = np.asarray(objects, dtype=np.int32).reshape(-1)
+        h["envObjects"] = np.asarray(env_objects, dtype=np.int32).reshape(-1)
 
     def _upload(self):
         d = self.device
@@ -250,8 +356,15 @@ class SimModelDO:
         self.vertexToEnv = T(h["vertexToEnv"], **i32)
         self.activeDragConstraint = torch.zeros(self.numVertices, **f32)
         ptv = h["pointToVertex"].reshape(-1, 2)
-        vis0 = np.zeros((self.numVisPoints, 3), dtype=np.float32)
+        vis0 = np.zeros((self.numAllVisPoints, 3), dtype=np.float32)
         vis0[ptv[:, 0]] = h["vertex"][ptv[:, 1]]
+        for off, q in self._staticVisPoints:  # rigid meshes: visual points that never move
+            vis0[off:off + len(q)] = q
+        inst = self.instrumentMesh
+        if inst is not None:  # local shape until the instrument's transforms are set
+            for e in range(self.numEnvs):
+                o = int(self.envInstrumentPointStart[e])
+                vis0[o:o + len(inst["points"])] = inst["points"]
         self.allVisPoint = T(vis0, **f32)
         self.visPoint = self.allVisPoint
         self.allVisFace = T(h["allVisFace"], **i32)
@@ -260,7 +373,14 @@ class SimModelDO:
         self.textureT = T(h["texture"], **f32)
         self.texCoordsT = T(h["texCoords"], **f32)
         self.texIndicesT = T(h["texIndices"], **i32)
-        self.envTextureT = T(h["envTexture"], **i32)
+        self.objectTextureT = T(h["objectTexture"], **i32)
+        self.envObjectsT = T(h["envObjects"], **i32)
+        self.envMapStartT = T(self.envMapStart, **i32)
+        self.envInstrumentPointStartT = T(self.envInstrumentPointStart, **i32)
+        # the instrument's visual mesh: local points and their transform slots (the
+        # reference's laparoscopeVertex / laparoscopeVertexToXForm, modelDO.py:1217-1221)
+        self.laparoscopeVertex = T(inst["points"] if inst is not None else np.zeros((0, 3), np.float32), **f32)
+        self.laparoscopeVertexToXForm = T(inst["slot"] if inst is not None else np.zeros(0, np.int32), **i32)
         self.pointToVertex = T(h["pointToVertex"], **i32)
         self.graspCand = T(h["graspCand"], **i32)
         self.graspCandStartT = T(self.graspCandStart, **i32)
@@ -374,8 +494,20 @@ class SimModelDO:
         check(lib().ffsrl_remap(ptr(self.allVisPoint), ptr(self.vertex), ptr(self.pointToVertex),
                                 self.numVisPoints, _lib.stream_handle(stream)))
 
-    def transformSimLaparoscopeMeshData(self):
-        """The instrument's visual mesh is not part of this model (synthetic instrument)."""
+    def transformSimLaparoscopeMeshData(self, stream=None, env_ids=None):
+        """updateLaparoscopeMeshKernel (modelDO.py:1446-1473): the instrument's visual points
+        of every env (or of the envs in the int32 device tensor ``env_ids``) from its
+        transforms.  Nothing to do without an instrument mesh or transforms."""
+        if self.instrumentMesh is None or not self.hasInstrumentKinematics:
+            return
+        self.require_cuda()
+        n = self.numEnvs if env_ids is None else int(env_ids.numel())
+        check(lib().ffsrl_instrument_visual_update(ptr(self.laparoscopeXForm), ptr(self.laparoscopeVertex),
+                                                   ptr(self.laparoscopeVertexToXForm),
+                                                   int(self.laparoscopeVertexToXForm.numel()), ptr(self.allVisPoint),
+                                                   ptr(self.envInstrumentPointStartT),
+                                                   None if env_ids is None else ptr(env_ids), n, self.numEnvs,
+                                                   _lib.stream_handle(stream)))
 
     def getVertexPositionsTensor(self, vertexId):
         return self.vertex[vertexId]
@@ -449,6 +581,8 @@ class SimModelDO:
         self.laparoscopeInitialXForm.copy_(self.laparoscopeXForm)
         self.laparoscopeHeight.copy_(torch.as_tensor(np.asarray(heights, dtype=np.float32).reshape(-1)))
         self.hasInstrumentKinematics = True
+        if self.device.type == "cuda":
+            self.transformSimLaparoscopeMeshData()
 
     def _require_kinematics(self):
         self.require_cuda()
@@ -473,6 +607,7 @@ class SimModelDO:
                                                    _lib.stream_handle(stream)))
         self.updateClampsDrag(self.laparoscopeDragCutHeat, self.laparoscopeDragCutHeatUpdate)
         self.transformSimMeshData(stream)
+        self.transformSimLaparoscopeMeshData(stream)
 
     def applyCartesianActions(self, cartesianActions, stream=None):
         """applyCartesianActions (modelDO.py:1364-1383): move each effector by [N, 3]."""
@@ -482,6 +617,7 @@ class SimModelDO:
                                                ptr(self.laparoscopeBase), ptr(self.laparoscopeTip),
                                                ptr(self.laparoscopeHeight), self.numEnvs, _lib.stream_handle(stream)))
         self.transformSimMeshData(stream)
+        self.transformSimLaparoscopeMeshData(stream)
 
     def applyCartesianActionsInWorkspace(self, cartesianActions, stream=None):
         """applyCartesianActionsInWorkspace (modelDO.py:1385-1404): components that would take
@@ -564,16 +700,22 @@ class SimModelDO:
             hm = sel.repeat_interleave(3)
             self.laparoscopeDragCutHeat.masked_fill_(hm, 0)
             self.laparoscopeDragCutHeatUpdate.masked_fill_(hm, 0)
+        self.transformSimLaparoscopeMeshData()
         self.transformSimMeshData()
 
-    def resetStochasticModel(self, *args, **kwargs):
-        """Restore every env (modelDO.py:1624-1645); the instrument returns to its initial pose."""
+    def resetStochasticModel(self, laparoscopeTranslation=None, laparoscopeRotation=None):
+        """Restore every env (modelDO.py:1624-1645); the instrument returns to its initial
+        pose, then, given a translation and rotation [N, 3], its rotation centre takes that
+        pose (``setRotationCenter``)."""
         self.vertex.copy_(self.initialVertex)
         self.laparoscopeBase.copy_(self.laparoscopeInitialBase)
         self.laparoscopeTip.copy_(self.laparoscopeInitialTip)
         self.laparoscopeXForm.copy_(self.laparoscopeInitialXForm)
         self.laparoscopeDragCutHeat.zero_()
         self.laparoscopeDragCutHeatUpdate.zero_()
+        if laparoscopeTranslation is not None and laparoscopeRotation is not None:
+            self.setRotationCenter(laparoscopeTranslation, laparoscopeRotation)
+        self.transformSimLaparoscopeMeshData()
         self.transformSimMeshData()
 
     def envSlice(self, e: int) -> slice:

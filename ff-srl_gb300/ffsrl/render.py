@@ -148,8 +148,9 @@ class WarpRaycastRendererDO:
         r.env_point_start = ptr(simModel.envVisPointStartT)
         r.render_mode = int(self.render_mode)
         if simModel.hasTextures:
-            r.texture, r.env_texture = ptr(simModel.textureT), ptr(simModel.envTextureT)
-            r.tex_coords, r.tex_indices = ptr(simModel.texCoordsT), ptr(simModel.texIndicesT)
+            r.texture, r.tex_coords, r.tex_indices = ptr(simModel.textureT), ptr(simModel.texCoordsT), \
+                ptr(simModel.texIndicesT)
+            r.env_objects, r.object_texture = ptr(simModel.envObjectsT), ptr(simModel.objectTextureT)
         return r
 
     def renderFunctionNew(self, simBVH, stream=None) -> None:

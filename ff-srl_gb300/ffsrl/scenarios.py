@@ -151,14 +151,18 @@ def beam_model(device, num_envs=1, neo=False, xpbd=False, mesh=None, **kw) -> tu
 
 
 def liver_model(device, num_envs, meshes=None, E=NH_E, nu=NH_NU, substeps=8, iterations=10, grasp=True,
-                collide=True, **kw) -> tuple[SimModelDO, list]:
+                collide=True, instrument_visual=True, **kw) -> tuple[SimModelDO, list]:
     """Config 1 (meshes=None: the 12/8/6 cm ellipsoid in every env) or a given list
-    of meshes (configs 2/4): Neo-Hookean + volume + distance, grasp and contact."""
+    of meshes (configs 2/4): Neo-Hookean + volume + distance, grasp and contact.  With
+    ``instrument_visual`` each env also renders its instrument (``meshgen.instrument_mesh``
+    with the dimensions of ``instrument_xforms``)."""
     if meshes is None:
         meshes = [mg.ellipsoid()] * num_envs
     mu, lam = lame(E, nu)
     flags = L.VOLUME | L.DISTANCE | L.NEOHOOKEAN | L.DRAG | (L.COLLIDE if collide else 0)
     kw.setdefault("environmentGravity", mg.gravity_force(meshes[0]))
+    if instrument_visual:
+        kw.setdefault("instrumentMesh", mg.instrument_mesh())
     m = SimModelDO(meshes, num_envs, device, simSubsteps=substeps, simFrameRate=60, simConstraintsSteps=iterations,
                    environmentGroundLevel=-100.0, constraints=flags, globalVolumeCompliance=1.0 / lam,
                    globalDeviatoricCompliance=1.0 / mu, globalLaparoscopeDragLookupRadius=0.5, **kw)

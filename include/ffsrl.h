@@ -145,6 +145,11 @@ typedef struct {
        12k+9..12k+11 padding, so each triangle is three 16-byte loads; 16-byte aligned */
     float* node_box;                 /* [8 * total_env_nodes] */
     float* tri_pos;                  /* [12 * total env faces] */
+    /* optional [total env faces]: the global face whose vertices enter a leaf's box in
+       place of face f (NULL: f itself).  Reproduces the reference refit's face shift at
+       the object boundaries (bvh.py:66-74 uses `>` where render.py:462-470 uses `>=`);
+       the traversal and tri_pos always use f.  Every entry must be a valid face id. */
+    const int32_t* refit_source;
 } ffsrl_bvh;
 
 /* ---- ray-cast renderer (render.py:826-1196) ------------------------------------ */
@@ -179,11 +184,16 @@ typedef struct {
        4 depth map (t/50 in all three channels); 0, 1 and 3 are Lambert-lit.  `depth` is t/50
        in every mode.  Values outside 0..4 are rejected. */
     int32_t render_mode;
+    /* textures (texture mode; NULL env_objects: no textures).  An env's visual faces are
+       its objects' faces one after another (soft mesh, rigid meshes, instrument); each
+       object may have a texture (modelDO.py:1052-1127).  texel (x, y) of a texture is
+       first + y + x*S (render.py:139-142). */
     const float* texture;            /* [3 * texels] RGB in [0, 1], every texture one after another */
-    const int32_t* env_texture;      /* [4N] per env: first texel, side S (0 = none), first tex coord,
-                                        first tex index; texel (x, y) of a texture is first + y + x*S */
+    const int32_t* env_objects;      /* [2N] per env: first entry in object_texture, number of objects */
+    const int32_t* object_texture;   /* [5 per object]: first env-local face, first texel, side S
+                                        (0 = no texture: vertex colour), first tex coord, first tex index */
     const float* tex_coords;         /* [2T] (u, v) */
-    const int32_t* tex_indices;      /* 3 per env-local visual face: tex coords relative to the env's first */
+    const int32_t* tex_indices;      /* 3 per object-local face: tex coords relative to the object's first */
 } ffsrl_render;
 
 /* ---- library ---------------------------------------------------------------- */
@@ -282,6 +292,15 @@ int32_t ffsrl_instrument_cartesian_envs(float* xform, const float* actions, cons
 int32_t ffsrl_instrument_set_rotation_center(float* xform, const float* translation, const float* rotation,
                                              float* base, float* tip, const float* height, int32_t num_envs,
                                              void* stream);
+/* transformSimLaparoscopeMeshData (modelDO.py:1446-1473, updateLaparoscopeMeshKernel
+   modelDO.py:202-216): the instrument's visual points of each env,
+   vis_point[env_first_point[e] + i] = transform point_slot[i] of env e applied to
+   local_point[i], i < num_points.  One local shape [3 * num_points] serves every env (the
+   reference keeps a copy per env); slots outside 0..6 are skipped.  env_ids NULL: all envs
+   (n must equal num_envs); otherwise the n listed envs. */
+int32_t ffsrl_instrument_visual_update(const float* xform, const float* local_point, const int32_t* point_slot,
+                                       int32_t num_points, float* vis_point, const int32_t* env_first_point,
+                                       const int32_t* env_ids, int32_t n, int32_t num_envs, void* stream);
 /* Rigidly translate each env's instrument (4 bases + 4 tips) by disp[3e..3e+2]. */
 int32_t ffsrl_move_tool(float* laparoscope_base, float* laparoscope_tip, const float* disp, int32_t num_envs,
                         void* stream);

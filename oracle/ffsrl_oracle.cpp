@@ -515,6 +515,35 @@ void refit(const ffsrl_bvh* b, const float* pts, const int32_t* faces) {
         for (int e = 0; e < b->num_envs; ++e) refit_node_level(b, pts, faces, e, L);
 }
 
+// refitBVHLevel's face shift (bvh.py:66-74).  The reference orders visual faces object by
+// object over all envs -- [mesh faces of every env][rigid faces of every env][instrument
+// faces of every env], M, Rg and Lf faces per env -- and its refit maps env e's local face
+// t with `>` where the traversal (render.py:462-470) uses `>=`, so local faces M and M + Rg
+// are boxed from another env's face.  Written here as the env-major global face id the
+// refit reads for each (env, local face): out[env_face_offset[e] + t].
+extern "C" void oracle_reference_refit_source(int N, int M, int Rg, int Lf, const int32_t* env_face_offset,
+                                              int32_t* out) {
+    const int F = M + Rg + Lf;
+    for (int e = 0; e < N; ++e)
+        for (int t = 0; t < F; ++t) {
+            int64_t g;
+            if (t > M + Rg) g = t + int64_t(N - 1) * (M + Rg) + int64_t(e) * Lf;
+            else if (t > M) g = t + int64_t(N - 1) * M + int64_t(e) * Rg;
+            else g = t + int64_t(e) * M;
+            int64_t env, loc;
+            if (g < int64_t(N) * M) {
+                env = g / M; loc = g % M;
+            } else if (g < int64_t(N) * (M + Rg)) {
+                int64_t h = g - int64_t(N) * M;
+                env = h / Rg; loc = M + h % Rg;
+            } else {
+                int64_t h = g - int64_t(N) * (M + Rg);
+                env = h / Lf; loc = M + Rg + h % Lf;
+            }
+            out[env_face_offset[e] + t] = int32_t(env_face_offset[env] + loc);
+        }
+}
+
 // one env's tree, all levels deepest first
 void refit_env(const ffsrl_bvh* b, const float* pts, const int32_t* faces, int e) {
     for (int L = b->max_level; L >= 0; --L) refit_node_level(b, pts, faces, e, L);
@@ -536,6 +565,7 @@ void refit_node_level(const ffsrl_bvh* b, const float* pts, const int32_t* faces
             int first = b->first_tri_id[n0 + n];
             for (int k = 0; k < b->tri_count[n0 + n]; ++k) {
                 int64_t f = int64_t(b->env_face_offset[e]) + b->tri_id[t0 + first + k];
+                if (b->refit_source) f = b->refit_source[f];  // the face the reference's refit boxes
                 V3<float> pA = ld3<float>(pts, faces[3 * f]), pB = ld3<float>(pts, faces[3 * f + 1]),
                           pC = ld3<float>(pts, faces[3 * f + 2]);
                 lo = vmin(pA, vmin(pB, vmin(pC, lo)));
@@ -563,6 +593,15 @@ inline V3<float> quat_rotate(const float* q, V3<float> x) {
 }
 
 struct Hit { int tri; float t; V3<float> p; };
+
+// index of the object of env e holding env-local face lf (visFaceToObjectId, render.py:360):
+// the last of the env's objects whose first face is <= lf
+int object_of(const ffsrl_render* r, int e, int lf) {
+    int o0 = r->env_objects[2 * e], no = r->env_objects[2 * e + 1];
+    int k = 0;
+    while (k + 1 < no && r->object_texture[5 * (o0 + k + 1)] <= lf) ++k;
+    return o0 + k;
+}
 
 // intersectAABB (render.py:588-609): returns hit flag and tmin
 inline bool slab(V3<float> ro, V3<float> rd, V3<float> lo, V3<float> hi, float* tnear) {
@@ -720,12 +759,13 @@ int render_env(const ffsrl_render* r, const ffsrl_bvh* b, int stack_cap, int e, 
                     V3<float> base;
                     if (r->render_mode == 0) {  // grayscale
                         base = mk<float>(1.0f, 1.0f, 1.0f);
-                    } else if (r->render_mode == 1 && r->env_texture && r->env_texture[4 * e + 1] > 0) {
+                    } else if (r->render_mode == 1 && r->env_objects &&
+                               r->object_texture[5 * object_of(r, e, int(h.tri - b->env_face_offset[e])) + 2] > 0) {
                         // texture_interpolation (render.py:123-148), indices clamped into the texture
-                        const int32_t* et = r->env_texture + 4 * e;
-                        int first = et[0], S = et[1], c0 = et[2];
                         int lf = (int)(h.tri - b->env_face_offset[e]);
-                        const int32_t* ti = r->tex_indices + et[3] + 3 * lf;
+                        const int32_t* ob = r->object_texture + 5 * object_of(r, e, lf);
+                        int first = ob[1], S = ob[2], c0 = ob[3];
+                        const int32_t* ti = r->tex_indices + ob[4] + 3 * (lf - ob[0]);
                         const float* ta = r->tex_coords + 2 * (c0 + ti[0]);
                         const float* tb = r->tex_coords + 2 * (c0 + ti[1]);
                         const float* tc = r->tex_coords + 2 * (c0 + ti[2]);
@@ -1050,6 +1090,22 @@ void oracle_instrument_set_rotation_center(float* xform, const float* t, const f
         Mat4 G = kshift_rotate(t[o], t[o + 1], t[o + 2], r[o], r[o + 1], r[o + 2]);
         kslot(X, 3, rc, kmul(kinv(rc), G));
         kends(X, height, base, tip, e);
+    }
+}
+
+// updateLaparoscopeMeshKernel (modelDO.py:202-216) over every env, as
+// transformSimLaparoscopeMeshData launches it (modelDO.py:1446-1473): the env's transform of
+// the point's slot, transposed out of storage, applied to the shared local point
+void oracle_instrument_visual(const float* xform, const float* local, const int* slot, int num_points, float* vis,
+                              const int* env_first_point, int num_envs) {
+    for (int e = 0; e < num_envs; ++e) {
+        const float* X = xform + 112ll * e;
+        for (int i = 0; i < num_points; ++i) {
+            if (slot[i] < 0 || slot[i] > 6) continue;
+            P3 p = kpoint(kload(X, slot[i]), p3(local[3 * i], local[3 * i + 1], local[3 * i + 2]));
+            int64_t o = 3ll * ((int64_t)env_first_point[e] + i);
+            vis[o] = p.x; vis[o + 1] = p.y; vis[o + 2] = p.z;
+        }
     }
 }
 

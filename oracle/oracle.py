@@ -52,6 +52,7 @@ def lib() -> C.CDLL:
         _lib.oracle_render.argtypes = [C.POINTER(L.Render), C.POINTER(L.Bvh), C.c_int]
         _lib.oracle_refit_mt.argtypes = [C.POINTER(L.Bvh), P, P, C.c_int]
         _lib.oracle_render_mt.argtypes = [C.POINTER(L.Render), C.POINTER(L.Bvh), C.c_int, C.c_int]
+        _lib.oracle_reference_refit_source.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, P, P]
         for f in ("oracle_step_f32", "oracle_step_f64", "oracle_render", "oracle_render_mt"):
             getattr(_lib, f).restype = C.c_int
     return _lib
@@ -116,11 +117,16 @@ class OracleSim:
         if rc:
             raise RuntimeError(f"oracle f64 step failed: {rc}")
 
-    def vis_points(self) -> np.ndarray:
+    def vis_points(self, instrument=None) -> np.ndarray:
+        """Every visual point: the soft meshes' remapped from the vertices, the rigid meshes'
+        as built, the instrument's from ``instrument`` (an OracleInstrument; without one,
+        the model's current host copy of those points)."""
         m = self.model
-        out = np.zeros((m.numVisPoints, 3), dtype=np.float32)
+        out = np.ascontiguousarray(m.allVisPoint.detach().cpu().numpy(), dtype=np.float32).copy()
         ptv = np.ascontiguousarray(m.host["pointToVertex"])
         lib().oracle_remap(out.ctypes.data, self.a["vertex"].ctypes.data, ptv.ctypes.data, m.numVisPoints)
+        if instrument is not None and m.instrumentMesh is not None:
+            instrument.visual(m.instrumentMesh["points"], m.instrumentMesh["slot"], out, m.envInstrumentPointStart)
         return out
 
 
@@ -131,6 +137,8 @@ def bvh_desc(bvh, arrays: dict) -> L.Bvh:
              "topo_tri_offset": bvh.topoTriOffset, "topo_max_level": bvh.topoMaxLevel, "left_node": bvh.leftNode,
              "first_tri_id": bvh.firstTriId, "tri_count": bvh.triCount, "level": bvh.level, "tri_id": bvh.triId,
              "aabb_min": bvh.aabbMin, "aabb_max": bvh.aabbMax}
+    if getattr(bvh, "refitSource", None) is not None:
+        names["refit_source"] = bvh.refitSource
     for k, t in names.items():
         arrays[k] = np.ascontiguousarray(t.detach().cpu().numpy())
     d = L.Bvh()
@@ -140,6 +148,15 @@ def bvh_desc(bvh, arrays: dict) -> L.Bvh:
     d.total_env_nodes, d.total_topology_nodes, d.max_level = (bvh.desc.total_env_nodes, bvh.desc.total_topology_nodes,
                                                               bvh.desc.max_level)
     return d
+
+
+def reference_refit_source(num_envs: int, M: int, Rg: int, Lf: int, env_face_offset) -> np.ndarray:
+    """The face each (env, local face) is boxed from by the reference's refit
+    (bvh.py:66-74), as env-major global face ids."""
+    efo = np.ascontiguousarray(np.asarray(env_face_offset, dtype=np.int32))
+    out = np.zeros(num_envs * (M + Rg + Lf), dtype=np.int32)
+    lib().oracle_reference_refit_source(num_envs, M, Rg, Lf, _p(efo), _p(out))
+    return out
 
 
 def refit(bvh, vis_points: np.ndarray, vis_face: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
@@ -176,8 +193,9 @@ def _render_desc(renderer, vis_points: np.ndarray):
     r.num_lights = a["light_dir"].shape[0]
     r.render_mode = int(renderer.render_mode)
     if m.hasTextures:
-        for k, src in (("texture", m.host["texture"]), ("env_texture", m.host["envTexture"]),
-                       ("tex_coords", m.host["texCoords"]), ("tex_indices", m.host["texIndices"])):
+        for k, src in (("texture", m.host["texture"]), ("env_objects", m.host["envObjects"]),
+                       ("object_texture", m.host["objectTexture"]), ("tex_coords", m.host["texCoords"]),
+                       ("tex_indices", m.host["texIndices"])):
             a[k] = np.ascontiguousarray(src)
             setattr(r, k, _p(a[k]))
     return r, a
@@ -211,7 +229,10 @@ class OracleScene:
         self.faces = np.ascontiguousarray(model.host["allVisFace"], dtype=np.int32)
         self.bvh_arrays = {}
         self.bvh = bvh_desc(bvh, self.bvh_arrays)
-        self.r, self.a = _render_desc(renderer, self.sim.vis_points())
+        self.inst = None
+        if model.instrumentMesh is not None and model.hasInstrumentKinematics:
+            self.inst = OracleInstrument.from_model(model)
+        self.r, self.a = _render_desc(renderer, self.sim.vis_points(self.inst))
         self.stack_cap = stack_cap
 
     def step(self, threads: int = 1) -> None:
@@ -220,6 +241,9 @@ class OracleScene:
         vp = self.a["vis_point"]
         lib_.oracle_remap(vp.ctypes.data, self.sim.a["vertex"].ctypes.data, self.ptv.ctypes.data,
                           self.model.numVisPoints)
+        if self.inst is not None:  # transformSimLaparoscopeMeshData, the end of stepModel
+            im = self.model.instrumentMesh
+            self.inst.visual(im["points"], im["slot"], vp, self.model.envInstrumentPointStart)
         lib_.oracle_refit_mt(C.byref(self.bvh), vp.ctypes.data, self.faces.ctypes.data, int(threads))
         rc = lib_.oracle_render_mt(C.byref(self.r), C.byref(self.bvh), int(self.stack_cap), int(threads))
         if rc:
@@ -235,6 +259,7 @@ def _kin_lib():
         lb.oracle_instrument_apply_actions.argtypes = [P, P, P, P, P, P, P, C.c_int]
         lb.oracle_instrument_cartesian.argtypes = [P, P, P, P, P, P, P, C.c_int]
         lb.oracle_instrument_set_rotation_center.argtypes = [P, P, P, P, P, P, C.c_int]
+        lb.oracle_instrument_visual.argtypes = [P, P, P, C.c_int, P, P, C.c_int]
         lb._kin_ready = True
     return lb
 
@@ -251,6 +276,13 @@ class OracleInstrument:
                                            np.asarray(a, dtype=np.int32).reshape(-1)).copy()
         self.dch, self.dchu = i(dch), i(dchu)
         self.violation = np.zeros(self.n, dtype=np.int32)
+
+    @classmethod
+    def from_model(cls, model):
+        """Host copy of a SimModelDO's instrument state."""
+        c = lambda t: t.detach().cpu().numpy()
+        return cls(c(model.laparoscopeXForm), c(model.laparoscopeHeight), c(model.laparoscopeBase),
+                   c(model.laparoscopeTip), c(model.laparoscopeDragCutHeat), c(model.laparoscopeDragCutHeatUpdate))
 
     def update(self):
         _kin_lib().oracle_instrument_update(_p(self.xform), _p(self.base), _p(self.tip), _p(self.height), self.n)
@@ -271,3 +303,12 @@ class OracleInstrument:
         r = np.ascontiguousarray(np.asarray(rotation, dtype=np.float32).reshape(-1))
         _kin_lib().oracle_instrument_set_rotation_center(_p(self.xform), _p(t), _p(r), _p(self.base), _p(self.tip),
                                                          _p(self.height), self.n)
+
+    def visual(self, local_points, point_slot, vis_points, env_first_point):
+        """Instrument visual points of every env written into ``vis_points`` (in place)."""
+        lp = np.ascontiguousarray(np.asarray(local_points, dtype=np.float32).reshape(-1))
+        sl = np.ascontiguousarray(np.asarray(point_slot, dtype=np.int32).reshape(-1))
+        fp = np.ascontiguousarray(np.asarray(env_first_point, dtype=np.int32).reshape(-1))
+        assert vis_points.dtype == np.float32 and vis_points.flags["C_CONTIGUOUS"]
+        _kin_lib().oracle_instrument_visual(_p(self.xform), _p(lp), _p(sl), len(sl), _p(vis_points), _p(fp), self.n)
+        return vis_points

@@ -71,7 +71,7 @@ def grasp_flags(model, radius: float = GRASP_RADIUS) -> np.ndarray:
 
 
 def liver_model(device, meshes):
-    return sc.liver_model(device, len(meshes), meshes=meshes)[0]
+    return sc.liver_model(device, len(meshes), meshes=meshes, instrument_visual=False)[0]
 
 
 def renderer(device, model, meshes):

@@ -264,7 +264,7 @@ def test_threaded_scene_matches_serial(oracle_lib):
     scene.step(threads=3)
     o = oracle.OracleSim(m)
     o.step(1)
-    vp = o.vis_points()
+    vp = o.vis_points(oracle.OracleInstrument.from_model(m))
     lo, hi = oracle.refit(bvh, vp, m.host["allVisFace"])
     col, dep, _ = oracle.render(r, bvh, vp, aabb=(lo, hi))
     np.testing.assert_array_equal(scene.sim.a["vertex"], o.a["vertex"])

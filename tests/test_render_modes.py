@@ -103,7 +103,9 @@ def test_texture_tables_per_distinct_mesh():
     m = SimModelDO([a, b, a, b], 4, "cpu", environmentGravity=(0.0, 0.0, 0.0))
     assert m.hasTextures
     assert m.host["texture"].size == 3 * S * S  # stored once for the two envs that share it
-    assert m.host["envTexture"].reshape(4, 4).tolist() == [[0, S, 0, 0], [0, 0, 0, 0]] * 2
+    # one object per env (the soft mesh): (first face, first texel, S, first coord, first index)
+    assert m.host["objectTexture"].reshape(-1, 5).tolist() == [[0, 0, S, 0, 0], [0, 0, 0, 0, 0]]
+    assert m.host["envObjects"].reshape(4, 2).tolist() == [[0, 1], [1, 1]] * 2
     bad = _flat(tex, np.zeros((2, 2), np.float32))  # vis_face refers to tex coord 2
     with pytest.raises(ValueError):
         SimModelDO(bad, 1, "cpu")
@@ -167,7 +169,8 @@ def test_render_modes_gpu_match_oracle(gpu, oracle_lib, fused):
             assert np.abs(g_col - col).max() < 1e-5, f"mode {mode}"
         seen[mode] = g_col
     # the texture changes the textured envs only
-    tex_env = m.host["envTexture"].reshape(-1, 4)[:, 1] > 0
+    ot, eo = m.host["objectTexture"].reshape(-1, 5), m.host["envObjects"].reshape(-1, 2)
+    tex_env = ot[eo[:, 0], 2] > 0  # the env's soft mesh has a texture
     assert not np.allclose(seen[1][tex_env], seen[3][tex_env], atol=1e-3)
     if fused:
         assert np.array_equal(seen[1][~tex_env], seen[3][~tex_env])
