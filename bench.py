@@ -64,7 +64,8 @@ def dist_env():
 
 def config(envs, n):
     return {"workload": f"{envs} mixed-size ellipsoid envs (tets log-uniform 500-20000), 8 substeps x 10 iterations, "
-                        f"Neo-Hookean+volume+distance+grasp+contact, BVH refit, {RES}x{RES} depth+colour ray-cast",
+                        f"Neo-Hookean+volume+distance+grasp+contact, kinematic instrument (rendered), BVH refit, "
+                        f"{RES}x{RES} depth+colour ray-cast",
             "envs_per_gpu": envs, "pool_meshes": POOL, "substeps": 8, "iterations": 10, "resolution": RES,
             "parallelism": f"env-shard x{n}", "l2": "working set (GBs) exceeds the 129 MB L2; no flush needed",
             "episode_steps": EPISODE, "episode_reset": "all envs to rest state + grasp, inside the timed region"}
@@ -368,9 +369,9 @@ def main():
             cpu = {"value": v, "unit": "env-steps/s", "cores": threads, "kind": "port",
                    "sample": f"32 envs of the same pool, 1 full env-step (8x10 solve, refit, {RES}x{RES} ray-cast), "
                              "oracle restatement, OpenMP over envs"}
-        # per step: instrument kinematics, one launch per size class, remap, fused refit, normal gather, rays;
-        # per episode reset: remap and grasp
-        launches = K * (n_cls + 5) + 2 * resets_timed
+        # per step: instrument kinematics, one launch per size class, remap, instrument visual points,
+        # fused refit, normal gather, rays; per episode reset: instrument visual points, remap and grasp
+        launches = K * (n_cls + 6) + 3 * resets_timed
         line = {"metric": METRIC, "value": value, "unit": "env-steps/s", "n_gpus": world, "steps": K,
                 "warmup": W, "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded meshes and random-walk actions)",

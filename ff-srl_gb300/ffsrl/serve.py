@@ -305,7 +305,8 @@ class EnvServer:
                     self.actor_clamp[batch[i].actor] = batch[i].clamp
             check(lib().ffsrl_batch_step_envs_lane(self.plan.handle, self.lanes.index(ln), ids.ctypes.data, n, 1, s))
             check(lib().ffsrl_remap_envs(ptr(m.allVisPoint), ptr(m.vertex), ptr(m.pointToVertex),
-                                         ptr(m.envVisPointStartT), ptr(ln.ids_d), n, m.numEnvs, s))
+                                         ptr(m.envMapStartT), ptr(ln.ids_d), n, m.numEnvs, s))
+            m.transformSimLaparoscopeMeshData(ln.stream, env_ids=ln.ids_d[:n])
             check(lib().ffsrl_bvh_refit_fused_envs(C.byref(self.bvh.desc), ptr(m.allVisPoint), ptr(m.allVisFace),
                                                    ptr(ln.ids_d), n, s))
             rd = self.renderer._desc(m)

@@ -223,7 +223,8 @@ int32_t ffsrl_step_model_noalloc(const ffsrl_model* model, const ffsrl_params* p
 int32_t ffsrl_remap(float* dst, const float* src, const int32_t* map, int32_t count, void* stream);
 
 /* remapAToBKernel for the listed envs only: the pairs of env e are map[2*point_start[e]
-   .. 2*point_start[e+1]) (device arrays). */
+   .. 2*point_start[e+1]) (device arrays; point_start is the prefix of each env's pair
+   count, its soft-mesh visual points -- rigid and instrument points have no pair). */
 int32_t ffsrl_remap_envs(float* dst, const float* src, const int32_t* map, const int32_t* point_start,
                          const int32_t* env_ids, int32_t n, int32_t num_envs, void* stream);
 

@@ -14,6 +14,11 @@ on the mesh generator giving the same floats on another machine.
               5 steps: positions and contact counts
   render.npz  the liver3 end state: BVH topologies, refit boxes and 16x16 colour/depth
               images from per-env cameras
+  scene.npz   three envs of one textured ellipsoid with a static rigid box under it and
+              the instrument's visual mesh (the multi-object layout): the instrument moved
+              by seeded actions, 3 steps, then visual points, the refit's face-shift
+              table, BVH topology and boxes, and 16x16 images in the texture, vertex-colour
+              and grayscale modes
 """
 
 from __future__ import annotations
@@ -27,6 +32,8 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parents[1]
 for p in (ROOT / "ff-srl_gb300", ROOT / "oracle"):
     sys.path.insert(0, str(p))
+
+import torch  # noqa: E402
 
 import oracle  # noqa: E402
 from ffsrl import SimBVH, WarpRaycastRendererDO  # noqa: E402
@@ -124,12 +131,90 @@ def make_render(pool, m, o) -> dict:
     return out
 
 
+SCENE_STEPS = 3
+SCENE_ENVS = 3
+SCENE_MODES = (1, 3, 0)
+INSTRUMENT_KEYS = ("points", "faces", "slot", "color")
+TEXTURE_KEYS = ("texture", "tex_coords", "tex_indices")
+RIGID_KEYS = ("vertex", "triangle", "color")
+
+
+def scene_inputs() -> tuple[dict, dict]:
+    """The scene's soft mesh (textured, one rigid box under it) and instrument mesh."""
+    base = mg.ellipsoid_for_tets(500, seed=31)
+    lo, hi = base["vertex"].min(axis=0), base["vertex"].max(axis=0)
+    box = mg.rigid_box([lo[0] - 2.0, lo[1] - 1.0, lo[2] - 2.0], [hi[0] + 2.0, lo[1] - 0.5, hi[2] + 2.0])
+    mesh = mg.with_rigids(mg.add_texture(base, size=16, seed=3), [box])
+    return mesh, mg.instrument_mesh()
+
+
+def pack_scene(mesh, inst) -> dict:
+    out = pack_meshes([mesh])
+    for key in TEXTURE_KEYS:
+        out[f"mesh0_{key}"] = np.asarray(mesh[key])
+    for key in RIGID_KEYS:
+        out[f"rigid0_{key}"] = np.asarray(mesh["rigids"][0][key])
+    for key in INSTRUMENT_KEYS:
+        out[f"instrument_{key}"] = np.asarray(inst[key])
+    return out
+
+
+def unpack_scene(z) -> tuple[dict, dict]:
+    mesh = unpack_meshes(z)[0]
+    for key in TEXTURE_KEYS:
+        mesh[key] = np.asarray(z[f"mesh0_{key}"])
+    mesh["rigids"] = [{key: np.asarray(z[f"rigid0_{key}"]) for key in RIGID_KEYS}]
+    return mesh, {key: np.asarray(z[f"instrument_{key}"]) for key in INSTRUMENT_KEYS}
+
+
+def scene_model(device, mesh, inst):
+    return sc.liver_model(device, SCENE_ENVS, meshes=[mesh] * SCENE_ENVS, instrumentMesh=inst)[0]
+
+
+def make_scene() -> dict:
+    mesh, inst = scene_inputs()
+    m = scene_model("cpu", mesh, inst)
+    # rest-state visual points with the instrument at its initial pose: the BVH build's input
+    vis0 = oracle.OracleSim(m).vis_points(oracle.OracleInstrument.from_model(m))
+    m.allVisPoint.copy_(torch.as_tensor(vis0))
+    bvh = SimBVH("cpu", m)
+    oi = oracle.OracleInstrument.from_model(m)
+    rng = np.random.default_rng(5)
+    for _ in range(4):
+        a = rng.uniform(-0.05, 0.05, size=(SCENE_ENVS, 5)).astype(np.float32)
+        a[:, 4] = 0.0  # the clamps stay closed
+        oi.apply_actions(a)
+    drag = grasp_flags(m)
+    o = oracle.OracleSim(m, {"active_drag_constraint": drag, "laparoscope_base": oi.base,
+                             "laparoscope_tip": oi.tip})
+    o.step(SCENE_STEPS)
+    vis = o.vis_points(oi)
+    src = oracle.reference_refit_source(SCENE_ENVS, m.numEnvMeshesVisFaces, m.numEnvRigidsVisFaces,
+                                        m.numEnvLaparoscopeVisFaces, m.envVisFaceStart[:-1])
+    assert np.array_equal(bvh.refitSource.numpy(), src)
+    lo, hi = oracle.refit(bvh, vis, m.host["allVisFace"])
+    r = renderer("cpu", m, [mesh] * SCENE_ENVS)
+    out = pack_scene(mesh, inst) | {
+        "steps": np.int32(SCENE_STEPS), "drag": drag, "xform": oi.xform.copy(), "height": oi.height.copy(),
+        "tool_base": oi.base.copy(), "tool_tip": oi.tip.copy(), "vertex": o.a["vertex"].copy(),
+        "vis_point_rest": vis0, "vis_point": vis, "refit_source": src, "aabb_min": lo, "aabb_max": hi,
+        "camera_pos": r.cameraPosT.cpu().numpy(), "camera_rot": r.cameraRotT.cpu().numpy()}
+    for mode in SCENE_MODES:
+        r.render_mode = mode
+        col, dep, _ = oracle.render(r, bvh, vis, aabb=(lo, hi))
+        out[f"color_mode{mode}"], out["depth"] = col, dep
+    for key in ("left_node", "first_tri_id", "tri_count", "level", "tri_id"):
+        out[f"topo0_{key}"] = np.asarray(bvh.topologies[0][key])
+    return out
+
+
 def main() -> None:
     np.savez_compressed(HERE / "beam.npz", **make_beam())
     fix, pool, m, o = make_liver()
     np.savez_compressed(HERE / "liver3.npz", **fix)
     np.savez_compressed(HERE / "render.npz", **make_render(pool, m, o))
-    for f in ("beam.npz", "liver3.npz", "render.npz"):
+    np.savez_compressed(HERE / "scene.npz", **make_scene())
+    for f in ("beam.npz", "liver3.npz", "render.npz", "scene.npz"):
         print(f, (HERE / f).stat().st_size, "bytes")
 
 
