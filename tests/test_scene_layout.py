@@ -197,10 +197,14 @@ def test_instrument_visual_follows_actions_and_steps(gpu, oracle_lib):
         o.apply_actions(a)
         integ.stepModel(m)  # ends with the visual update, as the reference's stepModel
     torch.cuda.synchronize()
+    # the kinematics agree to rounding (their sines and cosines are not bit-exact)...
+    X = m.laparoscopeXForm.cpu().numpy()
+    assert np.abs(X - o.xform).max() / max(np.abs(o.xform).max(), 1.0) < 1e-5
+    # ...and the visual points are exactly the oracle's transform of the library's transforms
     vis = m.allVisPoint.cpu().numpy()
     exp = vis.copy()
+    o.xform[:] = X
     o.visual(m.instrumentMesh["points"], m.instrumentMesh["slot"], exp, m.envInstrumentPointStart)
-    assert np.array_equal(m.laparoscopeXForm.cpu().numpy(), o.xform)
     assert np.array_equal(vis, exp)
     # the env-list form updates only the listed envs
     ids = torch.tensor([1, 3], dtype=torch.int32, device="cuda:0")
