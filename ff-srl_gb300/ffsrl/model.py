@@ -69,7 +69,13 @@ class SimModelDO:
                  toolRadius=(0.004, 0.002, 0.002), instrumentMesh=None):
         if hasattr(stage, "GetPrimAtPath"):
             raise _lib.FFSRLError(_lib.ERR_UNSUPPORTED,
-                                  "USD stages are not supported; pass ffsrl.meshgen mesh dicts (array scene)")
+                                  "USD stages are not supported; pass ffsrl.meshgen mesh dicts or an array scene file")
+        scenes = self._load_scenes(stage, int(numEnvs))
+        if scenes is not None:
+            stage = [sc_.mesh for sc_ in scenes]
+            if instrumentMesh is None:
+                ims = [sc_.instrument["mesh"] for sc_ in scenes if sc_.instrument and "mesh" in sc_.instrument]
+                instrumentMesh = ims[0] if ims else None
         meshes = stage if isinstance(stage, (list, tuple)) else [stage] * int(numEnvs)
         if len(meshes) != int(numEnvs):
             raise ValueError(f"got {len(meshes)} meshes for {numEnvs} environments")
@@ -122,6 +128,37 @@ class SimModelDO:
         self._concatenate(meshes, toolRadius)
         self._upload()
         self._batch = None
+        if scenes is not None and all(sc_.instrument is not None for sc_ in scenes):
+            ins = [sc_.instrument for sc_ in scenes]
+            base = np.concatenate([i["bases"] for i in ins]).astype(np.float32)
+            tip = np.concatenate([i["tips"] for i in ins]).astype(np.float32)
+            rad = np.concatenate([i["radii"] for i in ins]).astype(np.float32)
+            xf = np.stack([i["transforms"].reshape(-1) for i in ins]).astype(np.float32)
+            hts = np.stack([i["heights"] for i in ins]).astype(np.float32)
+            self.setTool(base, tip, rad)
+            self.setInstrument(xf, hts)
+            self.toolHost = {"base": base, "tip": tip, "radius": rad, "xform": xf, "height": hts}
+            self.setEffectorInitialPosition()
+
+    @staticmethod
+    def _load_scenes(stage, numEnvs):
+        """Array scene files (``ffsrl.scene``) for ``stage`` given as a path or a per-env list
+        holding paths; None when the stage is mesh dicts only.  A file shared by several
+        envs is read once, so they share its mesh."""
+        from . import scene as scene_io
+        items = [stage] * numEnvs if scene_io.is_scene_path(stage) else stage
+        if not isinstance(items, (list, tuple)) or not any(scene_io.is_scene_path(it) for it in items):
+            return None
+        cache, out = {}, []
+        for it in items:
+            if scene_io.is_scene_path(it):
+                key = str(it)
+                if key not in cache:
+                    cache[key] = scene_io.read_scene(key)
+                out.append(cache[key])
+            else:
+                out.append(scene_io.Scene(mesh=it))
+        return out
 
     # ------------------------------------------------------------------ build
     @staticmethod

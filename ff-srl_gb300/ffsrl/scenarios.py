@@ -121,6 +121,19 @@ def top_surface_point(mesh) -> np.ndarray:
     return v[np.argmax(v[:, 1])].astype(np.float64)
 
 
+def write_liver_scene(path, mesh, rigids=(), dip: float = 0.35, instrument_visual: bool = True) -> None:
+    """An array scene file (``ffsrl.scene``) of one soft body with the synthetic instrument
+    placed as ``place_instruments`` places it (effector ``dip`` below the highest surface
+    point) and its visual mesh."""
+    from . import scene as scene_io
+    pt = top_surface_point(mesh) - np.array([0.0, dip, 0.0])
+    xf, heights, b, t, r = instrument_xforms(pt[None])
+    inst = {"transforms": xf.reshape(7, 16), "heights": heights[0], "radii": r, "bases": b, "tips": t}
+    if instrument_visual:
+        inst.update(mg.instrument_mesh())
+    scene_io.write_scene(path, [mesh], rigids=rigids, instrument=inst)
+
+
 def place_instruments(model: SimModelDO, meshes: list, dip: float = 0.35) -> np.ndarray:
     """Kinematic instrument of env e with its effector ``dip`` cm below mesh e's highest
     surface point, pointing down, clamps closed (their tips then touch the surface);
@@ -151,22 +164,29 @@ def beam_model(device, num_envs=1, neo=False, xpbd=False, mesh=None, **kw) -> tu
 
 
 def liver_model(device, num_envs, meshes=None, E=NH_E, nu=NH_NU, substeps=8, iterations=10, grasp=True,
-                collide=True, instrument_visual=True, **kw) -> tuple[SimModelDO, list]:
+                collide=True, instrument_visual=True, scene=None, **kw) -> tuple[SimModelDO, list]:
     """Config 1 (meshes=None: the 12/8/6 cm ellipsoid in every env) or a given list
     of meshes (configs 2/4): Neo-Hookean + volume + distance, grasp and contact.  With
     ``instrument_visual`` each env also renders its instrument (``meshgen.instrument_mesh``
-    with the dimensions of ``instrument_xforms``)."""
-    if meshes is None:
-        meshes = [mg.ellipsoid()] * num_envs
+    with the dimensions of ``instrument_xforms``).  ``scene``: an array scene file
+    (``write_liver_scene``) in every env instead, its instrument included."""
+    stage = meshes
+    if scene is not None:
+        from . import scene as scene_io
+        meshes = [scene_io.read_scene(scene).mesh] * num_envs
+        stage = scene
+    elif meshes is None:
+        meshes = stage = [mg.ellipsoid()] * num_envs
     mu, lam = lame(E, nu)
     flags = L.VOLUME | L.DISTANCE | L.NEOHOOKEAN | L.DRAG | (L.COLLIDE if collide else 0)
     kw.setdefault("environmentGravity", mg.gravity_force(meshes[0]))
-    if instrument_visual:
+    if instrument_visual and scene is None:
         kw.setdefault("instrumentMesh", mg.instrument_mesh())
-    m = SimModelDO(meshes, num_envs, device, simSubsteps=substeps, simFrameRate=60, simConstraintsSteps=iterations,
+    m = SimModelDO(stage, num_envs, device, simSubsteps=substeps, simFrameRate=60, simConstraintsSteps=iterations,
                    environmentGroundLevel=-100.0, constraints=flags, globalVolumeCompliance=1.0 / lam,
                    globalDeviatoricCompliance=1.0 / mu, globalLaparoscopeDragLookupRadius=0.5, **kw)
-    place_instruments(m, meshes)
+    if scene is None:
+        place_instruments(m, meshes)
     return m, meshes
 
 

@@ -81,3 +81,26 @@ def test_validate_rejects_bad_child(built_lib):
     t["left_node"][0] = t["num_nodes"] - 1
     with pytest.raises(ValueError):
         SimBVH.validate(t, len(faces))
+
+
+def test_npz_reference_layout(built_lib, tmp_path):
+    # bvh.py:165-197: arr_0 triId, arr_1/arr_2 the boxes of the first env [numNodes, 3],
+    # arr_3..arr_6 leftNode, firstTriId, triCount, level -- a file written that way loads
+    mesh = mg.ellipsoid_for_tets(500, seed=4)
+    m = SimModelDO(mesh, 2, "cpu")
+    pts, faces = _surface(mesh)
+    t = build_topology(pts, faces)
+    np.savez(tmp_path / "ref.npz", t["tri_id"], t["aabb_min"], t["aabb_max"], t["left_node"], t["first_tri_id"],
+             t["tri_count"], t["level"])
+    b = SimBVH("cpu", m, load=True, path=str(tmp_path / "ref.npz"))
+    for k in ("left_node", "first_tri_id", "tri_count", "level", "tri_id"):
+        assert np.array_equal(b.topologies[0][k], t[k]), k
+    assert b.numNodes == t["num_nodes"] and b.maxLevel == t["max_level"]
+    b.saveBVH(str(tmp_path / "out.npz"))
+    z = np.load(tmp_path / "out.npz")
+    assert z.files == [f"arr_{k}" for k in range(7)]
+    assert z["arr_1"].shape == (t["num_nodes"], 3) and np.array_equal(z["arr_3"], t["left_node"])
+    # a file with fewer topologies than the model's distinct meshes is refused
+    two = SimModelDO([mesh, mg.ellipsoid_for_tets(700, seed=5)], 2, "cpu")
+    with pytest.raises(ValueError):
+        SimBVH("cpu", two, load=True, path=str(tmp_path / "ref.npz"))
