@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=5.0)
+    ap.add_argument("--no-graph", action="store_true", help="launch the env-step eagerly instead of a CUDA graph")
     return ap.parse_args()
 
 
@@ -239,12 +240,23 @@ def main():
         m.graspNearest(grasp_all, radius=GRASP_RADIUS)
         episode["steps"] = 1
 
-    def step(k):
-        episode_tick()
-        m.applyCartesianActionsInWorkspace(walk[k])
+    # one env-step (instrument move, batched step, visual points, refit, ray-cast) as a
+    # CUDA graph replayed every step; the action is copied into the buffer it reads
+    act_s = torch.zeros((envs, 3), dtype=torch.float32, device=device)
+
+    def core():
+        m.applyCartesianActionsInWorkspace(act_s)
         integ.stepModel(m, 1)
         bvh.refitBVH()
         r.renderNew(bvh, m)
+
+    from ffsrl.graphs import Graph
+    core_step = Graph(core, prepare=lambda: integ.plan(m)) if not args.no_graph else core
+
+    def step(k):
+        episode_tick()
+        act_s.copy_(walk[k])
+        core_step()
 
     def barrier():
         torch.cuda.synchronize()
@@ -307,10 +319,8 @@ def main():
         act_h[:, :3] = walk_h[k % len(walk_h)]
         act_h[:, 3] = 1.0
         act_d.copy_(act_h, non_blocking=True)
-        m.applyCartesianActionsInWorkspace(act_d[:, :3].contiguous())
-        integ.stepModel(m, 1)
-        bvh.refitBVH()
-        r.renderNew(bvh, m)
+        act_s.copy_(act_d[:, :3])
+        core_step()
         res_d[:, :3] = m.laparoscopeTip[3::4]
         res_d[:, 3] = m.laparoscopeInCollision.float()
         res_h.copy_(res_d, non_blocking=True)
@@ -375,7 +385,7 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": "env-steps/s", "n_gpus": world, "steps": K,
                 "warmup": W, "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded meshes and random-walk actions)",
-                "config": config(envs, world),
+                "config": config(envs, world), "cuda_graph": not args.no_graph,
                 "latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99)),
                                "what": "full-batch step latency (all envs), per timed step"},
                 "e2e": {"value": e2e, "unit": "env-steps/s", "h2d_bytes_per_step": envs * 16,

@@ -78,6 +78,11 @@ __device__ __forceinline__ float rsqrt_(float x) {
 }
 __device__ __forceinline__ double rsqrt_(double x) { return 1.0 / sqrt(x); }
 
+// Brings the line holding p into this SM's L1 (PTX prefetch.global.L1); the tet loop
+// requests the records its thread reads one loop trip later, so that read hits L1
+// instead of waiting for L2
+__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+
 // per-precision storage: predicted position + inverse mass, accumulator word
 template <class R> struct Store;
 struct Fixed { float scale, inv, bound; };
@@ -300,7 +305,7 @@ template <class R> struct ToolShared {
 template <class R, int BLOCK, int MODE>
 __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_batched(const Dev<R> D, const int* __restrict__ work, int nwork,
                                                    int* counter, int nsteps, unsigned char* scratch,
-                                                   long long scratch_stride, int max_nv) {
+                                                   long long scratch_stride, int max_nv, int prefetch) {
     typedef Store<R> S;
     typedef typename S::P P;
     typedef typename S::A A;
@@ -417,6 +422,13 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
                     if (fl & (FFSRL_VOLUME | FFSRL_VOLUME_XPBD | FFSRL_NEOHOOKEAN)) {
                         for (int t = tid; t < nt; t += BLOCK) {
                             const int gt = E.t0 + t;
+                            if (prefetch && t + BLOCK < nt) {  // this thread's next record
+                                const int gn = gt + BLOCK;
+                                prefetch_l1(D.tet_idx + gn);
+                                prefetch_l1(D.tet_va + gn);
+                                if (fl & FFSRL_NEOHOOKEAN) { prefetch_l1(D.nh0 + gn); prefetch_l1(D.nh1 + gn); }
+                                if (D.fold) prefetch_l1(D.tet_ed + gn);
+                            }
                             const uint2 ix = __ldg(D.tet_idx + gt);
                             const int ia = ix.x & 0xffff, ib = ix.x >> 16, ic = ix.y & 0xffff, id = ix.y >> 16;
                             const P PA = xp[ia], PB = xp[ib], PC = xp[ic], PD = xp[id];
@@ -667,8 +679,8 @@ template <class R> size_t scratch_bytes(int mode, int max_nv) {
     return (P + 3 * A + 4) * (size_t)max_nv;
 }
 
-typedef void (*kern_f)(const Dev<float>, const int*, int, int*, int, unsigned char*, long long, int);
-typedef void (*kern_d)(const Dev<double>, const int*, int, int*, int, unsigned char*, long long, int);
+typedef void (*kern_f)(const Dev<float>, const int*, int, int*, int, unsigned char*, long long, int, int);
+typedef void (*kern_d)(const Dev<double>, const int*, int, int*, int, unsigned char*, long long, int, int);
 
 kern_f pick_f(int block, int mode) {
 #define PK(B, M) if (block == B && mode == M) return k_batched<float, B, M>;
@@ -712,6 +724,7 @@ struct ffsrl_batch {
     // classes
     struct Class {
         int mode, block, max_nv, grid, members;
+        int prefetch = 0;  // L1 prefetch of the next tet record (autotuned)
         size_t smem, scratch_stride, scratch_offset;
         int work_offset, work_count;
     };
@@ -812,7 +825,7 @@ template <> int32_t launch_class<float>(ffsrl_batch* b, const ffsrl_batch::Class
     int grid = std::min(c.grid, nwork);
     if (grid <= 0) return FFSRL_OK;
     k<<<grid, c.block, c.smem, s>>>(D, work, nwork, counter, nsteps, scratch + c.scratch_offset,
-                                    (long long)c.scratch_stride, c.max_nv);
+                                    (long long)c.scratch_stride, c.max_nv, c.prefetch);
     FFSRL_LAUNCH_CHECK("ffsrl_batch: step kernel");
     return FFSRL_OK;
 }
@@ -839,7 +852,7 @@ template <> int32_t launch_class<double>(ffsrl_batch* b, const ffsrl_batch::Clas
     int grid = std::min(c.grid, nwork);
     if (grid <= 0) return FFSRL_OK;
     k<<<grid, c.block, c.smem, s>>>(D, work, nwork, counter, nsteps, scratch + c.scratch_offset,
-                                    (long long)c.scratch_stride, c.max_nv);
+                                    (long long)c.scratch_stride, c.max_nv, c.prefetch);
     FFSRL_LAUNCH_CHECK("ffsrl_batch: float64 step kernel");
     return FFSRL_OK;
 }
@@ -1628,6 +1641,14 @@ extern "C" int32_t ffsrl_batch_class_envs(const ffsrl_batch* b, int32_t cls, int
         return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_class_envs");
     const auto& c = b->classes[cls];
     for (int i = 0; i < c.work_count; ++i) env_ids[i] = b->work_host[c.work_offset + i];
+    return FFSRL_OK;
+}
+
+extern "C" int32_t ffsrl_batch_set_class_prefetch(ffsrl_batch* b, int32_t cls, int32_t on) {
+    if (!b || cls < 0 || cls >= (int)b->classes.size() || (on != 0 && on != 1))
+        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_set_class_prefetch");
+    FFSRL_CUDA_TRY(cudaDeviceSynchronize());
+    b->classes[cls].prefetch = on;
     return FFSRL_OK;
 }
 

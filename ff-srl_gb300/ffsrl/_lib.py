@@ -156,6 +156,7 @@ def lib() -> C.CDLL:
         "ffsrl_batch_class_info": ([P, I32, C.POINTER(I32), C.POINTER(I32), C.POINTER(I32), C.POINTER(I32)], I32),
         "ffsrl_batch_class_envs": ([P, I32, P], I32),
         "ffsrl_batch_set_class_block": ([P, I32, I32], I32),
+        "ffsrl_batch_set_class_prefetch": ([P, I32, I32], I32),
     }
     for name, (args, ret) in sig.items():
         f = getattr(L, name)

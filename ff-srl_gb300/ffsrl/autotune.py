@@ -2,7 +2,8 @@
 
 The batched step runs one launch per size class (environments grouped by vertex count).
 For each class this times the class's environments for one step at every block size
-that has a kernel instantiation and fits on an SM, keeps the fastest, and records the
+that has a kernel instantiation and fits on an SM, with and without the L1 prefetch of
+the tet records, keeps the fastest, and records the
 choice in a JSON cache keyed by the device and the class's shape, so later plans with
 the same classes skip the timing.  The model's state is saved before and restored after
 the timing runs.
@@ -22,6 +23,7 @@ import torch
 from ._lib import FFSRLError, check, lib
 
 CANDIDATES = (128, 256, 512, 1024)
+PREFETCH = (0, 1)  # L1 prefetch of each thread's next tet record off / on
 
 
 def cache_path() -> Path:
@@ -45,7 +47,7 @@ def _key(plan, cls) -> str:
     m = plan.model
     props = torch.cuda.get_device_properties(m.device)
     tets = int(sum(int(m.envTetStart[e + 1] - m.envTetStart[e]) for e in cls["envs"]))
-    sig = f"{props.name}|{props.multi_processor_count}|{m.constraintFlags}|{m.simSubsteps}|{m.simConstraints}|" \
+    sig = f"v2|{props.name}|{props.multi_processor_count}|{m.constraintFlags}|{m.simSubsteps}|{m.simConstraints}|" \
           f"{cls['mode']}|{cls['max_nv']}|{len(cls['envs'])}|{tets}|{plan.precision}"
     return hashlib.sha1(sig.encode()).hexdigest()[:16]
 
@@ -78,23 +80,30 @@ def autotune(plan, reps: int = 2, use_cache: bool = True, verbose: bool = False)
         for ci, cls in enumerate(_classes(plan)):
             key = _key(plan, cls)
             if key in cache:
-                check(lib().ffsrl_batch_set_class_block(plan.handle, ci, int(cache[key]["block"])))
-                result.append({"class": ci, "block": cache[key]["block"], "ms": cache[key]["ms"], "cached": True})
+                c = cache[key]
+                check(lib().ffsrl_batch_set_class_block(plan.handle, ci, int(c["block"])))
+                check(lib().ffsrl_batch_set_class_prefetch(plan.handle, ci, int(c.get("prefetch", 0))))
+                result.append({"class": ci, "block": c["block"], "prefetch": c.get("prefetch", 0), "ms": c["ms"],
+                               "cached": True})
                 continue
             best = None
             for b in CANDIDATES:
                 if lib().ffsrl_batch_set_class_block(plan.handle, ci, b) != 0:
                     continue
-                ms = _time(plan, cls["envs"], reps)
-                if verbose:
-                    print(f"autotune class {ci} (max_nv {cls['max_nv']}, {len(cls['envs'])} envs): block {b} {ms:.3f} ms")
-                if best is None or ms < best[1]:
-                    best = (b, ms)
+                for pf in PREFETCH:
+                    check(lib().ffsrl_batch_set_class_prefetch(plan.handle, ci, pf))
+                    ms = _time(plan, cls["envs"], reps)
+                    if verbose:
+                        print(f"autotune class {ci} (max_nv {cls['max_nv']}, {len(cls['envs'])} envs): "
+                              f"block {b} prefetch {pf} {ms:.3f} ms")
+                    if best is None or ms < best[2]:
+                        best = (b, pf, ms)
             if best is None:
                 raise FFSRLError(6, f"autotune: no block size fits class {ci}")
             check(lib().ffsrl_batch_set_class_block(plan.handle, ci, best[0]))
-            cache[key] = {"block": best[0], "ms": best[1]}
-            result.append({"class": ci, "block": best[0], "ms": best[1], "cached": False})
+            check(lib().ffsrl_batch_set_class_prefetch(plan.handle, ci, best[1]))
+            cache[key] = {"block": best[0], "prefetch": best[1], "ms": best[2]}
+            result.append({"class": ci, "block": best[0], "prefetch": best[1], "ms": best[2], "cached": False})
     finally:
         for t, s in zip((m.vertex, m.velocity, m.predictedVertex, m.laparoscopeInCollision, m.tetrahedronLambda,
                          m.edgeLambda), saved):

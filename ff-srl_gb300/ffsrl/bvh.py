@@ -13,6 +13,7 @@ reference's one launch per tree level (``refitBVHLoop``, ``bvh.py:419-440``).
 
 from __future__ import annotations
 
+import contextlib
 import ctypes as C
 
 import numpy as np
@@ -231,8 +232,18 @@ class SimBVH:
 
     # ------------------------------------------------------------------ refit
     def refitBVH(self, useGraph: bool = False, fused: bool = True, stream=None) -> None:
+        """Boxes from the current visual points (bvh.py:442-451).  ``useGraph`` captures the
+        refit into a CUDA graph on the first call and replays it afterwards, as the
+        reference's ``refitGraph``."""
         m = self.simModel
         m.require_cuda()
+        if useGraph:
+            from .graphs import Graph
+            if self.refitGraph is None or self.refitGraph[0] != fused:
+                self.refitGraph = (fused, Graph(lambda: self.refitBVH(fused=fused)))
+            with torch.cuda.stream(stream) if stream is not None else contextlib.nullcontext():
+                self.refitGraph[1]()
+            return
         s = _lib.stream_handle(stream)
         fn = lib().ffsrl_bvh_refit_fused if fused else lib().ffsrl_bvh_refit_levels
         check(fn(C.byref(self.desc), ptr(m.allVisPoint), ptr(m.allVisFace), s))

@@ -1,0 +1,49 @@
+"""CUDA graphs of the library's calls (the reference's ``wp.capture_begin`` /
+``wp.capture_launch``: ``bvh.py:442-451``, ``render.py:1108-1112``,
+``tests/testLiverRetraction.py:77-85``).
+
+``Graph(fn)`` records every launch ``fn`` makes on the current stream into one CUDA graph
+on its first call and replays that graph on every later call, as the reference does.
+The captured launches keep the device pointers and the scalar arguments they were
+recorded with, so the arrays ``fn`` uses must stay the same tensors (the model's arrays
+do) and host-side choices inside ``fn`` (a render mode, a step count) are fixed at
+capture; make a new ``Graph`` after changing them.  Everything the library launches goes
+to the current stream, which is the capture stream during the capture, so its calls
+record with no change; anything that must run before the first capture (plan building,
+autotuning, kernel attributes) is done by ``prepare``.
+"""
+
+from __future__ import annotations
+
+from typing import Callable
+
+import torch
+
+
+class Graph:
+    def __init__(self, fn: Callable[[], None], prepare: Callable[[], None] | None = None):
+        self.fn = fn
+        self.prepare = prepare
+        self.graph = None
+
+    def capture(self) -> None:
+        if self.prepare is not None:
+            self.prepare()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side), torch.cuda.graph(g, stream=side):
+            self.fn()
+        torch.cuda.current_stream().wait_stream(side)
+        self.graph = g
+
+    def __call__(self) -> None:
+        """Capture on the first call (which then replays once, so the call has its effect),
+        replay afterwards; the replay is ordered on the current stream."""
+        if self.graph is None:
+            self.capture()
+        self.graph.replay()
+
+    def reset(self) -> None:
+        self.graph = None

@@ -15,6 +15,7 @@ Two GPU forms with the same semantics:
 
 from __future__ import annotations
 
+import contextlib
 import ctypes as C
 
 import numpy as np
@@ -95,6 +96,7 @@ class SimIntegratorDO:
         self.autotune = bool(autotune)
         self.tuning = None
         self._plans = {}
+        self._graphs = {}
 
     def plan(self, simModel) -> BatchPlan:
         key = id(simModel)
@@ -107,8 +109,26 @@ class SimIntegratorDO:
                 self.tuning = autotune(p)
         return p
 
-    def stepModel(self, simModel, steps: int = 1, stream=None) -> None:
+    def stepModel(self, simModel, steps: int = 1, stream=None, useGraph: bool = False) -> None:
+        """integrator.py:1640-1744: ``steps`` env-steps, then the visual points.  With
+        ``useGraph`` the launches are captured into a CUDA graph on the first call and the
+        graph is replayed afterwards (the reference RL loop's ``wp.capture_launch``,
+        ``tests/testLiverRetraction.py:77-85``); one graph per model and step count."""
         simModel.require_cuda()
+        if useGraph:
+            from .graphs import Graph
+            key = (id(simModel), int(steps))
+            g = self._graphs.get(key)
+            if g is None or g[0] is not simModel:
+                prep = (lambda: self.plan(simModel)) if self.batched else None
+                g = (simModel, Graph(lambda: self._step(simModel, steps, None), prep))
+                self._graphs[key] = g
+            with torch.cuda.stream(stream) if stream is not None else contextlib.nullcontext():
+                g[1]()
+            return
+        self._step(simModel, steps, stream)
+
+    def _step(self, simModel, steps, stream) -> None:
         if self.batched:
             self.plan(simModel).step(steps, stream)
         else:
@@ -118,7 +138,7 @@ class SimIntegratorDO:
             for _ in range(int(steps)):
                 check(lib().ffsrl_step_model(C.byref(m), C.byref(prm), s))
         simModel.transformSimMeshData(stream)
-        simModel.transformSimLaparoscopeMeshData()
+        simModel.transformSimLaparoscopeMeshData(stream)
 
     def envStatus(self, simModel) -> np.ndarray:
         """Per-env status of the last batched step (0 ok, 7 non-finite state)."""

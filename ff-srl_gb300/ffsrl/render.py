@@ -17,6 +17,7 @@ Cameras: the reference shares one camera (``camera.pos[0]``, ``render.py:309``);
 
 from __future__ import annotations
 
+import contextlib
 import ctypes as C
 import math
 import warnings
@@ -159,8 +160,22 @@ class WarpRaycastRendererDO:
         fn = lib().ffsrl_render_fused if self.fused else lib().ffsrl_render_reference
         check(fn(C.byref(r), C.byref(simBVH.desc), _lib.stream_handle(stream)))
 
-    def renderNew(self, simBVH, simModel, stream=None) -> torch.Tensor:
-        self.renderFunctionNew(simBVH, stream)
+    def renderNew(self, simBVH, simModel, stream=None, useGraph: bool = False) -> torch.Tensor:
+        """Images [N, R, R, 3] (render.py:1099-1113).  ``useGraph`` captures the render
+        into a CUDA graph on the first call and replays it afterwards, as the reference's
+        ``renderGraph``; a new graph is captured when the BVH, shading mode, path or camera
+        tensors change."""
+        if useGraph:
+            from .graphs import Graph
+            key = (id(simBVH), self.render_mode, self.fused, self.cameraPosT.data_ptr(), self.cameraRotT.data_ptr(),
+                   self.lightDir.data_ptr())
+            if self.renderGraph is None or self.renderGraph[0] != key:
+                self.renderGraph = (key, Graph(lambda: self.renderFunctionNew(simBVH),
+                                               prepare=lambda: self._desc(self.simModel)))
+            with torch.cuda.stream(stream) if stream is not None else contextlib.nullcontext():
+                self.renderGraph[1]()
+        else:
+            self.renderFunctionNew(simBVH, stream)
         return self.pixels.view(self.numEnvs, self.height, self.width, 3)
 
     def depthImages(self) -> torch.Tensor:

@@ -252,3 +252,23 @@ def test_reset_fixed_model_subset_and_all(gpu):
     assert float(m.velocity[s1].abs().max()) == 0.0
     m.resetFixedModel(range(3))
     assert torch.equal(m.vertex, m.initialVertex)
+
+
+def test_prefetch_and_block_size_do_not_change_results(gpu):
+    # the autotuner's choices (block size, L1 prefetch of the tet records) change the
+    # schedule only: the fixed-point sums are exact, so every choice gives the same bits
+    meshes, _ = sc.mixed_meshes(6, pool_size=3, seed=31, t_lo=400, t_hi=3000)
+    out = []
+    for block, pf in ((256, 0), (256, 1), (512, 1), (1024, 1)):
+        m, _ = sc.liver_model("cuda:0", 6, meshes=meshes)
+        m.graspNearest(torch.ones(6, dtype=torch.int32, device="cuda:0"))
+        integ = SimIntegratorDO("cuda:0")
+        plan = integ.plan(m)
+        for c in range(plan.info()["num_classes"]):
+            if L.lib().ffsrl_batch_set_class_block(plan.handle, c, block) == 0:
+                L.check(L.lib().ffsrl_batch_set_class_prefetch(plan.handle, c, pf))
+        integ.stepModel(m, 3)
+        torch.cuda.synchronize()
+        out.append(m.vertex.cpu().numpy())
+    for o in out[1:]:
+        assert np.array_equal(o, out[0])
