@@ -1,6 +1,7 @@
 """CUDA graphs of the step, the refit, the render and a whole RL step (the reference's
 ``wp.capture_begin`` / ``wp.capture_launch``: bvh.py:442-451, render.py:1108-1112,
-tests/testLiverRetraction.py:77-85): replays give the eager results bit for bit."""
+tests/testLiverRetraction.py:77-85): replays give the eager results bit for bit (the
+batched step; the reference-shaped step's float atomics differ run to run)."""
 
 import numpy as np
 import pytest
@@ -41,7 +42,10 @@ def test_graphs_replay_the_eager_calls(gpu, batched):
         torch.cuda.synchronize()
         out.append(_state(m, bvh, r))
     for a, b in zip(*out):
-        assert np.array_equal(a, b)
+        if batched:  # exact fixed-point sums: the same bits
+            assert np.array_equal(a, b)
+        else:  # the reference-shaped step sums with float atomics, in a different order each run
+            assert np.abs(a - b).max() <= 1e-3 * max(np.abs(a).max(), 1.0)
 
 
 @pytest.mark.gpu
