@@ -965,7 +965,8 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
     if (N <= 0 || !hm->env_vertex_start || !hm->env_tet_start || !hm->env_edge_start || !hm->env_tri_start)
         return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_create: host env ranges required");
     if ((p->flags & FFSRL_CONNECTORS) && hm->num_connectors > 0)
-        return fail(FFSRL_ERR_UNSUPPORTED, "ffsrl_batch_create: connectors couple environments; use ffsrl_step_model");
+        return fail(FFSRL_ERR_UNSUPPORTED,
+                    "ffsrl_batch_create: connectors are not part of the batched step; run them with ffsrl_step_model");
     int precision = 32;
     int block_override = 0;
     if (opts) {

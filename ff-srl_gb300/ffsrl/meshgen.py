@@ -395,3 +395,33 @@ def with_rigids(mesh: dict, rigids) -> dict:
     out = dict(mesh)
     out["rigids"] = list(rigids)
     return out
+
+
+def connect_meshes(a: dict, b: dict, radius: float, kind: str = "centroid") -> dict:
+    """One soft body of two meshes with connectors (the reference's ``SimConnectorDO``,
+    ``modelDO.py:723-770``): every surface vertex of ``a`` within ``radius`` of a surface
+    triangle centroid of ``b`` is held to the nearest such centroid (barycentric
+    (1/3, 1/3, 1/3)), its rest distance the current one.  Ids are those of the merged
+    body (``a``'s vertices first)."""
+    from .scene import merge_meshes
+    out = dict(merge_meshes([a, b]))
+    nva = len(a["vertex"])
+    pa = np.asarray(a["vertex"], dtype=np.float64)
+    pb = np.asarray(b["vertex"], dtype=np.float64)
+    tri = np.asarray(b["triangle"], dtype=np.int64).reshape(-1, 3)
+    cen = pb[tri].mean(axis=1)
+    surf = np.unique(np.asarray(a["point_to_vertex"])[:, 1])
+    vid, tid, dist = [], [], []
+    for v in surf:
+        d = np.linalg.norm(cen - pa[v], axis=1)
+        k = int(np.argmin(d))
+        if d[k] < radius:
+            vid.append(int(v))
+            tid.append(tri[k] + nva)
+            dist.append(float(d[k]))
+    c = len(vid)
+    out["connector_vertex_id"] = np.asarray(vid, dtype=np.int32)
+    out["connector_triangle_id"] = np.asarray(tid, dtype=np.int32).reshape(c, 3)
+    out["connector_tri_bar"] = np.full((c, 3), 1.0 / 3.0, dtype=np.float32)
+    out["connector_rest_dist"] = np.asarray(dist, dtype=np.float32)
+    return out

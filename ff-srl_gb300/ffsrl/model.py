@@ -261,6 +261,7 @@ class SimModelDO:
         # grasp candidates: the surface (visual) vertices of each env's soft mesh
         self.graspCandStart = self.envMapStart.copy()
         h["graspCand"] = h["pointToVertex"][1::2].copy()
+        self._concatenate_connectors(h, meshes, nv, vo)
         self._concatenate_textures(h, rigids, nvf, ng, Lf)
         self.host = h
 
@@ -274,7 +275,7 @@ class SimModelDO:
         self.numAllVisFaces = int(self.envVisFaceStart[-1])
         self.numRigidVisPoints, self.numRigidVisFaces = int(nq.sum()), int(ng.sum())
         self.numLaparoscopeVisPoints, self.numLaparoscopeVisFaces = N * Lp, N * Lf
-        self.simConnectors = 0
+        self.simConnectors = int(len(h["connectorVertexId"]))
         # per-env sizes (the reference assumes identical envs; these hold env 0's)
         self.environmentNumVertices = int(nv[0])
         self.numEnvAllVertices = int(nv[0])
@@ -296,6 +297,34 @@ class SimModelDO:
         base[:, 1] = 10.1
         rad = np.tile(np.array([r[0], r[1], r[2], 0.0], dtype=np.float32), N)
         self.toolHost = {"base": base, "tip": tip, "radius": rad}
+
+    @staticmethod
+    def _concatenate_connectors(h, meshes, nv, vo):
+        """Connectors (``SimConnectorDO``, ``modelDO.py:723-770, 977-1015``): a point of one body
+        held at a rest distance from a barycentric point of a triangle of another body of
+        the same env.  A mesh dict lists them in its own vertex ids: ``connector_vertex_id``
+        [C], ``connector_triangle_id`` [C, 3], ``connector_tri_bar`` [C, 3],
+        ``connector_rest_dist`` [C]; here they become global ids, env after env."""
+        cv, ct, cb, cr = [], [], [], []
+        for e, m in enumerate(meshes):
+            if m.get("connector_vertex_id") is None:
+                continue
+            v = np.asarray(m["connector_vertex_id"], dtype=np.int64).reshape(-1)
+            t = np.asarray(m["connector_triangle_id"], dtype=np.int64).reshape(-1, 3)
+            b = np.asarray(m["connector_tri_bar"], dtype=np.float32).reshape(-1, 3)
+            r = np.asarray(m["connector_rest_dist"], dtype=np.float32).reshape(-1)
+            if not (len(v) == len(t) == len(b) == len(r)):
+                raise ValueError("connectors: vertex ids, triangles, barycentrics and rest distances differ in count")
+            if len(v) and (min(v.min(), t.min()) < 0 or max(v.max(), t.max()) >= nv[e]):
+                raise ValueError("connectors: vertex id out of range")
+            cv.append(v + vo[e])
+            ct.append((t + vo[e]).reshape(-1))
+            cb.append(b)
+            cr.append(r)
+        h["connectorVertexId"] = _cat(cv, np.int32)
+        h["connectorTriangleId"] = _cat(ct, np.int32)
+        h["connectorTriBar"] = _cat(cb, np.float32).reshape(-1, 3)
+        h["connectorRestDist"] = _cat(cr, np.float32)
 
     @staticmethod
     def _texture_entry(obj, num_faces, tables):
@@ -442,10 +471,10 @@ class SimModelDO:
         self.envEdgeStartT = T(self.envEdgeStart, **i32)
         self.envTriStartT = T(self.envTriStart, **i32)
         self.envVisPointStartT = T(self.envVisPointStart, **i32)
-        self.connectorVertexId = torch.zeros(0, **i32)
-        self.connectorTriangleId = torch.zeros(0, **i32)
-        self.connectorTriBar = torch.zeros((0, 3), **f32)
-        self.connectorRestDist = torch.zeros(0, **f32)
+        self.connectorVertexId = T(h["connectorVertexId"], **i32)
+        self.connectorTriangleId = T(h["connectorTriangleId"], **i32)
+        self.connectorTriBar = T(h["connectorTriBar"], **f32)
+        self.connectorRestDist = T(h["connectorRestDist"], **f32)
 
     # ------------------------------------------------------------ descriptors
     def require_cuda(self) -> None:

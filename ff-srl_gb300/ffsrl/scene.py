@@ -23,6 +23,9 @@ material (either prim)         ``material:diffuse_texture`` [S, S, 3] in [0, 1] 
                                reference holds an image path), ``primvars:st``,
                                ``primvars:st:indices`` (default: the faces,
                                ``modelDO.py:636-640``)
+simConnector prim              ``simConnector`` (1), ``pointBody`` / ``triBody`` (the
+                               bodies' prim paths), ``pointId``, ``triIds``, ``triBar``,
+                               ``restDist`` (``modelDO.py:751-770``)
 simLaparoscope prim            ``simLaparoscope`` (1), ``laparoscope:transforms`` [7, 16]
                                (the reference's storage), ``laparoscope:heights`` [4],
                                ``laparoscope:radii`` [4], ``laparoscope:bases`` /
@@ -62,6 +65,9 @@ MESH_ATTRS = (("vertex", "extMesh:vertex"), ("tetrahedron", "extMesh:elem"), ("e
               ("vis_point_color", "primvars:displayColor"), ("point_to_vertex", "mapping:pointToVertex"))
 EXTRA_ATTRS = (("tetrahedron_rest_volume_signed", "ffsrl:tetrahedronRestVolumeSigned"),
                ("rest_vertex", "ffsrl:restVertex"), ("fixed", "ffsrl:fixed"))
+# connector prim (modelDO.py:751-770): ids local to its bodies
+CONNECTOR_ATTRS = (("connector_vertex_id", "pointId"), ("connector_triangle_id", "triIds"),
+                   ("connector_tri_bar", "triBar"), ("connector_rest_dist", "restDist"))
 TEXTURE_ATTRS = (("texture", "material:diffuse_texture"), ("tex_coords", "primvars:st"),
                  ("tex_indices", "primvars:st:indices"))
 SHAPES = {"vertex": (-1, 3), "tetrahedron": (-1, 4), "edge": (-1, 2), "triangle": (-1, 3), "vis_face": (-1, 3),
@@ -127,6 +133,13 @@ def write_scene(path, meshes, rigids=(), instrument=None, params=None, names=Non
         for p, v in (params or {}).items():
             out[f"{prim}.param:{p}"] = np.float64(v)
         _put_texture(out, prim, m)
+        if m.get("connector_vertex_id") is not None and len(m["connector_vertex_id"]):
+            cp = f"/World/{name}Connector"
+            out[f"{cp}.simConnector"] = np.int32(1)
+            out[f"{cp}.pointBody"] = np.asarray(prim)
+            out[f"{cp}.triBody"] = np.asarray(prim)
+            for key, attr in CONNECTOR_ATTRS:
+                out[f"{cp}.{attr}"] = np.asarray(m[key])
     for k, r in enumerate(rigids):
         prim = f"/World/Rigid{k}"
         out[f"{prim}.simRigid"] = np.int32(1)
@@ -197,7 +210,23 @@ def read_scene(path) -> Scene:
             meshes.append(m)
         if not meshes:
             raise ValueError(f"{path}: no simMesh prim")
-        mesh = merge_meshes(meshes)
+        mesh = dict(merge_meshes(meshes))
+        prims = _prims(z, "simMesh")
+        offset = dict(zip(prims, np.cumsum([0] + [len(m["vertex"]) for m in meshes])[:-1].tolist()))
+        cv, ct, cb, cr = [], [], [], []
+        for cp in _prims(z, "simConnector"):
+            pb, tb = str(z[f"{cp}.pointBody"]), str(z[f"{cp}.triBody"])
+            if pb not in offset or tb not in offset:
+                raise ValueError(f"{path}: connector {cp} names a body that is not a simMesh prim")
+            cv.append(np.asarray(z[f"{cp}.pointId"], dtype=np.int64).reshape(-1) + offset[pb])
+            ct.append(np.asarray(z[f"{cp}.triIds"], dtype=np.int64).reshape(-1, 3) + offset[tb])
+            cb.append(np.asarray(z[f"{cp}.triBar"], dtype=np.float32).reshape(-1, 3))
+            cr.append(np.asarray(z[f"{cp}.restDist"], dtype=np.float32).reshape(-1))
+        if cv:
+            mesh["connector_vertex_id"] = np.concatenate(cv).astype(np.int32)
+            mesh["connector_triangle_id"] = np.concatenate(ct).astype(np.int32)
+            mesh["connector_tri_bar"] = np.concatenate(cb)
+            mesh["connector_rest_dist"] = np.concatenate(cr)
         rigids = []
         for prim in _prims(z, "simRigid"):
             q = _world(z[f"{prim}.points"], z[f"{prim}.xformOp:transform"] if f"{prim}.xformOp:transform" in z

@@ -97,11 +97,13 @@ class OracleSim:
             "laparoscope_in_collision": np.zeros(model.numEnvs, dtype=np.int32),
             "env_vertex_start": model.envVertexStart, "env_tet_start": model.envTetStart,
             "env_edge_start": model.envEdgeStart, "env_tri_start": model.envTriStart,
+            "connector_triangle_id": h["connectorTriangleId"], "connector_tri_bar": h["connectorTriBar"],
+            "connector_vertex_id": h["connectorVertexId"], "connector_rest_dist": h["connectorRestDist"],
         }
         self.a = {k: np.ascontiguousarray(v) for k, v in self.a.items()}
         m = L.Model()
         m.num_vertices, m.num_tetrahedrons, m.num_edges = V, model.numTetrahedrons, model.numEdges
-        m.num_triangles, m.num_connectors, m.num_envs = model.numTriangles, 0, model.numEnvs
+        m.num_triangles, m.num_connectors, m.num_envs = model.numTriangles, model.simConnectors, model.numEnvs
         for k, v in self.a.items():
             setattr(m, k, _p(v))
         self.desc = m
