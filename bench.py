@@ -295,6 +295,14 @@ def main():
     ks[1].record(stream)
     torch.cuda.synchronize()
     step_kernel_ms = ks[0].elapsed_time(ks[1]) / kreps
+    # the observation alone: fused refit, vertex normals and the ray-cast
+    ks[0].record(stream)
+    for _ in range(kreps):
+        bvh.refitBVH()
+        r.renderNew(bvh, m)
+    ks[1].record(stream)
+    torch.cuda.synchronize()
+    observe_ms = ks[0].elapsed_time(ks[1]) / kreps
     alg = algorithmic_bytes(m)
     peak, peak_kind = peaks()
     achieved = alg / (step_kernel_ms / 1000.0) / 1e9
@@ -393,6 +401,8 @@ def main():
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                              "kernel": "k_batched (batched step, all size classes)", "kernel_ms": step_kernel_ms},
+                "observe_ms": {"value": observe_ms, "what": f"fused BVH refit + vertex normals + {RES}x{RES} "
+                                                          "ray-cast of all envs, per step"},
                 "cpu_baseline": cpu, "plain": plain, "serving": serving, "gpu_launches": launches,
                 "autotune": integ.tuning,
                 "clocks": clk.summary(), "env_status_nonzero": int((status != 0).sum())}
