@@ -429,7 +429,13 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
                                 if (fl & FFSRL_NEOHOOKEAN) { prefetch_l1(D.nh0 + gn); prefetch_l1(D.nh1 + gn); }
                                 if (D.fold) prefetch_l1(D.tet_ed + gn);
                             }
+                            // every record of the tet is requested up front, so its loads are in
+                            // flight together
                             const uint2 ix = __ldg(D.tet_idx + gt);
+                            const float2 va = __ldg(D.tet_va + gt);
+                            float4 n0 = make_float4(0.f, 0.f, 0.f, 0.f), n1 = n0, ed = n0;
+                            if (fl & FFSRL_NEOHOOKEAN) { n0 = __ldg(D.nh0 + gt); n1 = __ldg(D.nh1 + gt); }
+                            if (D.fold) ed = __ldg(D.tet_ed + gt);
                             const int ia = ix.x & 0xffff, ib = ix.x >> 16, ic = ix.y & 0xffff, id = ix.y >> 16;
                             const P PA = xp[ia], PB = xp[ib], PC = xp[ic], PD = xp[id];
                             const t3<R> pa = S::pos(PA), pb = S::pos(PB), pc = S::pos(PC), pd = S::pos(PD);
@@ -438,7 +444,6 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
                             t3<R> dA = T3<R>(0, 0, 0), dB = dA, dC = dA, dD = dA;
                             int k = 0;     // constraints that contributed
                             int skip = 0;  // statically counted constraints that skipped on degenerate geometry
-                            const float2 va = __ldg(D.tet_va + gt);
                             const bool anym = mA != R(0) || mB != R(0) || mC != R(0) || mD != R(0);
                             // cofactor columns of Ds = [p1 p2 p3]: the volume gradient, and (times det Dm^-1) the
                             // Neo-Hookean hydrostatic gradient cof(F) Dm^-T = det(Dm^-1) cof(Ds)
@@ -476,7 +481,6 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
                             if (fl & FFSRL_NEOHOOKEAN) {
                                 // neoHookeanConstraints (integrator.py:578-698) with F = Ds Dm^-1 written through
                                 // M = Dm^-1 Dm^-T: |F|^2 = sum_ij (Ds^T Ds)_ij M_ij, F Dm^-T = Ds M, det F = det Ds det Dm^-1
-                                const float4 n0 = __ldg(D.nh0 + gt), n1 = __ldg(D.nh1 + gt);
                                 const R m00 = R(n0.x), m01 = R(n0.y), m02 = R(n0.z), m11 = R(n0.w);
                                 const R m12 = R(n1.x), m22 = R(n1.y), detD = R(n1.z), inv_rv = R(n1.w);
                                 const R C = s6 * detD - R(1) - nh_off;
@@ -508,7 +512,6 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
                             const int ktet = k;  // tet constraints merged into each vertex's term
                             if (D.fold) {
                                 // distanceConstraints (integrator.py:65-109) of the edges this tet solves
-                                const float4 ed = __ldg(D.tet_ed + gt);
                                 if (ed.y != 0.0f) k += fold_edge<R>(pa, pb, mA, mB, R(ed.x), R(ed.y), dA, dB, ia, ib, cnt, it, R(D.ks_distance), &s_dyn_it, sc);
                                 if (ed.w != 0.0f) {
                                     if (ed.z > 0.0f) k += fold_edge<R>(pc, pd, mC, mD, R(ed.z), R(ed.w), dC, dD, ic, id, cnt, it, R(D.ks_distance), &s_dyn_it, sc);
@@ -684,7 +687,7 @@ typedef void (*kern_d)(const Dev<double>, const int*, int, int*, int, unsigned c
 
 kern_f pick_f(int block, int mode) {
 #define PK(B, M) if (block == B && mode == M) return k_batched<float, B, M>;
-    PK(128, 0) PK(256, 0) PK(512, 0) PK(1024, 0)
+    PK(128, 0) PK(256, 0) PK(512, 0) PK(768, 0) PK(1024, 0)
     PK(256, 1) PK(512, 1) PK(1024, 1)
     PK(256, 2) PK(512, 2)
 #undef PK

@@ -240,117 +240,59 @@ __device__ __forceinline__ EnvView env_view(const ffsrl_bvh& b, int e) {
     return v;
 }
 
-// The part of intersectAABB's decision that does not depend on tMin, for a box tested
-// before it is popped: `hit` is (tmax >= 0 && tmax >= tmin) as the reference decides it,
-// and [lo, hi] holds the reference's tnear (tmin).  The reciprocal form decides when it
-// is farther from every threshold than its rounding (8 float ulps of the summed
-// distances, as in node_hit); otherwise the reference's divisions give both exactly.
-struct BoxTest { bool hit; float lo, hi; };
-
-__device__ __forceinline__ BoxTest box_test(v3 ro, v3 rd, v3 inv, float4 a, float4 c) {
-    const v3 lo = mk(a.x, a.y, a.z), hi = mk(c.x, c.y, c.z);
-    float t1 = (lo.x - ro.x) * inv.x, t2 = (hi.x - ro.x) * inv.x;
-    float t3 = (lo.y - ro.y) * inv.y, t4 = (hi.y - ro.y) * inv.y;
-    float t5 = (lo.z - ro.z) * inv.z, t6 = (hi.z - ro.z) * inv.z;
-    float m = ((fabsf(t1) + fabsf(t2)) + (fabsf(t3) + fabsf(t4))) + (fabsf(t5) + fabsf(t6));
-    BoxTest r;
-    if (m < 3.0e37f) {
-        float tmin = fmaxf(fmaxf(fminf(t1, t2), fminf(t3, t4)), fminf(t5, t6));
-        float tmax = fminf(fminf(fmaxf(t1, t2), fmaxf(t3, t4)), fmaxf(t5, t6));
-        float g = m * 4.76837158e-7f;  // 8 * 2^-24 * m
-        if (tmax < -g || tmax - tmin < -2.0f * g) { r.hit = false; r.lo = r.hi = 0.0f; return r; }
-        if (tmax > g && tmax - tmin > 2.0f * g) { r.hit = true; r.lo = tmin - g; r.hi = tmin + g; return r; }
-    }
-    float tn;
-    r.hit = slab(ro, rd, lo, hi, tn);
-    r.lo = r.hi = tn;
-    return r;
-}
-
-// a node's traversal word from its packed box: leftNode for an inner node, the bitwise
-// complement of (first * 256 + min(count, 255)) for a leaf
-__device__ __forceinline__ int node_info(float4 a, float4 c) {
-    const int left = __float_as_int(a.w);
-    return left == -1 ? ~__float_as_int(c.w) : left;
-}
-
 // meshQueryRayManyEnvs (render.py:411-498): nearest hit with 0 < t < tMin, stack LIFO
 // with the right child popped first.  Returns the global face id or -1.
-// Over the packed copies written by the refit.  A node's box is tested when its parent
-// is expanded, with both children's boxes loaded together: a child whose box the ray
-// misses is never pushed (the reference pushes it, pops it and rejects it, which changes
-// nothing), and a pushed child carries its tnear interval, so the reference's pop-time
-// test tnear < tMin is decided against the tMin of that moment.  The nodes taken, their
-// order and the hits are the reference's.
+// Traversal over the packed copies written by the refit: two 16-byte loads per node and
+// contiguous leaf triangles; the same node order, tests and hits as query().
 __device__ int query_packed(const EnvView& ev, v3 ro, v3 rd, float& t_hit, v3& p_hit, int* err) {
-    int4 stack[kStackCap];  // node, traversal word, tnear interval (float bits)
-    int count = 0;
+    int stack[kStackCap];
+    int count = 1;
+    stack[0] = 0;
     float tMin = 1e6f;
     int hit_tri = -1;
     int visits = 0;
     const v3 inv = mk(1.0f / rd.x, 1.0f / rd.y, 1.0f / rd.z);
-    {
-        const float4 a = __ldg(ev.box), c = __ldg(ev.box + 1);
-        const BoxTest bt = box_test(ro, rd, inv, a, c);
-        if (bt.hit) stack[count++] = make_int4(0, node_info(a, c), __float_as_int(bt.lo), __float_as_int(bt.hi));
-    }
     while (count) {
-        const int4 e = stack[--count];
+        int node = stack[--count];
         if (++visits > ev.nn) {
             atomicExch(err, FFSRL_ERR_STACK_OVERFLOW);
             return -1;
         }
-        const int node = e.x, info = e.y;
-        const float lo = __int_as_float(e.z), hi = __int_as_float(e.w);
-        bool take;
-        if (hi < tMin) {
-            take = true;
-        } else if (lo >= tMin) {
-            take = false;
-        } else {  // within the rounding band: the reference's division form decides
-            const float4 a = __ldg(ev.box + 2 * node), c = __ldg(ev.box + 2 * node + 1);
-            float tn;
-            const bool h = slab(ro, rd, mk(a.x, a.y, a.z), mk(c.x, c.y, c.z), tn);
-            take = h && tn < tMin;
-        }
-        if (!take) continue;
-        if (info < 0) {
-            const int fc = ~info;
-            const int first = fc >> 8;
-            int cnt = fc & 255;
-            if (cnt == 255) cnt = ev.count[node];
-            for (int k = 0; k < cnt; ++k) {
-                const float4* q = ev.tpos + 3ll * (first + k);
-                const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2);
-                v3 A = mk(q0.x, q0.y, q0.z);
-                v3 B = mk(q0.w, q1.x, q1.y);
-                v3 C = mk(q1.z, q1.w, q2.x);
-                v3 p;
-                float t = moller_trumbore(A, B, C, ro, rd, p);
-                if (t < tMin && t > 0.0f) {
-                    tMin = t;
-                    hit_tri = (int)(ev.fofs + ev.tri[first + k]);
-                    t_hit = t;
-                    p_hit = p;
+        const float4 a = __ldg(ev.box + 2 * node), c = __ldg(ev.box + 2 * node + 1);
+        if (node_hit(ro, rd, inv, mk(a.x, a.y, a.z), mk(c.x, c.y, c.z), tMin)) {
+            int left = __float_as_int(a.w);
+            if (left == -1) {
+                int fc = __float_as_int(c.w);
+                int first = fc >> 8, cnt = fc & 255;
+                if (cnt == 255) cnt = ev.count[node];
+                for (int k = 0; k < cnt; ++k) {
+                    const float4* q = ev.tpos + 3ll * (first + k);
+                    const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2);
+                    v3 A = mk(q0.x, q0.y, q0.z);
+                    v3 B = mk(q0.w, q1.x, q1.y);
+                    v3 C = mk(q1.z, q1.w, q2.x);
+                    v3 p;
+                    float t = moller_trumbore(A, B, C, ro, rd, p);
+                    if (t < tMin && t > 0.0f) {
+                        tMin = t;
+                        hit_tri = (int)(ev.fofs + ev.tri[first + k]);
+                        t_hit = t;
+                        p_hit = p;
+                    }
                 }
+            } else {
+                if (left < 0 || left + 1 >= ev.nn) {
+                    atomicExch(err, FFSRL_ERR_INVALID_ARGUMENT);
+                    return -1;
+                }
+                if (count + 2 > kStackCap) {
+                    atomicExch(err, FFSRL_ERR_STACK_OVERFLOW);
+                    return -1;
+                }
+                stack[count] = left;
+                stack[count + 1] = left + 1;
+                count += 2;
             }
-        } else {
-            const int left = info;
-            if (left < 1 || left + 1 >= ev.nn) {
-                atomicExch(err, FFSRL_ERR_INVALID_ARGUMENT);
-                return -1;
-            }
-            if (count + 2 > kStackCap) {
-                atomicExch(err, FFSRL_ERR_STACK_OVERFLOW);
-                return -1;
-            }
-            const float4 la = __ldg(ev.box + 2 * left), lc = __ldg(ev.box + 2 * left + 1);
-            const float4 ra = __ldg(ev.box + 2 * left + 2), rc = __ldg(ev.box + 2 * left + 3);
-            const BoxTest bl = box_test(ro, rd, inv, la, lc);
-            const BoxTest br = box_test(ro, rd, inv, ra, rc);
-            if (bl.hit) stack[count++] = make_int4(left, node_info(la, lc), __float_as_int(bl.lo), __float_as_int(bl.hi));
-            if (br.hit)
-                stack[count++] = make_int4(left + 1, node_info(ra, rc), __float_as_int(br.lo), __float_as_int(br.hi));
         }
     }
     if (tMin >= 1e6f) hit_tri = -1;

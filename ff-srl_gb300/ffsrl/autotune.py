@@ -22,7 +22,7 @@ import torch
 
 from ._lib import FFSRLError, check, lib
 
-CANDIDATES = (128, 256, 512, 1024)
+CANDIDATES = (128, 256, 512, 768, 1024)
 PREFETCH = (0, 1)  # L1 prefetch of each thread's next tet record off / on
 
 
