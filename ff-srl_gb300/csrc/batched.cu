@@ -302,7 +302,9 @@ template <class R> struct ToolShared {
 
 // MODE 0: positions and accumulators in shared memory.  MODE 1: positions in shared
 // memory, accumulators in the block's global scratch.  MODE 2: both in global scratch.
-template <class R, int BLOCK, int MODE>
+// PIPE: the tet loop holds the thread's next tet record in registers, loaded while the
+// current one is solved (for block sizes that leave the registers for it).
+template <class R, int BLOCK, int MODE, bool PIPE = false>
 __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_batched(const Dev<R> D, const int* __restrict__ work, int nwork,
                                                    int* counter, int nsteps, unsigned char* scratch,
                                                    long long scratch_stride, int max_nv, int prefetch) {
@@ -420,22 +422,45 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
                 for (int it = 0; it < D.iterations; ++it) {
                     // ---- tet constraints: volume, XPBD volume, Neo-Hookean ----
                     if (fl & (FFSRL_VOLUME | FFSRL_VOLUME_XPBD | FFSRL_NEOHOOKEAN)) {
+                        const bool nhf = (fl & FFSRL_NEOHOOKEAN) != 0;
+                        uint2 ix_n = make_uint2(0u, 0u);
+                        float2 va_n = make_float2(0.f, 0.f);
+                        float4 n0_n = make_float4(0.f, 0.f, 0.f, 0.f), n1_n = n0_n, ed_n = n0_n;
+                        if (PIPE && tid < nt) {
+                            const int g0 = E.t0 + tid;
+                            ix_n = __ldg(D.tet_idx + g0); va_n = __ldg(D.tet_va + g0);
+                            if (nhf) { n0_n = __ldg(D.nh0 + g0); n1_n = __ldg(D.nh1 + g0); }
+                            if (D.fold) ed_n = __ldg(D.tet_ed + g0);
+                        }
                         for (int t = tid; t < nt; t += BLOCK) {
                             const int gt = E.t0 + t;
-                            if (prefetch && t + BLOCK < nt) {  // this thread's next record
-                                const int gn = gt + BLOCK;
-                                prefetch_l1(D.tet_idx + gn);
-                                prefetch_l1(D.tet_va + gn);
-                                if (fl & FFSRL_NEOHOOKEAN) { prefetch_l1(D.nh0 + gn); prefetch_l1(D.nh1 + gn); }
-                                if (D.fold) prefetch_l1(D.tet_ed + gn);
+                            uint2 ix;
+                            float2 va;
+                            float4 n0, n1, ed;
+                            if (PIPE) {
+                                ix = ix_n; va = va_n; n0 = n0_n; n1 = n1_n; ed = ed_n;
+                                if (t + BLOCK < nt) {  // the next record, in flight while this tet is solved
+                                    const int gn = gt + BLOCK;
+                                    ix_n = __ldg(D.tet_idx + gn); va_n = __ldg(D.tet_va + gn);
+                                    if (nhf) { n0_n = __ldg(D.nh0 + gn); n1_n = __ldg(D.nh1 + gn); }
+                                    if (D.fold) ed_n = __ldg(D.tet_ed + gn);
+                                }
+                            } else {
+                                if (prefetch && t + BLOCK < nt) {  // this thread's next record, into L1
+                                    const int gn = gt + BLOCK;
+                                    prefetch_l1(D.tet_idx + gn);
+                                    prefetch_l1(D.tet_va + gn);
+                                    if (nhf) { prefetch_l1(D.nh0 + gn); prefetch_l1(D.nh1 + gn); }
+                                    if (D.fold) prefetch_l1(D.tet_ed + gn);
+                                }
+                                // every record of the tet is requested up front, so its loads are in
+                                // flight together
+                                ix = __ldg(D.tet_idx + gt);
+                                va = __ldg(D.tet_va + gt);
+                                n0 = n1 = ed = make_float4(0.f, 0.f, 0.f, 0.f);
+                                if (nhf) { n0 = __ldg(D.nh0 + gt); n1 = __ldg(D.nh1 + gt); }
+                                if (D.fold) ed = __ldg(D.tet_ed + gt);
                             }
-                            // every record of the tet is requested up front, so its loads are in
-                            // flight together
-                            const uint2 ix = __ldg(D.tet_idx + gt);
-                            const float2 va = __ldg(D.tet_va + gt);
-                            float4 n0 = make_float4(0.f, 0.f, 0.f, 0.f), n1 = n0, ed = n0;
-                            if (fl & FFSRL_NEOHOOKEAN) { n0 = __ldg(D.nh0 + gt); n1 = __ldg(D.nh1 + gt); }
-                            if (D.fold) ed = __ldg(D.tet_ed + gt);
                             const int ia = ix.x & 0xffff, ib = ix.x >> 16, ic = ix.y & 0xffff, id = ix.y >> 16;
                             const P PA = xp[ia], PB = xp[ib], PC = xp[ic], PD = xp[id];
                             const t3<R> pa = S::pos(PA), pb = S::pos(PB), pc = S::pos(PC), pd = S::pos(PD);
@@ -685,9 +710,16 @@ template <class R> size_t scratch_bytes(int mode, int max_nv) {
 typedef void (*kern_f)(const Dev<float>, const int*, int, int*, int, unsigned char*, long long, int, int);
 typedef void (*kern_d)(const Dev<double>, const int*, int, int*, int, unsigned char*, long long, int, int);
 
-kern_f pick_f(int block, int mode) {
+// prefetch 0: none, 1: L1 prefetch of the next record, 2: the next record held in
+// registers (PIPE instantiations only)
+kern_f pick_f(int block, int mode, int prefetch = 0) {
+    if (prefetch == 2) {
+        if (mode == 0 && block == 512) return k_batched<float, 512, 0, true>;
+        if (mode == 0 && block == 640) return k_batched<float, 640, 0, true>;
+        return nullptr;
+    }
 #define PK(B, M) if (block == B && mode == M) return k_batched<float, B, M>;
-    PK(128, 0) PK(256, 0) PK(512, 0) PK(768, 0) PK(1024, 0)
+    PK(128, 0) PK(256, 0) PK(512, 0) PK(640, 0) PK(768, 0) PK(1024, 0)
     PK(256, 1) PK(512, 1) PK(1024, 1)
     PK(256, 2) PK(512, 2)
 #undef PK
@@ -822,13 +854,13 @@ Dev<float> make_dev_f(ffsrl_batch* b) {
 
 template <> int32_t launch_class<float>(ffsrl_batch* b, const ffsrl_batch::Class& c, const int* work, int nwork,
                                         int* counter, unsigned char* scratch, int nsteps, cudaStream_t s) {
-    kern_f k = pick_f(c.block, c.mode);
+    kern_f k = pick_f(c.block, c.mode, c.prefetch);
     if (!k) return fail(FFSRL_ERR_UNSUPPORTED, "ffsrl_batch: no kernel for block/mode");
     Dev<float> D = make_dev_f(b);
     int grid = std::min(c.grid, nwork);
     if (grid <= 0) return FFSRL_OK;
     k<<<grid, c.block, c.smem, s>>>(D, work, nwork, counter, nsteps, scratch + c.scratch_offset,
-                                    (long long)c.scratch_stride, c.max_nv, c.prefetch);
+                                    (long long)c.scratch_stride, c.max_nv, c.prefetch == 1 ? 1 : 0);
     FFSRL_LAUNCH_CHECK("ffsrl_batch: step kernel");
     return FFSRL_OK;
 }
@@ -855,7 +887,7 @@ template <> int32_t launch_class<double>(ffsrl_batch* b, const ffsrl_batch::Clas
     int grid = std::min(c.grid, nwork);
     if (grid <= 0) return FFSRL_OK;
     k<<<grid, c.block, c.smem, s>>>(D, work, nwork, counter, nsteps, scratch + c.scratch_offset,
-                                    (long long)c.scratch_stride, c.max_nv, c.prefetch);
+                                    (long long)c.scratch_stride, c.max_nv, c.prefetch == 1 ? 1 : 0);
     FFSRL_LAUNCH_CHECK("ffsrl_batch: float64 step kernel");
     return FFSRL_OK;
 }
@@ -940,7 +972,8 @@ int32_t configure_class(ffsrl_batch* b, ffsrl_batch::Class& c, int block, size_t
     if (b->precision == 64) block = 256;
     if (c.mode == 1 && block < 256) block = 256;
     if (c.mode == 2 && block > 512) block = 512;
-    const void* kfn = b->precision == 64 ? (const void*)pick_d(block, c.mode) : (const void*)pick_f(block, c.mode);
+    const void* kfn = b->precision == 64 ? (const void*)pick_d(block, c.mode)
+                                         : (const void*)pick_f(block, c.mode, c.prefetch);
     if (!kfn) return fail(FFSRL_ERR_UNSUPPORTED, "ffsrl_batch: no kernel for block " + std::to_string(block) +
                                                      " in mode " + std::to_string(c.mode));
     if (c.smem > 48 * 1024) {
@@ -1648,11 +1681,16 @@ extern "C" int32_t ffsrl_batch_class_envs(const ffsrl_batch* b, int32_t cls, int
     return FFSRL_OK;
 }
 
-extern "C" int32_t ffsrl_batch_set_class_prefetch(ffsrl_batch* b, int32_t cls, int32_t on) {
-    if (!b || cls < 0 || cls >= (int)b->classes.size() || (on != 0 && on != 1))
+extern "C" int32_t ffsrl_batch_set_class_prefetch(ffsrl_batch* b, int32_t cls, int32_t kind) {
+    if (!b || cls < 0 || cls >= (int)b->classes.size() || kind < 0 || kind > 2)
         return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_set_class_prefetch");
+    if (kind == 2 && b->precision == 64)
+        return fail(FFSRL_ERR_UNSUPPORTED, "ffsrl_batch_set_class_prefetch: no float64 register pipeline");
     FFSRL_CUDA_TRY(cudaDeviceSynchronize());
-    b->classes[cls].prefetch = on;
+    ffsrl_batch::Class c = b->classes[cls];
+    c.prefetch = kind;
+    if (int32_t st = configure_class(b, c, c.block, b->dyn_budget)) return st;
+    b->classes[cls] = c;
     return FFSRL_OK;
 }
 

@@ -22,8 +22,8 @@ import torch
 
 from ._lib import FFSRLError, check, lib
 
-CANDIDATES = (128, 256, 512, 768, 1024)
-PREFETCH = (0, 1)  # L1 prefetch of each thread's next tet record off / on
+CANDIDATES = (128, 256, 512, 640, 768, 1024)
+PREFETCH = (0, 1, 2)  # next tet record: not fetched ahead, into L1, into registers
 
 
 def cache_path() -> Path:
@@ -47,7 +47,7 @@ def _key(plan, cls) -> str:
     m = plan.model
     props = torch.cuda.get_device_properties(m.device)
     tets = int(sum(int(m.envTetStart[e + 1] - m.envTetStart[e]) for e in cls["envs"]))
-    sig = f"v2|{props.name}|{props.multi_processor_count}|{m.constraintFlags}|{m.simSubsteps}|{m.simConstraints}|" \
+    sig = f"v3|{props.name}|{props.multi_processor_count}|{m.constraintFlags}|{m.simSubsteps}|{m.simConstraints}|" \
           f"{cls['mode']}|{cls['max_nv']}|{len(cls['envs'])}|{tets}|{plan.precision}"
     return hashlib.sha1(sig.encode()).hexdigest()[:16]
 
@@ -81,6 +81,7 @@ def autotune(plan, reps: int = 2, use_cache: bool = True, verbose: bool = False)
             key = _key(plan, cls)
             if key in cache:
                 c = cache[key]
+                check(lib().ffsrl_batch_set_class_prefetch(plan.handle, ci, 0))
                 check(lib().ffsrl_batch_set_class_block(plan.handle, ci, int(c["block"])))
                 check(lib().ffsrl_batch_set_class_prefetch(plan.handle, ci, int(c.get("prefetch", 0))))
                 result.append({"class": ci, "block": c["block"], "prefetch": c.get("prefetch", 0), "ms": c["ms"],
@@ -88,10 +89,12 @@ def autotune(plan, reps: int = 2, use_cache: bool = True, verbose: bool = False)
                 continue
             best = None
             for b in CANDIDATES:
+                check(lib().ffsrl_batch_set_class_prefetch(plan.handle, ci, 0))
                 if lib().ffsrl_batch_set_class_block(plan.handle, ci, b) != 0:
                     continue
                 for pf in PREFETCH:
-                    check(lib().ffsrl_batch_set_class_prefetch(plan.handle, ci, pf))
+                    if lib().ffsrl_batch_set_class_prefetch(plan.handle, ci, pf) != 0:
+                        continue
                     ms = _time(plan, cls["envs"], reps)
                     if verbose:
                         print(f"autotune class {ci} (max_nv {cls['max_nv']}, {len(cls['envs'])} envs): "
@@ -100,6 +103,7 @@ def autotune(plan, reps: int = 2, use_cache: bool = True, verbose: bool = False)
                         best = (b, pf, ms)
             if best is None:
                 raise FFSRLError(6, f"autotune: no block size fits class {ci}")
+            check(lib().ffsrl_batch_set_class_prefetch(plan.handle, ci, 0))
             check(lib().ffsrl_batch_set_class_block(plan.handle, ci, best[0]))
             check(lib().ffsrl_batch_set_class_prefetch(plan.handle, ci, best[1]))
             cache[key] = {"block": best[0], "prefetch": best[1], "ms": best[2]}

@@ -371,9 +371,11 @@ int32_t ffsrl_batch_class_info(const ffsrl_batch* b, int32_t cls, int32_t* max_n
                                int32_t* num_envs);
 int32_t ffsrl_batch_class_envs(const ffsrl_batch* b, int32_t cls, int32_t* env_ids);
 int32_t ffsrl_batch_set_class_block(ffsrl_batch* b, int32_t cls, int32_t block);
-/* Autotuner hook: on = 1 makes class cls's kernel request each thread's next tet record
-   into L1 one loop trip ahead (prefetch.global.L1); results are unchanged. */
-int32_t ffsrl_batch_set_class_prefetch(ffsrl_batch* b, int32_t cls, int32_t on);
+/* Autotuner hook, how class cls's kernel fetches each thread's next tet record one loop
+   trip ahead: 0 not at all, 1 into L1 (prefetch.global.L1), 2 into registers (block sizes
+   512 and 640, float32).  Results are unchanged.  A kind the class's block size has no
+   kernel for is refused and leaves the class as it was. */
+int32_t ffsrl_batch_set_class_prefetch(ffsrl_batch* b, int32_t cls, int32_t kind);
 /* Copies the float64 plan's state (x, v, predicted, each [3V]) to host memory. */
 int32_t ffsrl_batch_state_f64(const ffsrl_batch* b, double* host_xvx);
 /* per-env status after a step: 0 ok, FFSRL_ERR_NONFINITE if the env's state went non-finite */

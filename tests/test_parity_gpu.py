@@ -259,7 +259,7 @@ def test_prefetch_and_block_size_do_not_change_results(gpu):
     # schedule only: the fixed-point sums are exact, so every choice gives the same bits
     meshes, _ = sc.mixed_meshes(6, pool_size=3, seed=31, t_lo=400, t_hi=3000)
     out = []
-    for block, pf in ((256, 0), (256, 1), (512, 1), (768, 0), (1024, 1)):
+    for block, pf in ((256, 0), (256, 1), (512, 2), (640, 2), (768, 0), (1024, 1)):
         m, _ = sc.liver_model("cuda:0", 6, meshes=meshes)
         m.graspNearest(torch.ones(6, dtype=torch.int32, device="cuda:0"))
         integ = SimIntegratorDO("cuda:0")
