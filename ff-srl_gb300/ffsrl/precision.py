@@ -27,11 +27,16 @@ def det_f(x: np.ndarray, tets: np.ndarray, rest_signed: np.ndarray) -> np.ndarra
 
 def precision_report(meshes, steps: int, substeps: int = 16, iterations: int = 50, nu: float = 0.49,
                      device: str = "cuda:0") -> dict:
+    """Config-3 form: the liver constraint set (no contact) at Poisson ratio ``nu``."""
+    make = lambda: sc.liver_model(device, len(meshes), meshes=meshes, nu=nu, substeps=substeps,
+                                  iterations=iterations, collide=False)[0]
+    return compare(make(), make(), steps) | {"substeps": substeps, "iterations": iterations, "nu": nu}
+
+
+def compare(m32, m64, steps: int) -> dict:
+    """Steps two identical models, one in the float32 batched kernel and one in its float64
+    build, and reports the float32 run's errors against the float64 run."""
     import torch
-    m32, _ = sc.liver_model(device, len(meshes), meshes=meshes, nu=nu, substeps=substeps, iterations=iterations,
-                            collide=False)
-    m64, _ = sc.liver_model(device, len(meshes), meshes=meshes, nu=nu, substeps=substeps, iterations=iterations,
-                            collide=False)
     p32 = BatchPlan(m32)
     p64 = BatchPlan(m64, precision=64)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
@@ -49,7 +54,7 @@ def precision_report(meshes, steps: int, substeps: int = 16, iterations: int = 5
     rest = m32.host["tetrahedronRestVolumeSigned"]
     j32, j64 = det_f(x32, tets, rest), det_f(x64, tets, rest)
     return {
-        "envs": len(meshes), "steps": steps, "substeps": substeps, "iterations": iterations, "nu": nu,
+        "envs": int(m32.numEnvs), "steps": steps, "substeps": m32.simSubsteps, "iterations": m32.simConstraints,
         "vertices": int(m32.numVertices), "tets": int(m32.numTetrahedrons),
         "max_pos_err": float(d.max()), "rms_pos_err": float(np.sqrt((d ** 2).mean())),
         "max_pos_err_rel": float(d.max() / scale), "rms_pos_err_rel": float(np.sqrt((d ** 2).mean()) / scale),
@@ -58,3 +63,35 @@ def precision_report(meshes, steps: int, substeps: int = 16, iterations: int = 5
         "ms_f32": ev[0].elapsed_time(ev[1]), "ms_f64": ev[1].elapsed_time(ev[2]),
         "finite": bool(np.isfinite(x32).all() and np.isfinite(x64).all()),
     }
+
+
+def all_configs(device: str = "cuda:0") -> list[dict]:
+    """The float32-vs-float64 report for each workload: the beam (config 0, reference
+    step, 25 steps), the 12/8/6 cm ellipsoid (config 1, Neo-Hookean, grasp, 5 steps),
+    envs of the mixed-size pool shared by the throughput and serving workloads (configs 2
+    and 4, 16 envs, 5 steps) and the nearly incompressible ellipsoid (config 3, nu 0.49,
+    16 substeps x 50 iterations, 3 steps).  The float64 build is slow, so the env counts
+    and step counts are samples of each workload."""
+    import torch
+    from . import meshgen as mg
+    out = []
+    beam = lambda: sc.beam_model(device, 1)[0]
+    out.append({"config": "0 beam, reference step"} | compare(beam(), beam(), 25))
+
+    def liver(meshes, **kw):
+        m, _ = sc.liver_model(device, len(meshes), meshes=meshes, **kw)
+        m.graspNearest(torch.ones(len(meshes), dtype=torch.int32, device=device), radius=0.5)
+        return m
+
+    ell = [mg.ellipsoid()]
+    out.append({"config": "1 ellipsoid, Neo-Hookean + grasp + contact"} | compare(liver(ell), liver(ell), 5))
+    pool, _ = sc.mixed_meshes(16, pool_size=64, seed=0)
+    out.append({"config": "2/4 mixed-size pool, 16 envs"} | compare(liver(pool), liver(pool), 5))
+    out.append({"config": "3 ellipsoid, nu 0.49, 16 x 50"} | precision_report(ell, steps=3, device=device))
+    return out
+
+
+if __name__ == "__main__":
+    import json
+    for row in all_configs():
+        print(json.dumps(row))
