@@ -297,8 +297,13 @@ template <class R> struct ToolShared {
     t3<R> base[3], tip[3];
     R radius[3];
     t3<R> blo[3], bhi[3];  // conservative contact boxes per capsule
+    t3<R> ulo, uhi;        // their union
     t3<R> drag_tip;
 };
+
+// near-contact triangles an iteration's scan hands to the whole block (entries: triangle
+// << 3 | capsule mask); more than this are solved by the thread that found them
+constexpr int kNearCap = 512;
 
 // MODE 0: positions and accumulators in shared memory.  MODE 1: positions in shared
 // memory, accumulators in the block's global scratch.  MODE 2: both in global scratch.
@@ -318,6 +323,8 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
     __shared__ int s_any_contact;
     __shared__ int s_any_drag;
     __shared__ int s_dyn_it;  // iteration in which a constraint skipped on degenerate geometry
+    __shared__ int s_near_n;
+    __shared__ unsigned s_near[kNearCap];
     __shared__ ToolShared<R> tool;
 
     unsigned char* gbase = scratch + (long long)blockIdx.x * scratch_stride;
@@ -364,19 +371,28 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
 
         if (tid == 0) { s_incol = 0; s_bad = 0; s_any_drag = 0; s_dyn_it = -1; }
         bool bad = false;
-        if (tid < 3) {
-            long long k = 4ll * env + tid;
-            t3<R> b = prom<R>(ldf3(D.lap_base, k)), t = prom<R>(ldf3(D.lap_tip, k));
-            R r = R(D.lap_radius[k]);
-            tool.base[tid] = b; tool.tip[tid] = t; tool.radius[tid] = r;
-            t3<R> cn = normalize(t - b);
-            t3<R> off = cn * r;
-            t3<R> pa = b + off, pb = t - off;
-            R mag = rmax(rmax(rmax(fabs(pa.x), fabs(pa.y)), rmax(fabs(pa.z), fabs(pb.x))), rmax(fabs(pb.y), fabs(pb.z)));
-            R m = r + R(1e-4) * (R(1) + mag);
-            tool.blo[tid] = T3<R>(rmin(pa.x, pb.x) - m, rmin(pa.y, pb.y) - m, rmin(pa.z, pb.z) - m);
-            tool.bhi[tid] = T3<R>(rmax(pa.x, pb.x) + m, rmax(pa.y, pb.y) + m, rmax(pa.z, pb.z) + m);
-            if (tid == 2) tool.drag_tip = t;
+        if (tid == 0) {
+            for (int i = 0; i < 3; ++i) {
+                long long k = 4ll * env + i;
+                t3<R> b = prom<R>(ldf3(D.lap_base, k)), t = prom<R>(ldf3(D.lap_tip, k));
+                R r = R(D.lap_radius[k]);
+                tool.base[i] = b; tool.tip[i] = t; tool.radius[i] = r;
+                t3<R> cn = normalize(t - b);
+                t3<R> off = cn * r;
+                t3<R> pa = b + off, pb = t - off;
+                R mag = rmax(rmax(rmax(fabs(pa.x), fabs(pa.y)), rmax(fabs(pa.z), fabs(pb.x))),
+                             rmax(fabs(pb.y), fabs(pb.z)));
+                R m = r + R(1e-4) * (R(1) + mag);
+                tool.blo[i] = T3<R>(rmin(pa.x, pb.x) - m, rmin(pa.y, pb.y) - m, rmin(pa.z, pb.z) - m);
+                tool.bhi[i] = T3<R>(rmax(pa.x, pb.x) + m, rmax(pa.y, pb.y) + m, rmax(pa.z, pb.z) + m);
+                if (i == 2) tool.drag_tip = t;
+            }
+            tool.ulo = T3<R>(rmin(tool.blo[0].x, rmin(tool.blo[1].x, tool.blo[2].x)),
+                             rmin(tool.blo[0].y, rmin(tool.blo[1].y, tool.blo[2].y)),
+                             rmin(tool.blo[0].z, rmin(tool.blo[1].z, tool.blo[2].z)));
+            tool.uhi = T3<R>(rmax(tool.bhi[0].x, rmax(tool.bhi[1].x, tool.bhi[2].x)),
+                             rmax(tool.bhi[0].y, rmax(tool.bhi[1].y, tool.bhi[2].y)),
+                             rmax(tool.bhi[0].z, rmax(tool.bhi[1].z, tool.bhi[2].z)));
         }
         for (int i = tid; i < nv; i += BLOCK) {
             acc[3 * i] = A(0); acc[3 * i + 1] = A(0); acc[3 * i + 2] = A(0);
@@ -597,6 +613,7 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
                     __syncthreads();
                     // ---- applyConstraints + dragConstraintsDO ----
                     const bool restore = s_dyn_it == it;
+                    if (tid == 0) { s_any_contact = 0; s_near_n = 0; }  // for this iteration's contact phase
                     for (int i = tid; i < nv; i += BLOCK) {
                         int c = cnt[i];
                         P q = xp[i];
@@ -618,25 +635,13 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
                     }
                     __syncthreads();
                     // ---- collideLaparoscopeDO (integrator.py:981-1050), positions as of phase start ----
+                    // A scan tests every surface triangle's box against the capsules' boxes (their
+                    // union first) and lists the near ones; the block then solves the listed
+                    // triangles, one per thread, so the few contacts do not serialise a warp.
                     if ((fl & FFSRL_COLLIDE) && nf > 0) {
-                        if (tid == 0) s_any_contact = 0;
-                        __syncthreads();
                         const R ks = R(D.ks_contact);
-                        for (int f = tid; f < nf; f += BLOCK) {
-                            const uint2 tr = __ldg(D.tri_idx + (long long)E.f0 + f);
-                            if ((tr.y >> 16) == 1u) continue;
-                            const int a = tr.x & 0xffff, b = tr.x >> 16, c = tr.y & 0xffff;
-                            const P PA = xp[a], PB = xp[b], PC = xp[c];
+                        auto contact = [&](int a, int b, int c, const P& PA, const P& PB, const P& PC, unsigned near) {
                             const t3<R> pA = S::pos(PA), pB = S::pos(PB), pC = S::pos(PC);
-                            const t3<R> lo = T3<R>(rmin(pA.x, rmin(pB.x, pC.x)), rmin(pA.y, rmin(pB.y, pC.y)), rmin(pA.z, rmin(pB.z, pC.z)));
-                            const t3<R> hi = T3<R>(rmax(pA.x, rmax(pB.x, pC.x)), rmax(pA.y, rmax(pB.y, pC.y)), rmax(pA.z, rmax(pB.z, pC.z)));
-                            unsigned near = 0;
-                            for (int i = 0; i < 3; ++i) {
-                                bool apart = lo.x > tool.bhi[i].x || lo.y > tool.bhi[i].y || lo.z > tool.bhi[i].z ||
-                                             hi.x < tool.blo[i].x || hi.y < tool.blo[i].y || hi.z < tool.blo[i].z;
-                                if (!apart) near |= 1u << i;
-                            }
-                            if (!near) continue;
                             t3<R> centre = (pA + pB + pC) * R(0.3333f);
                             t3<R> n = normalize(cross(pB - pA, pC - pA));
                             t3<R> tA = T3<R>(0, 0, 0), tB = tA, tC = tA;
@@ -644,16 +649,48 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
                             for (int i = 0; i < 3; ++i) {
                                 if (!((near >> i) & 1u)) continue;
                                 t3<R> rA = T3<R>(0, 0, 0), rB = rA, rC = rA;
-                                capsule_response(tool.tip[i], tool.base[i], tool.radius[i], n, centre, pA, pB, pC, ks, rA, rB, rC);
+                                capsule_response(tool.tip[i], tool.base[i], tool.radius[i], n, centre, pA, pB, pC, ks, rA,
+                                                 rB, rC);
                                 tA = tA + rA; tB = tB + rB; tC = tC + rC;
                                 tl = tl + length(rA) + length(rB) + length(rC);
                             }
                             if (tl > R(0)) atomicAdd(&s_incol, 1);
-                            if (!(tl > R(0)) && !isnan(tl)) continue;  // every response is zero
+                            if (!(tl > R(0)) && !isnan(tl)) return;  // every response is zero
                             s_any_contact = 1;
                             if (PA.w > R(0)) add3<R>(acc, a, tA, bad, fx);
                             if (PB.w > R(0)) add3<R>(acc, b, tB, bad, fx);
                             if (PC.w > R(0)) add3<R>(acc, c, tC, bad, fx);
+                        };
+                        for (int f = tid; f < nf; f += BLOCK) {
+                            const uint2 tr = __ldg(D.tri_idx + (long long)E.f0 + f);
+                            if ((tr.y >> 16) == 1u) continue;
+                            const int a = tr.x & 0xffff, b = tr.x >> 16, c = tr.y & 0xffff;
+                            const P PA = xp[a], PB = xp[b], PC = xp[c];
+                            const t3<R> lo = T3<R>(rmin(PA.x, rmin(PB.x, PC.x)), rmin(PA.y, rmin(PB.y, PC.y)),
+                                                   rmin(PA.z, rmin(PB.z, PC.z)));
+                            const t3<R> hi = T3<R>(rmax(PA.x, rmax(PB.x, PC.x)), rmax(PA.y, rmax(PB.y, PC.y)),
+                                                   rmax(PA.z, rmax(PB.z, PC.z)));
+                            if (lo.x > tool.uhi.x || lo.y > tool.uhi.y || lo.z > tool.uhi.z || hi.x < tool.ulo.x ||
+                                hi.y < tool.ulo.y || hi.z < tool.ulo.z)
+                                continue;
+                            unsigned near = 0;
+                            for (int i = 0; i < 3; ++i) {
+                                bool apart = lo.x > tool.bhi[i].x || lo.y > tool.bhi[i].y || lo.z > tool.bhi[i].z ||
+                                             hi.x < tool.blo[i].x || hi.y < tool.blo[i].y || hi.z < tool.blo[i].z;
+                                if (!apart) near |= 1u << i;
+                            }
+                            if (!near) continue;
+                            const int k = atomicAdd(&s_near_n, 1);
+                            if (k < kNearCap) s_near[k] = ((unsigned)f << 3) | near;
+                            else contact(a, b, c, PA, PB, PC, near);
+                        }
+                        __syncthreads();
+                        const int nnear = min(s_near_n, kNearCap);
+                        for (int k = tid; k < nnear; k += BLOCK) {
+                            const unsigned w = s_near[k];
+                            const uint2 tr = __ldg(D.tri_idx + (long long)E.f0 + (w >> 3));
+                            const int a = tr.x & 0xffff, b = tr.x >> 16, c = tr.y & 0xffff;
+                            contact(a, b, c, xp[a], xp[b], xp[c], w & 7u);
                         }
                         __syncthreads();
                         if (s_any_contact) {
