@@ -305,6 +305,17 @@ template <class R> struct ToolShared {
 // << 3 | capsule mask); more than this are solved by the thread that found them
 constexpr int kNearCap = 512;
 
+// Dynamic shared memory of a block: its env state (positions and inverse masses, the
+// accumulators and counts in MODE 0) for up to max_nv vertices, then the grasp bits; a
+// class may add its envs' surface triangles behind that (8-byte aligned)
+template <class R> __host__ __device__ size_t smem_bytes(int mode, int max_nv) {
+    size_t P = sizeof(typename Store<R>::P), A = sizeof(typename Store<R>::A);
+    size_t bits = 4 * (size_t)((max_nv + 31) / 32 + 1);
+    if (mode == 0) return (P + 3 * A + 4) * (size_t)max_nv + bits;
+    if (mode == 1) return P * (size_t)max_nv + bits;
+    return bits;
+}
+
 // MODE 0: positions and accumulators in shared memory.  MODE 1: positions in shared
 // memory, accumulators in the block's global scratch.  MODE 2: both in global scratch.
 // PIPE: the tet loop holds the thread's next tet record in registers, loaded while the
@@ -312,7 +323,8 @@ constexpr int kNearCap = 512;
 template <class R, int BLOCK, int MODE, bool PIPE = false>
 __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_batched(const Dev<R> D, const int* __restrict__ work, int nwork,
                                                    int* counter, int nsteps, unsigned char* scratch,
-                                                   long long scratch_stride, int max_nv, int prefetch) {
+                                                   long long scratch_stride, int max_nv, int prefetch,
+                                                   int tri_cap) {
     typedef Store<R> S;
     typedef typename S::P P;
     typedef typename S::A A;
@@ -410,6 +422,12 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
                     if (word) s_any_drag = 1;
                 }
             }
+        }
+        // the env's surface triangles, when the class keeps them in shared memory
+        uint2* tri_s = nullptr;
+        if (tri_cap) {
+            tri_s = reinterpret_cast<uint2*>(smem + ((smem_bytes<R>(MODE, max_nv) + 7) & ~(size_t)7));
+            for (int f = tid; f < nf; f += BLOCK) tri_s[f] = __ldg(D.tri_idx + (long long)E.f0 + f);
         }
         // inverse masses ride in .w for the whole step
         for (int i = tid; i < nv; i += BLOCK) {
@@ -662,7 +680,7 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
                             if (PC.w > R(0)) add3<R>(acc, c, tC, bad, fx);
                         };
                         for (int f = tid; f < nf; f += BLOCK) {
-                            const uint2 tr = __ldg(D.tri_idx + (long long)E.f0 + f);
+                            const uint2 tr = tri_s ? tri_s[f] : __ldg(D.tri_idx + (long long)E.f0 + f);
                             if ((tr.y >> 16) == 1u) continue;
                             const int a = tr.x & 0xffff, b = tr.x >> 16, c = tr.y & 0xffff;
                             const P PA = xp[a], PB = xp[b], PC = xp[c];
@@ -688,7 +706,7 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
                         const int nnear = min(s_near_n, kNearCap);
                         for (int k = tid; k < nnear; k += BLOCK) {
                             const unsigned w = s_near[k];
-                            const uint2 tr = __ldg(D.tri_idx + (long long)E.f0 + (w >> 3));
+                            const uint2 tr = tri_s ? tri_s[w >> 3] : __ldg(D.tri_idx + (long long)E.f0 + (w >> 3));
                             const int a = tr.x & 0xffff, b = tr.x >> 16, c = tr.y & 0xffff;
                             contact(a, b, c, xp[a], xp[b], xp[c], w & 7u);
                         }
@@ -730,13 +748,6 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
     }
 }
 
-template <class R> size_t smem_bytes(int mode, int max_nv) {
-    size_t P = sizeof(typename Store<R>::P), A = sizeof(typename Store<R>::A);
-    size_t bits = 4 * (size_t)((max_nv + 31) / 32 + 1);
-    if (mode == 0) return (P + 3 * A + 4) * (size_t)max_nv + bits;
-    if (mode == 1) return P * (size_t)max_nv + bits;
-    return bits;
-}
 template <class R> size_t scratch_bytes(int mode, int max_nv) {
     size_t P = sizeof(typename Store<R>::P), A = sizeof(typename Store<R>::A);
     if (mode == 0) return 0;
@@ -744,8 +755,8 @@ template <class R> size_t scratch_bytes(int mode, int max_nv) {
     return (P + 3 * A + 4) * (size_t)max_nv;
 }
 
-typedef void (*kern_f)(const Dev<float>, const int*, int, int*, int, unsigned char*, long long, int, int);
-typedef void (*kern_d)(const Dev<double>, const int*, int, int*, int, unsigned char*, long long, int, int);
+typedef void (*kern_f)(const Dev<float>, const int*, int, int*, int, unsigned char*, long long, int, int, int);
+typedef void (*kern_d)(const Dev<double>, const int*, int, int*, int, unsigned char*, long long, int, int, int);
 
 // prefetch 0: none, 1: L1 prefetch of the next record, 2: the next record held in
 // registers (PIPE instantiations only)
@@ -797,6 +808,7 @@ struct ffsrl_batch {
     struct Class {
         int mode, block, max_nv, grid, members;
         int prefetch = 0;  // L1 prefetch of the next tet record (autotuned)
+        int tri_cap = 0;   // surface triangles kept in shared memory per env (0: read from L2)
         size_t smem, scratch_stride, scratch_offset;
         int work_offset, work_count;
     };
@@ -897,7 +909,7 @@ template <> int32_t launch_class<float>(ffsrl_batch* b, const ffsrl_batch::Class
     int grid = std::min(c.grid, nwork);
     if (grid <= 0) return FFSRL_OK;
     k<<<grid, c.block, c.smem, s>>>(D, work, nwork, counter, nsteps, scratch + c.scratch_offset,
-                                    (long long)c.scratch_stride, c.max_nv, c.prefetch == 1 ? 1 : 0);
+                                    (long long)c.scratch_stride, c.max_nv, c.prefetch == 1 ? 1 : 0, c.tri_cap);
     FFSRL_LAUNCH_CHECK("ffsrl_batch: step kernel");
     return FFSRL_OK;
 }
@@ -924,7 +936,7 @@ template <> int32_t launch_class<double>(ffsrl_batch* b, const ffsrl_batch::Clas
     int grid = std::min(c.grid, nwork);
     if (grid <= 0) return FFSRL_OK;
     k<<<grid, c.block, c.smem, s>>>(D, work, nwork, counter, nsteps, scratch + c.scratch_offset,
-                                    (long long)c.scratch_stride, c.max_nv, c.prefetch == 1 ? 1 : 0);
+                                    (long long)c.scratch_stride, c.max_nv, c.prefetch == 1 ? 1 : 0, c.tri_cap);
     FFSRL_LAUNCH_CHECK("ffsrl_batch: float64 step kernel");
     return FFSRL_OK;
 }
@@ -1558,6 +1570,14 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
         c.max_nv = 1;
         for (int e : mem) c.max_nv = std::max(c.max_nv, env[e].nv);
         c.smem = precision == 64 ? smem_bytes<double>(c.mode, c.max_nv) : smem_bytes<float>(c.mode, c.max_nv);
+        if (p->flags & FFSRL_COLLIDE) {
+            // the contact scan reads every surface triangle in every iteration: keep the
+            // env's triangles in shared memory when they fit
+            int max_nf = 0;
+            for (int e : mem) max_nf = std::max(max_nf, env[e].nf);
+            const size_t with = ((c.smem + 7) & ~(size_t)7) + 8 * (size_t)max_nf;
+            if (max_nf > 0 && with <= dyn_budget) { c.tri_cap = max_nf; c.smem = with; }
+        }
         c.scratch_stride = precision == 64 ? scratch_bytes<double>(c.mode, c.max_nv) : scratch_bytes<float>(c.mode, c.max_nv);
         c.scratch_stride = (c.scratch_stride + 255) & ~(size_t)255;
         c.members = (int)mem.size();
