@@ -703,14 +703,16 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
                             else contact(a, b, c, PA, PB, PC, near);
                         }
                         __syncthreads();
-                        const int nnear = min(s_near_n, kNearCap);
-                        for (int k = tid; k < nnear; k += BLOCK) {
-                            const unsigned w = s_near[k];
-                            const uint2 tr = tri_s ? tri_s[w >> 3] : __ldg(D.tri_idx + (long long)E.f0 + (w >> 3));
-                            const int a = tr.x & 0xffff, b = tr.x >> 16, c = tr.y & 0xffff;
-                            contact(a, b, c, xp[a], xp[b], xp[c], w & 7u);
+                        const int nnear = min(s_near_n, kNearCap);  // the same for every thread
+                        if (nnear > 0) {
+                            for (int k = tid; k < nnear; k += BLOCK) {
+                                const unsigned w = s_near[k];
+                                const uint2 tr = tri_s ? tri_s[w >> 3] : __ldg(D.tri_idx + (long long)E.f0 + (w >> 3));
+                                const int a = tr.x & 0xffff, b = tr.x >> 16, c = tr.y & 0xffff;
+                                contact(a, b, c, xp[a], xp[b], xp[c], w & 7u);
+                            }
+                            __syncthreads();
                         }
-                        __syncthreads();
                         if (s_any_contact) {
                             for (int i = tid; i < nv; i += BLOCK) {
                                 P q = xp[i];
