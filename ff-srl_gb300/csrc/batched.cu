@@ -320,7 +320,11 @@ template <class R> __host__ __device__ size_t smem_bytes(int mode, int max_nv) {
 // memory, accumulators in the block's global scratch.  MODE 2: both in global scratch.
 // PIPE: the tet loop holds the thread's next tet record in registers, loaded while the
 // current one is solved (for block sizes that leave the registers for it).
-template <class R, int BLOCK, int MODE, bool PIPE = false>
+// FL: the constraint selection fixed at compile time (0: read from the parameters); the
+// liver set (volume, distance, Neo-Hookean, grasp, contact) has its own instantiations.
+constexpr unsigned kLiverFlags = FFSRL_VOLUME | FFSRL_DISTANCE | FFSRL_NEOHOOKEAN | FFSRL_DRAG | FFSRL_COLLIDE;
+
+template <class R, int BLOCK, int MODE, bool PIPE = false, unsigned FL = 0>
 __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_batched(const Dev<R> D, const int* __restrict__ work, int nwork,
                                                    int* counter, int nsteps, unsigned char* scratch,
                                                    long long scratch_stride, int max_nv, int prefetch,
@@ -342,7 +346,7 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
     unsigned char* gbase = scratch + (long long)blockIdx.x * scratch_stride;
     const int tid = threadIdx.x;
     const R dt = R(D.dt);
-    const unsigned fl = D.flags;
+    const unsigned fl = FL ? FL : D.flags;
     const Fixed fx = D.fx;
     const R sc = S::prescale(fx);  // power of two: scaling a product by it is exact
     // Neo-Hookean constants, hoisted with the reference's association order:
@@ -762,7 +766,14 @@ typedef void (*kern_d)(const Dev<double>, const int*, int, int*, int, unsigned c
 
 // prefetch 0: none, 1: L1 prefetch of the next record, 2: the next record held in
 // registers (PIPE instantiations only)
-kern_f pick_f(int block, int mode, int prefetch = 0) {
+kern_f pick_f(int block, int mode, int prefetch = 0, unsigned flags = 0) {
+    if (flags == kLiverFlags && mode == 0 && prefetch != 2) {
+        if (block == 256) return k_batched<float, 256, 0, false, kLiverFlags>;
+        if (block == 512) return k_batched<float, 512, 0, false, kLiverFlags>;
+        if (block == 640) return k_batched<float, 640, 0, false, kLiverFlags>;
+        if (block == 768) return k_batched<float, 768, 0, false, kLiverFlags>;
+        if (block == 1024) return k_batched<float, 1024, 0, false, kLiverFlags>;
+    }
     if (prefetch == 2) {
         if (mode == 0 && block == 512) return k_batched<float, 512, 0, true>;
         if (mode == 0 && block == 640) return k_batched<float, 640, 0, true>;
@@ -905,7 +916,7 @@ Dev<float> make_dev_f(ffsrl_batch* b) {
 
 template <> int32_t launch_class<float>(ffsrl_batch* b, const ffsrl_batch::Class& c, const int* work, int nwork,
                                         int* counter, unsigned char* scratch, int nsteps, cudaStream_t s) {
-    kern_f k = pick_f(c.block, c.mode, c.prefetch);
+    kern_f k = pick_f(c.block, c.mode, c.prefetch, b->params.flags);
     if (!k) return fail(FFSRL_ERR_UNSUPPORTED, "ffsrl_batch: no kernel for block/mode");
     Dev<float> D = make_dev_f(b);
     int grid = std::min(c.grid, nwork);
@@ -1024,7 +1035,7 @@ int32_t configure_class(ffsrl_batch* b, ffsrl_batch::Class& c, int block, size_t
     if (c.mode == 1 && block < 256) block = 256;
     if (c.mode == 2 && block > 512) block = 512;
     const void* kfn = b->precision == 64 ? (const void*)pick_d(block, c.mode)
-                                         : (const void*)pick_f(block, c.mode, c.prefetch);
+                                         : (const void*)pick_f(block, c.mode, c.prefetch, b->params.flags);
     if (!kfn) return fail(FFSRL_ERR_UNSUPPORTED, "ffsrl_batch: no kernel for block " + std::to_string(block) +
                                                      " in mode " + std::to_string(c.mode));
     if (c.smem > 48 * 1024) {
