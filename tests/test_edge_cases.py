@@ -57,7 +57,7 @@ def test_env_too_large_for_the_batched_step(gpu, oracle_lib):
     m = SimModelDO(big, 1, "cuda:0", simSubsteps=1, simConstraintsSteps=1, environmentGroundLevel=-100.0)
     with pytest.raises(L.FFSRLError) as err:
         SimIntegratorDO("cuda:0").stepModel(m)
-    assert err.value.code == L.ERR_INVALID_ARGUMENT
+    assert err.value.code == L.ERR_UNSUPPORTED
     o = oracle.OracleSim(m)
     SimIntegratorDO("cuda:0", batched=False).stepModel(m)
     o.step(1)
