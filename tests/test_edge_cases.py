@@ -72,7 +72,10 @@ def test_zero_steps_and_unreachable_grasp(gpu):
     SimIntegratorDO("cuda:0").stepModel(m, 0)
     torch.cuda.synchronize()
     assert torch.equal(m.vertex, x0)
-    # the drag point is parked 10 cm above the beam: nothing within 0.5 cm is grasped
+    # the instrument lifted 50 cm clear of the beam: nothing within 0.5 cm of the drag point
+    lift = torch.zeros((2, 3), device="cuda:0")
+    lift[:, 1] = 50.0
+    m.moveTool(lift)
     m.graspNearest(torch.ones(2, dtype=torch.int32, device="cuda:0"), radius=0.5)
     torch.cuda.synchronize()
     assert not m.activeDragConstraint.any()
