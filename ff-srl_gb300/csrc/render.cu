@@ -485,7 +485,9 @@ __global__ void k_downsample(ffsrl_render r) {
 
 // One thread per ray; the four rays of a pixel sit in consecutive lanes and are summed
 // by shuffles in downsample_kernel's order ((r00 + r01) + r10) + r11, then divided by 4.
-// A block covers an 8x8 pixel tile of one env so neighbouring rays share BVH nodes in L1.
+// A block covers an 8x8 pixel tile of one env so neighbouring rays share BVH nodes in L1,
+// and a warp's rays cover a compact 4x2-pixel patch (3% faster than a row of 8 pixels:
+// closer rays take more of the same nodes).
 __global__ void __launch_bounds__(256) k_rays(ffsrl_render r, ffsrl_bvh b, const int* __restrict__ ids, int n_ids) {
     const int R = r.resolution, W = 2 * R, H = 2 * R;
     const int tiles_x = (R + 7) / 8;
@@ -494,8 +496,10 @@ __global__ void __launch_bounds__(256) k_rays(ffsrl_render r, ffsrl_bvh b, const
     const int e = ids ? (k < n_ids ? ids[k] : r.num_envs) : k;
     const int tile = blockIdx.x % tiles;
     const int pix = threadIdx.x >> 2, q = threadIdx.x & 3;
-    const int px = (tile % tiles_x) * 8 + (pix & 7);
-    const int py = (tile / tiles_x) * 8 + (pix >> 3);
+    // a warp's eight pixels form a 4x2 patch; the tile's eight warps form 2x4 patches
+    const int wp = pix >> 3, j = pix & 7;
+    const int px = (tile % tiles_x) * 8 + (wp & 1) * 4 + (j & 3);
+    const int py = (tile / tiles_x) * 8 + (wp >> 1) * 2 + (j >> 2);
     const bool valid = e >= 0 && e < r.num_envs && px < R && py < R;
     Shade s;
     s.color = mk(0.0f, 0.0f, 0.0f);
