@@ -130,7 +130,7 @@ template <> struct Store<double> {
 // v0/nv: the env's vertices in the model arrays; t0/e0/f0: its constraint tables, which
 // envs with identical tables share; mt0/me0: its tets/edges in the model arrays (for the
 // XPBD multipliers, which are per env)
-struct EnvRec { int v0, nv, t0, nt, e0, ne, f0, nf, mt0, me0; };
+struct EnvRec { int v0, nv, t0, nt, e0, ne, f0, nf, mt0, me0, c0, nc; };
 
 template <class R> __device__ __forceinline__ R abs_sum(t3<R> d) { return fabs(d.x) + fabs(d.y) + fabs(d.z); }
 
@@ -183,6 +183,12 @@ template <class R> struct Dev {
     const float4* tet_ed;      // distance constraints solved by the tet: (L0 of A-B, active, +-L0, active);
                                // the second is C-D for +L0 and A-C for -L0; active 0 = none
     int fold;                  // distance constraints folded into the tet records
+    const uint2* conn_idx;     // connectors: (point | triangle a << 16, b | c << 16), env-local ids
+    const float4* conn_bar;    // (barycentric 0, 1, 2, rest distance)
+    const unsigned char* conn_vert;  // per vertex (global id): 1 when a connector holds it
+    int* pend;                 // [3V] connector corrections waiting for the next apply (fixed point)
+    int* pcnt;                 // [V] their counts
+    float conn_w, conn_ks, conn_mul;  // mass weight ratio, kS, rest length multiplier
     const int* tet_orig;       // env-local model tet id of each (colour-ordered) record, for XPBD lambdas
     const int* edge_orig;      // env-local model edge id of each record
     Fixed fx;
@@ -347,6 +353,7 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
     const int tid = threadIdx.x;
     const R dt = R(D.dt);
     const unsigned fl = FL ? FL : D.flags;
+    const bool has_conn = (fl & FFSRL_CONNECTORS) && D.conn_idx != nullptr;
     const Fixed fx = D.fx;
     const R sc = S::prescale(fx);  // power of two: scaling a product by it is exact
     // Neo-Hookean constants, hoisted with the reference's association order:
@@ -640,10 +647,19 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
                         int c = cnt[i];
                         P q = xp[i];
                         t3<R> x = S::pos(q);
+                        A s0 = acc[3 * i], s1 = acc[3 * i + 1], s2 = acc[3 * i + 2];
+                        if (has_conn && D.conn_vert[E.v0 + i]) {
+                            // the connector corrections of the previous iteration (or step) join
+                            // this apply, as the reference's persistent dP does
+                            const long long g = (long long)E.v0 + i;
+                            c += D.pcnt[g];
+                            s0 += A(D.pend[3 * g]); s1 += A(D.pend[3 * g + 1]); s2 += A(D.pend[3 * g + 2]);
+                            D.pcnt[g] = 0;
+                            D.pend[3 * g] = 0; D.pend[3 * g + 1] = 0; D.pend[3 * g + 2] = 0;
+                        }
                         if (c > 0) {
                             const R rN = rcp(R(c));
-                            x = x + T3<R>(S::get(acc[3 * i], fx) * rN, S::get(acc[3 * i + 1], fx) * rN,
-                                          S::get(acc[3 * i + 2], fx) * rN);
+                            x = x + T3<R>(S::get(s0, fx) * rN, S::get(s1, fx) * rN, S::get(s2, fx) * rN);
                             acc[3 * i] = A(0); acc[3 * i + 1] = A(0); acc[3 * i + 2] = A(0);
                         }
                         if (restore) cnt[i] = __ldg(D.cnt0 + E.v0 + i);
@@ -656,6 +672,31 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
                         xp[i] = S::make(x, q.w);
                     }
                     __syncthreads();
+                    // ---- triToPointDistanceConstraintsDO (integrator.py:300-353): corrections for the
+                    // next apply, from the positions after the grasp (before the contact) ----
+                    if (has_conn && E.nc > 0) {
+                        for (int k = tid; k < E.nc; k += BLOCK) {
+                            const uint2 ci = __ldg(D.conn_idx + E.c0 + k);
+                            const float4 cb = __ldg(D.conn_bar + E.c0 + k);
+                            const int v = ci.x & 0xffff, ta = ci.x >> 16, tb = ci.y & 0xffff, tc = ci.y >> 16;
+                            const t3<R> bar = T3<R>(R(cb.x), R(cb.y), R(cb.z));
+                            const t3<R> centre = S::pos(xp[ta]) * bar.x + S::pos(xp[tb]) * bar.y + S::pos(xp[tc]) * bar.z;
+                            const t3<R> dir = S::pos(xp[v]) - centre;
+                            const R len = length(dir);
+                            if (len < R(BEPS)) continue;
+                            const R wp = R(D.conn_w), wt = R(1) - wp;
+                            const R Cc = len - R(cb.w) * R(D.conn_mul);
+                            const R sden = wp + wt * (bar.x * bar.x + bar.y * bar.y + bar.z * bar.z);
+                            const t3<R> delta = (Cc / sden) * (dir / len) * R(D.conn_ks);
+                            A* pend = reinterpret_cast<A*>(D.pend);
+                            add3<R>(pend, E.v0 + v, -(delta * wp), bad, fx);
+                            add3<R>(pend, E.v0 + ta, delta * wt * bar.x, bad, fx);
+                            add3<R>(pend, E.v0 + tb, delta * wt * bar.y, bad, fx);
+                            add3<R>(pend, E.v0 + tc, delta * wt * bar.z, bad, fx);
+                            atomicAdd(D.pcnt + E.v0 + v, 1); atomicAdd(D.pcnt + E.v0 + ta, 1);
+                            atomicAdd(D.pcnt + E.v0 + tb, 1); atomicAdd(D.pcnt + E.v0 + tc, 1);
+                        }
+                    }
                     // ---- collideLaparoscopeDO (integrator.py:981-1050), positions as of phase start ----
                     // A scan tests every surface triangle's box against the capsules' boxes (their
                     // union first) and lists the near ones; the block then solves the listed
@@ -814,6 +855,8 @@ struct ffsrl_batch {
     int* d_cnt0 = nullptr;        // static per-vertex contribution counts
     int* d_tet_orig = nullptr;    // record -> model tet id
     int* d_edge_orig = nullptr;   // record -> model edge id
+    uint2* d_conn_idx = nullptr; float4* d_conn_bar = nullptr; unsigned char* d_conn_vert = nullptr;
+    int* d_pend = nullptr; int* d_pcnt = nullptr;  // pending connector corrections, kept between steps
     Fixed fx{1.0f, 1.0f, 1.0f};
     int64_t device_bytes = 0;
     size_t dyn_budget = 0;
@@ -867,6 +910,7 @@ void free_batch(ffsrl_batch* b) {
     cudaFree(b->d_work); cudaFree(b->d_status); cudaFree(b->d_scratch);
     cudaFree(b->d_state64); cudaFree(b->d_cnt0); cudaFree(b->d_tet_orig);
     cudaFree(b->d_edge_orig);
+    cudaFree(b->d_conn_idx); cudaFree(b->d_conn_bar); cudaFree(b->d_conn_vert); cudaFree(b->d_pend); cudaFree(b->d_pcnt);
     for (auto& l : b->lanes) {
         for (auto s : l.streams) if (s) cudaStreamDestroy(s);
         for (auto e : l.done) if (e) cudaEventDestroy(e);
@@ -904,6 +948,9 @@ Dev<float> make_dev_f(ffsrl_batch* b) {
     D.env_status = b->d_status;
     D.cnt0 = b->d_cnt0; D.tet_orig = b->d_tet_orig; D.edge_orig = b->d_edge_orig; D.fx = b->fx;
     D.tet_ed = b->d_tet_ed; D.fold = b->d_tet_ed != nullptr;
+    D.conn_idx = b->d_conn_idx; D.conn_bar = b->d_conn_bar; D.conn_vert = b->d_conn_vert;
+    D.pend = b->d_pend; D.pcnt = b->d_pcnt;
+    D.conn_w = p.connector_mass_weight_ratio; D.conn_ks = p.connector_ks; D.conn_mul = p.connector_rest_length_mul;
     D.flags = p.flags; D.substeps = p.substeps; D.iterations = p.iterations;
     D.dt = p.dt; D.gx = p.gravity[0]; D.gy = p.gravity[1]; D.gz = p.gravity[2];
     D.damping = p.velocity_dampening; D.ground = p.ground_level;
@@ -1062,15 +1109,17 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
     const int N = hm->num_envs;
     if (N <= 0 || !hm->env_vertex_start || !hm->env_tet_start || !hm->env_edge_start || !hm->env_tri_start)
         return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_create: host env ranges required");
-    if ((p->flags & FFSRL_CONNECTORS) && hm->num_connectors > 0)
-        return fail(FFSRL_ERR_UNSUPPORTED,
-                    "ffsrl_batch_create: connectors are not part of the batched step; run them with ffsrl_step_model");
     int precision = 32;
     int block_override = 0;
     if (opts) {
         block_override = opts->block_threads;
         if (opts->reserved[0] == 64) precision = 64;
     }
+    const bool conn = (p->flags & FFSRL_CONNECTORS) && hm->num_connectors > 0;
+    if (conn && (precision == 64 || !hm->connector_vertex_id || !hm->connector_triangle_id ||
+                 !hm->connector_tri_bar || !hm->connector_rest_dist))
+        return fail(FFSRL_ERR_UNSUPPORTED, "ffsrl_batch_create: connectors need the float32 step and all four "
+                                           "connector arrays");
     ffsrl_batch* b = new ffsrl_batch();
     b->num_envs = N;
     b->params = *p;
@@ -1231,6 +1280,60 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
     for (int64_t f = 0; f < F; ++f)
         for (int k = 0; k < 3; ++k) tri_deg[hm->triangle[3 * f + k]] += 1;
     int max_terms = 1;
+    // ---- connectors (triToPointDistanceConstraintsDO): each belongs to the env of its
+    // point, and all four of its vertices must lie in that env ----
+    std::vector<uint2> conn_idx;
+    std::vector<float4> conn_bar;
+    std::vector<unsigned char> conn_vert;
+    if (conn) {
+        const int64_t C = hm->num_connectors;
+        std::vector<std::vector<int>> per(N);
+        auto env_of = [&](int g) {
+            int lo = 0, hi = N - 1;
+            while (lo < hi) {
+                int mid = (lo + hi + 1) / 2;
+                if (hm->env_vertex_start[mid] <= g) lo = mid; else hi = mid - 1;
+            }
+            return lo;
+        };
+        for (int64_t c = 0; c < C; ++c) {
+            const int g[4] = {hm->connector_vertex_id[c], hm->connector_triangle_id[3 * c],
+                              hm->connector_triangle_id[3 * c + 1], hm->connector_triangle_id[3 * c + 2]};
+            for (int k = 0; k < 4; ++k)
+                if (g[k] < 0 || g[k] >= V) {
+                    free_batch(b);
+                    return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_batch_create: connector vertex id out of range");
+                }
+            const int e = env_of(g[0]);
+            for (int k = 1; k < 4; ++k)
+                if (env_of(g[k]) != e) {
+                    free_batch(b);
+                    return fail(FFSRL_ERR_UNSUPPORTED, "ffsrl_batch_create: connector " + std::to_string(c) +
+                                                           " joins two environments");
+                }
+            per[e].push_back((int)c);
+        }
+        conn_vert.assign(V, 0);
+        for (int e = 0; e < N; ++e) {
+            env[e].c0 = (int)conn_idx.size();
+            env[e].nc = (int)per[e].size();
+            const int v0 = env[e].v0;
+            for (int c : per[e]) {
+                const int g[4] = {hm->connector_vertex_id[c], hm->connector_triangle_id[3ll * c],
+                                  hm->connector_triangle_id[3ll * c + 1], hm->connector_triangle_id[3ll * c + 2]};
+                for (int k = 0; k < 4; ++k) conn_vert[g[k]] = 1;
+                conn_idx.push_back(make_uint2((unsigned)(g[0] - v0) | ((unsigned)(g[1] - v0) << 16),
+                                              (unsigned)(g[2] - v0) | ((unsigned)(g[3] - v0) << 16)));
+                conn_bar.push_back(make_float4(hm->connector_tri_bar[3ll * c], hm->connector_tri_bar[3ll * c + 1],
+                                               hm->connector_tri_bar[3ll * c + 2], hm->connector_rest_dist[c]));
+            }
+        }
+        // a connector adds one term to each of its vertices' sums
+        for (int64_t c = 0; c < C; ++c) {
+            tri_deg[hm->connector_vertex_id[c]] += 1;
+            for (int k = 0; k < 3; ++k) tri_deg[hm->connector_triangle_id[3 * c + k]] += 1;
+        }
+    }
     for (int64_t v = 0; v < V; ++v) max_terms = std::max(max_terms, cnt0[v] + tri_deg[v]);
 
     // ---- fixed-point scale: one unit ~ a quarter float ulp of the largest coordinate ----
@@ -1619,6 +1722,10 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
         (st = dalloc(b, &b->d_edge_idx, edge_idx.size())) || (st = upload(b->d_edge_idx, edge_idx)) ||
         (st = dalloc(b, &b->d_edge_la, edge_la.size())) || (st = upload(b->d_edge_la, edge_la)) ||
         (st = dalloc(b, &b->d_tri_idx, tri_idx.size())) || (st = upload(b->d_tri_idx, tri_idx)) ||
+        (st = dalloc(b, &b->d_conn_idx, conn_idx.size())) || (st = upload(b->d_conn_idx, conn_idx)) ||
+        (st = dalloc(b, &b->d_conn_bar, conn_bar.size())) || (st = upload(b->d_conn_bar, conn_bar)) ||
+        (st = dalloc(b, &b->d_conn_vert, conn_vert.size())) || (st = upload(b->d_conn_vert, conn_vert)) ||
+        (st = dalloc(b, &b->d_pend, conn ? 3 * (size_t)V : 0)) || (st = dalloc(b, &b->d_pcnt, conn ? (size_t)V : 0)) ||
         (st = dalloc(b, &b->d_work, (size_t)N)) || (st = upload(b->d_work, b->work_host)) ||
         (st = dalloc(b, &b->d_status, (size_t)N)) ||
         (st = dalloc(b, &b->d_scratch, scratch_total * kLanes))) {
@@ -1626,6 +1733,10 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
         return st;
     }
     FFSRL_CUDA_TRY(cudaMemset(b->d_status, 0, sizeof(int) * N));
+    if (conn) {
+        FFSRL_CUDA_TRY(cudaMemset(b->d_pend, 0, sizeof(int) * 3 * (size_t)V));
+        FFSRL_CUDA_TRY(cudaMemset(b->d_pcnt, 0, sizeof(int) * (size_t)V));
+    }
     if (precision == 64) {
         if ((st = dalloc(b, &b->d_state64, 9 * (size_t)V))) { free_batch(b); return st; }
         // double state initialised from the model's float state

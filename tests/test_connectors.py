@@ -1,6 +1,6 @@
 """Connectors (triToPointDistanceConstraintsDO, integrator.py:300-353; SimConnectorDO,
 modelDO.py:723-770, 977-1015): a known answer of the oracle, the model's global ids, the
-scene-file prims, and the reference-shaped GPU step against the oracle."""
+scene-file prims, and the reference-shaped and batched GPU steps against the oracle."""
 
 import numpy as np
 import pytest
@@ -76,23 +76,27 @@ def test_scene_file_connectors(tmp_path):
 
 
 @pytest.mark.gpu
-def test_connectors_reference_step_matches_oracle(gpu, oracle_lib):
+@pytest.mark.parametrize("batched", [False, True])
+def test_connectors_step_matches_oracle(gpu, oracle_lib, batched):
     import torch
     body = _connected()
     kw = dict(constraints=L.REFERENCE_STEP, simSubsteps=4, simConstraintsSteps=5, environmentGroundLevel=-100.0,
               environmentGravity=mg.gravity_force(body))
-    m = SimModelDO(body, 3, "cuda:0", **kw)
+    m = SimModelDO([body, mg.beam(4, 2, 2), body], 3, "cuda:0", **kw)
     o = oracle.OracleSim(m)
-    integ = SimIntegratorDO("cuda:0", batched=False)
-    integ.stepModel(m, 3)
-    o.step(3)
+    integ = SimIntegratorDO("cuda:0", batched=batched)
+    for _ in range(3):  # separate calls: the pending corrections carry over between steps
+        integ.stepModel(m, 1)
+        o.step(1)
     torch.cuda.synchronize()
     x = m.vertex.cpu().numpy()
     e = np.abs(x - o.a["vertex"]).max() / np.abs(o.a["vertex"]).max()
-    print(f"[connectors] reference-shaped step vs oracle, 3 steps: {e:.2e}")
+    print(f"[connectors] batched={batched} step vs oracle, 3 steps: {e:.2e}")
     assert e < 1e-4
-    # the connector terms waiting for the next step match too
-    assert np.array_equal(m.constraintsNumber.cpu().numpy(), o.a["constraints_number"])
-    # the batched step does not take connectors and says so
-    with pytest.raises(L.FFSRLError):
-        SimIntegratorDO("cuda:0").stepModel(m)
+    if not batched:  # the reference-shaped step keeps them in the model's dP and counts
+        assert np.array_equal(m.constraintsNumber.cpu().numpy(), o.a["constraints_number"])
+    # without the connectors the bodies move differently: the test sees them
+    free = SimModelDO([body, mg.beam(4, 2, 2), body], 3, "cuda:0", **(kw | {"constraints": L.REFERENCE_STEP & ~L.CONNECTORS}))
+    SimIntegratorDO("cuda:0", batched=batched).stepModel(free, 3)
+    torch.cuda.synchronize()
+    assert np.abs(free.vertex.cpu().numpy() - x).max() > 100 * np.abs(x - o.a["vertex"]).max()
