@@ -550,6 +550,8 @@ class SimModelDO:
             "laparoscope_in_collision": self.laparoscopeInCollision.cpu().numpy().copy(),
             "env_vertex_start": self.envVertexStart, "env_tet_start": self.envTetStart,
             "env_edge_start": self.envEdgeStart, "env_tri_start": self.envTriStart,
+            "connector_triangle_id": h["connectorTriangleId"], "connector_tri_bar": h["connectorTriBar"],
+            "connector_vertex_id": h["connectorVertexId"], "connector_rest_dist": h["connectorRestDist"],
         }
         return self._fill(_lib.Model(), arrs), arrs
 
