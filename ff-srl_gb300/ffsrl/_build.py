@@ -30,6 +30,7 @@ UNITS = {
     "batched.cu": ["-prec-div=false", "-prec-sqrt=false"],
     "render.cu": ["-fmad=false"],
     "instrument.cu": ["-fmad=false"],
+    "cutting.cu": ["-fmad=false"],
     "bvh_build.cpp": [],
 }
 

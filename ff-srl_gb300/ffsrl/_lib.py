@@ -157,6 +157,15 @@ def lib() -> C.CDLL:
         "ffsrl_batch_class_envs": ([P, I32, P], I32),
         "ffsrl_batch_set_class_block": ([P, I32, I32], I32),
         "ffsrl_batch_set_class_prefetch": ([P, I32, I32], I32),
+        "ffsrl_edge_breaker": ([P, P, P, P, P, I32, F32, F32, P], I32),
+        "ffsrl_check_edge_breaker": ([P, P, P, P, I32, P, I32, P, P, P, P, F32, P, P, P], I32),
+        "ffsrl_tetrahedron_breaker": ([P, P, P, P, P, I32, F32, P], I32),
+        "ffsrl_heat_propagation": ([P, P, P, P, I32, F32, F32, F32, P], I32),
+        "ffsrl_heat_update": ([P, P, P, P, P, P, I32, I32, P], I32),
+        "ffsrl_check_heat": ([P, P, P, P, P, F32, I32, P], I32),
+        "ffsrl_heat_laparoscope": ([P, P, P, P, P, P, P, F32, F32, I32, P], I32),
+        "ffsrl_cut_edges": ([P, P, P, P, P, I32, P, I32, P, P, P, P, P, P, P], I32),
+        "ffsrl_update_active_values": ([P, P, P, I32, I32, P], I32),
     }
     for name, (args, ret) in sig.items():
         f = getattr(L, name)

@@ -11,6 +11,11 @@ capture; make a new ``Graph`` after changing them.  Everything the library launc
 to the current stream, which is the capture stream during the capture, so its calls
 record with no change; anything that must run before the first capture (plan building,
 autotuning, kernel attributes) is done by ``prepare``.
+
+A graph holds a reference to every batched-step plan its capture launched, so a plan
+the integrator replaces (after cutting changes the model's active values or holes) stays
+allocated while an older graph can still replay it; such a graph steps the topology it
+was captured with until it is made again.
 """
 
 from __future__ import annotations
@@ -19,12 +24,21 @@ from typing import Callable
 
 import torch
 
+_capturing: list[list] = []
+
+
+def keep(obj) -> None:
+    """Tie ``obj`` (a plan a launch reads) to the graph being captured, if any."""
+    if _capturing:
+        _capturing[-1].append(obj)
+
 
 class Graph:
     def __init__(self, fn: Callable[[], None], prepare: Callable[[], None] | None = None):
         self.fn = fn
         self.prepare = prepare
         self.graph = None
+        self._kept: list = []
 
     def capture(self) -> None:
         if self.prepare is not None:
@@ -33,10 +47,16 @@ class Graph:
         g = torch.cuda.CUDAGraph()
         side = torch.cuda.Stream()
         side.wait_stream(torch.cuda.current_stream())
-        with torch.cuda.stream(side), torch.cuda.graph(g, stream=side):
-            self.fn()
+        kept: list = []
+        _capturing.append(kept)
+        try:
+            with torch.cuda.stream(side), torch.cuda.graph(g, stream=side):
+                self.fn()
+        finally:
+            _capturing.pop()
         torch.cuda.current_stream().wait_stream(side)
         self.graph = g
+        self._kept = kept
 
     def __call__(self) -> None:
         """Capture on the first call (which then replays once, so the call has its effect),
@@ -47,3 +67,4 @@ class Graph:
 
     def reset(self) -> None:
         self.graph = None
+        self._kept = []

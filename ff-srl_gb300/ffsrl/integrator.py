@@ -21,7 +21,7 @@ import ctypes as C
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, graphs
 from ._lib import check, lib, ptr
 
 
@@ -43,12 +43,15 @@ class BatchPlan:
         self.handle = h
         self.model = model
         self.precision = precision
+        self.version = getattr(model, "topologyVersion", 0)
         self._host_arrays = None  # the plan has copied what it needs
 
     def step(self, n_steps: int = 1, stream=None) -> None:
+        graphs.keep(self)
         check(lib().ffsrl_batch_step(self.handle, int(n_steps), _lib.stream_handle(stream)))
 
     def step_envs(self, env_ids, n_steps: int = 1, stream=None) -> None:
+        graphs.keep(self)
         ids = np.ascontiguousarray(np.asarray(env_ids, dtype=np.int32))
         check(lib().ffsrl_batch_step_envs(self.handle, ids.ctypes.data, int(ids.size), int(n_steps),
                                           _lib.stream_handle(stream)))
@@ -99,9 +102,12 @@ class SimIntegratorDO:
         self._graphs = {}
 
     def plan(self, simModel) -> BatchPlan:
+        """The model's batched plan, built on first use and rebuilt when the model's active
+        values or holes have changed since (``simModel.topologyVersion``, bumped by the
+        cutting and heating calls).  A rebuild starts with empty connector accumulators."""
         key = id(simModel)
         p = self._plans.get(key)
-        if p is None or p.model is not simModel:
+        if p is None or p.model is not simModel or p.version != simModel.topologyVersion:
             p = BatchPlan(simModel, self.blockThreads)
             self._plans[key] = p
             if self.autotune and self.blockThreads == 0:
@@ -119,9 +125,10 @@ class SimIntegratorDO:
             from .graphs import Graph
             key = (id(simModel), int(steps))
             g = self._graphs.get(key)
-            if g is None or g[0] is not simModel:
+            if g is None or g[0] is not simModel or g[2] != simModel.topologyVersion:
+                # a changed topology rebuilds the plan, so the graph holding the old one goes
                 prep = (lambda: self.plan(simModel)) if self.batched else None
-                g = (simModel, Graph(lambda: self._step(simModel, steps, None), prep))
+                g = (simModel, Graph(lambda: self._step(simModel, steps, None), prep), simModel.topologyVersion)
                 self._graphs[key] = g
             with torch.cuda.stream(stream) if stream is not None else contextlib.nullcontext():
                 g[1]()

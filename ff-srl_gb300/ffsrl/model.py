@@ -128,6 +128,9 @@ class SimModelDO:
         self._concatenate(meshes, toolRadius)
         self._upload()
         self._batch = None
+        # bumped by calls that change active values or holes (cutting, heating): the
+        # batched step's plan packs those and is rebuilt when this changes
+        self.topologyVersion = 0
         if scenes is not None and all(sc_.instrument is not None for sc_ in scenes):
             ins = [sc_.instrument for sc_ in scenes]
             base = np.concatenate([i["bases"] for i in ins]).astype(np.float32)

@@ -381,6 +381,82 @@ int32_t ffsrl_batch_state_f64(const ffsrl_batch* b, double* host_xvx);
 /* per-env status after a step: 0 ok, FFSRL_ERR_NONFINITE if the env's state went non-finite */
 int32_t ffsrl_batch_env_status(const ffsrl_batch* b, int32_t* host_status, int32_t num_envs);
 
+/* ---- cutting and heating (integrator.py:700-918, 1153-1185, 1406-1518, 1583-1605) ----
+   Library calls over the env-major arrays; the reference's DO step does not launch them.
+   One thread per element.  Element maps use -1 for "none" (no neighbour, no surface
+   triangle) and such entries are skipped.  Instrument points are the capsule tips
+   [3 * 4 * num_envs] (entry 4e+k of env e: k = 0 rod, 1 and 2 the clamps); an element's
+   env comes from an optional element -> env map (NULL: env 0, the reference's single
+   instrument).  An optional env_tet_start [num_envs + 1] with that map limits a tet scan
+   to the edge's env, which gives the result of the reference's scan over all tets. */
+/* edgeBreakerKernel (integrator.py:700-731): an edge with active_edge != 0, rest length
+   and current length both at least 2.22e-16, and stretch C = len / rest - 1 above
+   break_threshold adds (C - break_threshold) * break_factor to breaker_value[e]. */
+int32_t ffsrl_edge_breaker(const float* predicted, const int32_t* edge, const float* rest_length,
+                           const float* active_edge, float* breaker_value, int32_t num_edges, float break_factor,
+                           float break_threshold, void* stream);
+/* checkEdgeBreakerKernel (integrator.py:733-775): an edge whose breaker value exceeds
+   break_limit gets flip_edges[e] = -1 (if 0 and active == 1), opens the surface triangles
+   edge_to_triangles[2e], [2e+1] (holes[f] = 1) and, where some tet holds both its
+   vertices, sets flip_tets[e] = -1 if flip_tets[e] is 0 and active_tet[e] is 1.  The
+   reference indexes the tet flags by the EDGE id; edges with ids >= num_tets skip that
+   part. */
+int32_t ffsrl_check_edge_breaker(const float* breaker_value, const int32_t* edge, const float* active_edge,
+                                 int32_t* flip_edges, int32_t num_edges, const int32_t* tetrahedron, int32_t num_tets,
+                                 const float* active_tet, int32_t* flip_tets, const int32_t* edge_to_triangles,
+                                 int32_t* holes, float break_limit, const int32_t* edge_to_env,
+                                 const int32_t* env_tet_start, void* stream);
+/* tetrahedronBreaker (integrator.py:777-818): a tet with active == 1 whose signed volume
+   exceeds its rest volume adds (volume - rest) * break_factor to breaker_value[t].
+   tetrahedron is [4T] (the reference's four per-corner arrays interleaved). */
+int32_t ffsrl_tetrahedron_breaker(const float* predicted, const int32_t* tetrahedron, const float* rest_volume,
+                                  const float* active_tet, float* breaker_value, int32_t num_tets,
+                                  float break_factor, void* stream);
+/* tetrahedronHeatPropagation (integrator.py:820-847): for a tet with active != 0,
+   new_heat[t] = h (1 - loss) + transfer * sum over active neighbours n of (h_n - h) conduction.
+   neighbors is [4T], entry i the tet across the face opposite vertex i, or -1. */
+int32_t ffsrl_heat_propagation(const float* active_tet, const int32_t* neighbors, const float* heat,
+                               float* new_heat, int32_t num_tets, float conduction, float transfer, float loss,
+                               void* stream);
+/* tetrahedronHeatUpdate (integrator.py:849-872): heat[t] = new_heat[t] for active tets
+   (0 otherwise); each vertex of an active tet takes heat / 4 from the highest-id active
+   tet holding it, the last writer of a serial run.  owner_scratch is num_vertices ints
+   of device scratch. */
+int32_t ffsrl_heat_update(float* heat, const float* new_heat, const float* active_tet, const int32_t* tetrahedron,
+                          float* vertex_heat, int32_t* owner_scratch, int32_t num_tets, int32_t num_vertices,
+                          void* stream);
+/* checkTetrahedronHeat (integrator.py:874-895) with rest_volume NULL: heat > heat_limit
+   and flip_tets[t] == 0 set flip_tets[t] = -1 and open the tet's surface triangles
+   tet_to_triangles[4t..4t+3].  checkTetrahedronHeatVolumeProportional
+   (integrator.py:897-918) with rest_volume: heat > heat_limit * rest_volume[t] does the
+   same whatever flip_tets[t] was. */
+int32_t ffsrl_check_heat(const float* heat, int32_t* flip_tets, const float* rest_volume,
+                         const int32_t* tet_to_triangles, int32_t* holes, float heat_limit, int32_t num_tets,
+                         void* stream);
+/* heatLaparoscope (integrator.py:1153-1185): each surface triangle whose closest point to
+   the midpoint of its env's clamp tips (entries 4e+1, 4e+2) lies within sphere_radius adds
+   heat_quantum to its tet triangle_to_tet[f] if that tet is active. */
+int32_t ffsrl_heat_laparoscope(const int32_t* triangle, const float* positions, const float* active_tet, float* heat,
+                               const int32_t* triangle_to_tet, const float* capsule_tips,
+                               const int32_t* triangle_to_env, float sphere_radius, float heat_quantum,
+                               int32_t num_triangles, void* stream);
+/* findIntersectingEdges (integrator.py:1406-1458) with checkSegmentTriangleIntersection
+   (integrator.py:1471-1518): an edge crossing the triangle (rod tip, right clamp tip,
+   left clamp tip) of its env gets flip_edges[e] = -1 (if 0 and active == 1), opens its
+   surface triangles, and flips (-1) every tet holding both its vertices whose flag is 0
+   and whose active value is 1. */
+int32_t ffsrl_cut_edges(const float* positions, const float* capsule_tips, const int32_t* edge,
+                        const float* active_edge, int32_t* flip_edges, int32_t num_edges, const int32_t* tetrahedron,
+                        int32_t num_tets, const float* active_tet, int32_t* flip_tets,
+                        const int32_t* edge_to_triangles, int32_t* holes, const int32_t* edge_to_env,
+                        const int32_t* env_tet_start, void* stream);
+/* inDeCreaseActiveValues (integrator.py:1583-1605): element t with flip f != 0 takes
+   active = table[f] (f > 0, then f + 1) or table[steps + f] (f < 0, then f - 1), and
+   the counter returns to 0 once |f| >= steps.  table holds steps + 1 values (the
+   reference: sqrt(k / 5), k = 0..5).  Counters with |f| > steps are left alone. */
+int32_t ffsrl_update_active_values(int32_t* flip, float* active, const float* table, int32_t steps, int32_t n,
+                                   void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1109,4 +1109,171 @@ void oracle_instrument_visual(const float* xform, const float* local, const int*
     }
 }
 
+// ---- cutting and heating (integrator.py:700-918, 1153-1185, 1406-1518, 1583-1605),
+// serial in thread order.  Map entries of -1 are skipped (the reference would index with
+// them).  An element's env comes from the optional env map (env 0 without it, the
+// reference's single instrument); a tet scan for an edge visits every tet, as the
+// reference does.
+
+// edgeBreakerKernel (integrator.py:700-731)
+void oracle_edge_breaker(const float* xp, const int* edge, const float* rest, const float* active, float* value,
+                         int ne, float factor, float threshold) {
+    for (int t = 0; t < ne; ++t) {
+        if (active[t] == 0.0f) continue;
+        float L0 = rest[t];
+        if (L0 < float(kFloatEpsilon)) continue;
+        float len = length(ld3<float>(xp, edge[2 * t + 1]) - ld3<float>(xp, edge[2 * t]));
+        if (len < float(kFloatEpsilon)) continue;
+        float C = len / L0 - 1.0f;
+        if (C > threshold) value[t] = value[t] + (C - threshold) * factor;
+    }
+}
+
+static bool tet_holds(const int* q, int v) { return v == q[0] || v == q[1] || v == q[2] || v == q[3]; }
+
+// checkEdgeBreakerKernel (integrator.py:733-775); the tet flag indexed by the edge id is
+// the reference's, applied only where that id is a tet id
+void oracle_check_edge_breaker(const float* value, const int* edge, const float* active_edge, int* flip_edges, int ne,
+                               const int* tet, int nt, const float* active_tet, int* flip_tets, const int* edge_tris,
+                               int* holes, float limit) {
+    for (int t = 0; t < ne; ++t) {
+        if (!(value[t] > limit)) continue;
+        if (flip_edges[t] == 0 && active_edge[t] == 1.0f) flip_edges[t] = -1;
+        int a = edge[2 * t], b = edge[2 * t + 1];
+        for (int k = 0; k < 2; ++k)
+            if (edge_tris[2 * t + k] > -1) holes[edge_tris[2 * t + k]] = 1;
+        if (t >= nt) continue;
+        for (int i = 0; i < nt; ++i)
+            if (tet_holds(tet + 4 * i, a) && tet_holds(tet + 4 * i, b) && flip_tets[t] == 0 && active_tet[t] == 1.0f)
+                flip_tets[t] = -1;
+    }
+}
+
+// tetrahedronBreaker (integrator.py:777-818)
+void oracle_tetrahedron_breaker(const float* xp, const int* tet, const float* rest, const float* active, float* value,
+                                int nt, float factor) {
+    for (int t = 0; t < nt; ++t) {
+        if (!(active[t] == 1.0f)) continue;
+        V3<float> pa = ld3<float>(xp, tet[4 * t]);
+        V3<float> p1 = ld3<float>(xp, tet[4 * t + 1]) - pa, p2 = ld3<float>(xp, tet[4 * t + 2]) - pa,
+                  p3 = ld3<float>(xp, tet[4 * t + 3]) - pa;
+        float C = dot(cross(p1, p2), p3) / 6.0f - rest[t];
+        if (C > 0.0f) value[t] = value[t] + C * factor;
+    }
+}
+
+// tetrahedronHeatPropagation (integrator.py:820-847)
+void oracle_heat_propagation(const float* active, const int* nbr, const float* heat, float* new_heat, int nt,
+                             float conduction, float transfer, float loss) {
+    for (int t = 0; t < nt; ++t) {
+        if (active[t] == 0.0f) continue;
+        float h = heat[t], avg = 0.0f;
+        for (int i = 0; i < 4; ++i) {
+            int n = nbr[4 * t + i];
+            if (n > -1 && active[n] > 0.0f) avg = avg + (heat[n] - h) * conduction;
+        }
+        new_heat[t] = h * (1.0f - loss) + avg * transfer;
+    }
+}
+
+// tetrahedronHeatUpdate (integrator.py:849-872): a vertex keeps the last write, the
+// highest tet id holding it
+void oracle_heat_update(float* heat, const float* new_heat, const float* active, const int* tet, float* vertex_heat,
+                        int nt) {
+    for (int t = 0; t < nt; ++t) {
+        if (active[t] > 0.0f) {
+            float h = new_heat[t];
+            heat[t] = h;
+            for (int k = 0; k < 4; ++k) vertex_heat[tet[4 * t + k]] = h / 4.0f;
+        } else {
+            heat[t] = 0.0f;
+        }
+    }
+}
+
+// checkTetrahedronHeat (integrator.py:874-895), or with rest volumes
+// checkTetrahedronHeatVolumeProportional (integrator.py:897-918)
+void oracle_check_heat(const float* heat, int* flip, const float* rest, const int* tet_tris, int* holes, float limit,
+                       int nt) {
+    for (int t = 0; t < nt; ++t) {
+        bool hot = rest ? heat[t] > limit * rest[t] : heat[t] > limit;
+        if (!hot || (!rest && flip[t] != 0)) continue;
+        flip[t] = -1;
+        for (int i = 0; i < 4; ++i)
+            if (tet_tris[4 * t + i] > -1) holes[tet_tris[4 * t + i]] = 1;
+    }
+}
+
+// heatLaparoscope (integrator.py:1153-1185): a serial read-add-write per triangle
+void oracle_heat_laparoscope(const int* tri, const float* pos, const float* active, float* heat, const int* tri_tet,
+                             const float* tips, const int* tri_env, float radius, float quantum, int nf) {
+    for (int t = 0; t < nf; ++t) {
+        int e = tri_env ? tri_env[t] : 0;
+        V3<float> centre = (ld3<float>(tips, 4 * e + 1) + ld3<float>(tips, 4 * e + 2)) / 2.0f;
+        V3<float> a = ld3<float>(pos, tri[3 * t]), b = ld3<float>(pos, tri[3 * t + 1]), c = ld3<float>(pos, tri[3 * t + 2]);
+        V3<float> bary = closest_bary(a, b, c, centre);
+        V3<float> closest = a * bary.x + b * bary.y + c * bary.z;
+        if (length(closest - centre) < radius) {
+            int k = tri_tet[t];
+            if (k > -1 && active[k] > 0.0f) heat[k] = heat[k] + quantum;
+        }
+    }
+}
+
+// checkSegmentTriangleIntersection (integrator.py:1471-1518)
+int oracle_segment_triangle(const float* pA_, const float* pB_, const float* pC_, const float* sA_, const float* sB_) {
+    V3<float> pA = ld3<float>(pA_, 0), pB = ld3<float>(pB_, 0), pC = ld3<float>(pC_, 0);
+    V3<float> sA = ld3<float>(sA_, 0), sB = ld3<float>(sB_, 0);
+    V3<float> u = pB - pA, v = pC - pA, n = cross(u, v);
+    if (n.x == 0.0f && n.y == 0.0f && n.z == 0.0f) return -1;
+    V3<float> dir = sB - sA, w0 = sA - pA;
+    float a = -dot(n, w0), b = dot(n, dir);
+    if (std::fabs(b) < float(kFloatEpsilon)) return a == 0.0f ? 2 : 0;
+    float r = a / b;
+    if (r < 0.0f || r > 1.0f) return 0;
+    V3<float> I = sA + r * dir;
+    float uu = dot(u, u), uv = dot(u, v), vv = dot(v, v);
+    V3<float> w = I - pA;
+    float wu = dot(w, u), wv = dot(w, v);
+    float D = uv * uv - uu * vv;
+    float s = (uv * wv - vv * wu) / D;
+    if (s < 0.0f || s > 1.0f) return 0;
+    float tt = (uv * wu - uu * wv) / D;
+    if (tt < 0.0f || (s + tt) > 1.0f) return 0;
+    return 1;
+}
+
+// findIntersectingEdges (integrator.py:1406-1458): the triangle (rod tip, right clamp
+// tip, left clamp tip) of the edge's env
+void oracle_cut_edges(const float* pos, const float* tips, const int* edge, const float* active_edge, int* flip_edges,
+                      int ne, const int* tet, int nt, const float* active_tet, int* flip_tets, const int* edge_tris,
+                      int* holes, const int* edge_env) {
+    for (int t = 0; t < ne; ++t) {
+        int e = edge_env ? edge_env[t] : 0;
+        int a = edge[2 * t], b = edge[2 * t + 1];
+        const float* T0 = tips + 12ll * e;
+        if (oracle_segment_triangle(T0, T0 + 6, T0 + 3, pos + 3ll * a, pos + 3ll * b) != 1) continue;
+        if (flip_edges[t] == 0 && active_edge[t] == 1.0f) flip_edges[t] = -1;
+        for (int k = 0; k < 2; ++k)
+            if (edge_tris[2 * t + k] > -1) holes[edge_tris[2 * t + k]] = 1;
+        for (int i = 0; i < nt; ++i)
+            if (tet_holds(tet + 4 * i, a) && tet_holds(tet + 4 * i, b) && flip_tets[i] == 0 && active_tet[i] == 1.0f)
+                flip_tets[i] = -1;
+    }
+}
+
+// inDeCreaseActiveValues (integrator.py:1583-1605); counters beyond the table are left
+// alone (the reference would read past it)
+void oracle_update_active_values(int* flip, float* active, const float* table, int steps, int n) {
+    for (int t = 0; t < n; ++t) {
+        int f = flip[t];
+        if (f == 0 || f > steps || f < -steps) continue;
+        int k;
+        if (f > 0) { k = f; flip[t] = f + 1; }
+        else { k = steps + f; flip[t] = f - 1; }
+        active[t] = table[k];
+        if (std::abs(f) >= steps) flip[t] = 0;
+    }
+}
+
 }  // extern "C"

@@ -314,3 +314,125 @@ class OracleInstrument:
         assert vis_points.dtype == np.float32 and vis_points.flags["C_CONTIGUOUS"]
         _kin_lib().oracle_instrument_visual(_p(self.xform), _p(lp), _p(sl), len(sl), _p(vis_points), _p(fp), self.n)
         return vis_points
+
+
+# ---------------------------------------------------------------- cutting and heating
+def _cut_lib():
+    lb = lib()
+    if not getattr(lb, "_cut_ready", False):
+        P, I, F = C.c_void_p, C.c_int, C.c_float
+        lb.oracle_edge_breaker.argtypes = [P, P, P, P, P, I, F, F]
+        lb.oracle_check_edge_breaker.argtypes = [P, P, P, P, I, P, I, P, P, P, P, F]
+        lb.oracle_tetrahedron_breaker.argtypes = [P, P, P, P, P, I, F]
+        lb.oracle_heat_propagation.argtypes = [P, P, P, P, I, F, F, F]
+        lb.oracle_heat_update.argtypes = [P, P, P, P, P, I]
+        lb.oracle_check_heat.argtypes = [P, P, P, P, P, F, I]
+        lb.oracle_heat_laparoscope.argtypes = [P, P, P, P, P, P, P, F, F, I]
+        lb.oracle_segment_triangle.argtypes = [P, P, P, P, P]
+        lb.oracle_segment_triangle.restype = C.c_int
+        lb.oracle_cut_edges.argtypes = [P, P, P, P, P, I, P, I, P, P, P, P, P]
+        lb.oracle_update_active_values.argtypes = [P, P, P, I, I]
+        lb._cut_ready = True
+    return lb
+
+
+def segment_triangle(pA, pB, pC, sA, sB) -> int:
+    """checkSegmentTriangleIntersection (integrator.py:1471-1518) on float32 points."""
+    f = lambda a: np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(3))
+    a = [f(x) for x in (pA, pB, pC, sA, sB)]
+    return int(_cut_lib().oracle_segment_triangle(*[_p(x) for x in a]))
+
+
+class OracleCutting:
+    """Host restatement of ffsrl.cutting.SimCutting: the same state and calls over numpy
+    copies, each call a serial loop in thread order (integrator.py:700-918, 1153-1185,
+    1406-1518, 1583-1605).  ``a`` holds every array by the SimCutting / SimModelDO name."""
+
+    ARRAYS = ("edgeBreaker", "tetrahedronBreaker", "flipEdge", "flipTetrahedron", "tetrahedronHeat",
+              "tetrahedronNewHeat", "vertexHeat", "edgesToTriangles", "tetrahedronNeighbors",
+              "tetrahedronToTriangle", "triangleToTetrahedron", "sqrtValues")
+    MODEL = ("vertex", "predictedVertex", "edge", "edgeRestLength", "activeEdge", "tetrahedron",
+             "tetrahedronRestVolume", "activeTetrahedron", "triangle", "triToEnv", "hole", "laparoscopeTip")
+
+    GLOBALS = ("globalBreakFactor", "globalBreakThreshold", "globalHeatConduction", "globalHeatTransfer",
+               "globalHeatLoss", "globalHeatLimit", "globalHeatSphereRadius", "globalHeatQuantum")
+    DTYPES = {"flipEdge": np.int32, "flipTetrahedron": np.int32, "edgesToTriangles": np.int32,
+              "tetrahedronNeighbors": np.int32, "tetrahedronToTriangle": np.int32, "triangleToTetrahedron": np.int32,
+              "edge": np.int32, "tetrahedron": np.int32, "triangle": np.int32, "triToEnv": np.int32,
+              "hole": np.int32, "edgeToEnv": np.int32}
+
+    def __init__(self, arrays: dict, params: dict | None = None):
+        """``arrays`` by name (see ARRAYS, MODEL and ``edgeToEnv``), copied as flat
+        float32 / int32; ``params`` the model's global factors (default 1.0)."""
+        self.a = {k: np.ascontiguousarray(np.asarray(v, dtype=self.DTYPES.get(k, np.float32)).reshape(-1)).copy()
+                  for k, v in arrays.items()}
+        self.g = {k: 1.0 for k in self.GLOBALS}
+        self.g.update(params or {})
+        self.E, self.T, self.F = len(self.a["edgeRestLength"]), len(self.a["tetrahedronRestVolume"]), \
+            len(self.a["triToEnv"])
+
+    @classmethod
+    def from_cutting(cls, cutting):
+        """Host copy of a SimCutting's state and its model's arrays."""
+        c = lambda t: t.detach().cpu().numpy()
+        m = cutting.model
+        arrays = {k: c(getattr(cutting, k)) for k in cls.ARRAYS}
+        arrays.update({k: c(getattr(m, k)) for k in cls.MODEL})
+        arrays["edgeToEnv"] = c(cutting.edgeToEnv)
+        return cls(arrays, {k: getattr(m, k) for k in cls.GLOBALS})
+
+    def _q(self, k):
+        return _p(self.a[k])
+
+    def checkEdgeBreaking(self, breakFactor=None, breakThreshold=None, breakLimit=1.0):
+        bf = self.g["globalBreakFactor"] if breakFactor is None else breakFactor
+        bt = self.g["globalBreakThreshold"] if breakThreshold is None else breakThreshold
+        lb, q = _cut_lib(), self._q
+        lb.oracle_edge_breaker(q("predictedVertex"), q("edge"), q("edgeRestLength"), q("activeEdge"), q("edgeBreaker"),
+                               self.E, float(bf), float(bt))
+        lb.oracle_check_edge_breaker(q("edgeBreaker"), q("edge"), q("activeEdge"), q("flipEdge"), self.E,
+                                     q("tetrahedron"), self.T, q("activeTetrahedron"), q("flipTetrahedron"),
+                                     q("edgesToTriangles"), q("hole"), float(breakLimit))
+
+    def checkTetrahedronBreaking(self, breakFactor=None):
+        bf = self.g["globalBreakFactor"] if breakFactor is None else breakFactor
+        q = self._q
+        _cut_lib().oracle_tetrahedron_breaker(q("predictedVertex"), q("tetrahedron"), q("tetrahedronRestVolume"),
+                                              q("activeTetrahedron"), q("tetrahedronBreaker"), self.T, float(bf))
+
+    def propagateHeat(self, heatConduction=None, heatTransfer=None, heatLoss=None):
+        c = self.g["globalHeatConduction"] if heatConduction is None else heatConduction
+        t = self.g["globalHeatTransfer"] if heatTransfer is None else heatTransfer
+        lo = self.g["globalHeatLoss"] if heatLoss is None else heatLoss
+        lb, q = _cut_lib(), self._q
+        lb.oracle_heat_propagation(q("activeTetrahedron"), q("tetrahedronNeighbors"), q("tetrahedronHeat"),
+                                   q("tetrahedronNewHeat"), self.T, float(c), float(t), float(lo))
+        lb.oracle_heat_update(q("tetrahedronHeat"), q("tetrahedronNewHeat"), q("activeTetrahedron"), q("tetrahedron"),
+                              q("vertexHeat"), self.T)
+
+    def checkHeat(self, heatLimit=None, volumeProportional=False):
+        hl = self.g["globalHeatLimit"] if heatLimit is None else heatLimit
+        q = self._q
+        _cut_lib().oracle_check_heat(q("tetrahedronHeat"), q("flipTetrahedron"),
+                                     q("tetrahedronRestVolume") if volumeProportional else None,
+                                     q("tetrahedronToTriangle"), q("hole"), float(hl), self.T)
+
+    def heatLaparoscope(self, heatSphereRadius=None, heatQuantum=None):
+        r = self.g["globalHeatSphereRadius"] if heatSphereRadius is None else heatSphereRadius
+        qn = self.g["globalHeatQuantum"] if heatQuantum is None else heatQuantum
+        q = self._q
+        _cut_lib().oracle_heat_laparoscope(q("triangle"), q("predictedVertex"), q("activeTetrahedron"),
+                                           q("tetrahedronHeat"), q("triangleToTetrahedron"), q("laparoscopeTip"),
+                                           q("triToEnv"), float(r), float(qn), self.F)
+
+    def cutLaparoscope(self):
+        q = self._q
+        _cut_lib().oracle_cut_edges(q("vertex"), q("laparoscopeTip"), q("edge"), q("activeEdge"), q("flipEdge"),
+                                    self.E, q("tetrahedron"), self.T, q("activeTetrahedron"), q("flipTetrahedron"),
+                                    q("edgesToTriangles"), q("hole"), q("edgeToEnv"))
+
+    def updateActiveValues(self, steps=5):
+        lb, q = _cut_lib(), self._q
+        lb.oracle_update_active_values(q("flipEdge"), q("activeEdge"), q("sqrtValues"), int(steps), self.E)
+        lb.oracle_update_active_values(q("flipTetrahedron"), q("activeTetrahedron"), q("sqrtValues"), int(steps),
+                                       self.T)
