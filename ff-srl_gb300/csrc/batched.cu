@@ -363,7 +363,12 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
     const R nh_uD = R(D.dev_c) / dt / dt;
 
     for (;;) {
-        if (tid == 0) s_work = atomicAdd(counter, 1);
+        // the per-env flags are cleared before the barrier: after it, any warp may set them
+        // (the grasp bits below set s_any_drag from every warp)
+        if (tid == 0) {
+            s_work = atomicAdd(counter, 1);
+            s_incol = 0; s_bad = 0; s_any_drag = 0; s_dyn_it = -1;
+        }
         __syncthreads();
         const int w = s_work;
         if (w >= nwork) return;
@@ -392,7 +397,6 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1)) k_bat
             cnt = reinterpret_cast<int*>(gbase + (sizeof(P) + 3 * sizeof(A)) * (size_t)max_nv);
         }
 
-        if (tid == 0) { s_incol = 0; s_bad = 0; s_any_drag = 0; s_dyn_it = -1; }
         bool bad = false;
         if (tid == 0) {
             for (int i = 0; i < 3; ++i) {

@@ -229,13 +229,15 @@ class SimCutting:
                                      _lib.stream_handle(stream)))
         self._touch()
 
-    def heatLaparoscope(self, heatSphereRadius=None, heatQuantum=None, stream=None):
+    def heatLaparoscope(self, heatSphereRadius=None, heatQuantum=None, positions=None, stream=None):
         """heatLaparoscope (integrator.py:1153-1185): surface triangles near the midpoint of
-        each env's clamp tips heat their tets."""
+        each env's clamp tips heat their tets.  Positions default to the model's current
+        vertices (the reference has no call site that fixes the array)."""
         m = self.model
         r = m.globalHeatSphereRadius if heatSphereRadius is None else heatSphereRadius
         q = m.globalHeatQuantum if heatQuantum is None else heatQuantum
-        check(lib().ffsrl_heat_laparoscope(ptr(m.triangle), ptr(m.predictedVertex), ptr(m.activeTetrahedron),
+        x = m.vertex if positions is None else positions
+        check(lib().ffsrl_heat_laparoscope(ptr(m.triangle), ptr(x), ptr(m.activeTetrahedron),
                                            ptr(self.tetrahedronHeat), ptr(self.triangleToTetrahedron),
                                            ptr(m.laparoscopeTip), ptr(m.triToEnv), float(r), float(q),
                                            m.numTriangles, _lib.stream_handle(stream)))

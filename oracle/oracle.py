@@ -421,7 +421,7 @@ class OracleCutting:
         r = self.g["globalHeatSphereRadius"] if heatSphereRadius is None else heatSphereRadius
         qn = self.g["globalHeatQuantum"] if heatQuantum is None else heatQuantum
         q = self._q
-        _cut_lib().oracle_heat_laparoscope(q("triangle"), q("predictedVertex"), q("activeTetrahedron"),
+        _cut_lib().oracle_heat_laparoscope(q("triangle"), q("vertex"), q("activeTetrahedron"),
                                            q("tetrahedronHeat"), q("triangleToTetrahedron"), q("laparoscopeTip"),
                                            q("triToEnv"), float(r), float(qn), self.F)
 
