@@ -16,7 +16,10 @@ simMesh prim                   ``simMesh`` (1), ``extMesh:vertex`` (local), ``ex
                                ``extMesh:inverseRestPosition`` (Dm^-1, [T, 3, 3]),
                                ``points``, ``faceVertexIndices``, ``primvars:displayColor``,
                                ``mapping:pointToVertex``, ``param:*`` scalars,
-                               ``xformOp:transform`` (optional)
+                               ``xformOp:transform`` (optional); the cutting maps
+                               ``mapping:edgeToTriangles``, ``triangleToTetrahedron``,
+                               ``tetrahedronToTriangles``, ``tetrahedronNeighbors``
+                               (optional, mesh-local ids, -1 for none)
 simRigid prim                  ``simRigid`` (1), ``points`` (local), ``faceVertexIndices``,
                                ``primvars:displayColor``, ``xformOp:transform`` (optional)
 material (either prim)         ``material:diffuse_texture`` [S, S, 3] in [0, 1] (the
@@ -63,7 +66,11 @@ MESH_ATTRS = (("vertex", "extMesh:vertex"), ("tetrahedron", "extMesh:elem"), ("e
               ("inverse_mass", "extMesh:inverseMass"), ("tetrahedron_rest_volume", "extMesh:tetrahedronRestVolume"),
               ("tetrahedron_dm_inv", "extMesh:inverseRestPosition"), ("vis_face", "faceVertexIndices"),
               ("vis_point_color", "primvars:displayColor"), ("point_to_vertex", "mapping:pointToVertex"))
-EXTRA_ATTRS = (("tetrahedron_rest_volume_signed", "ffsrl:tetrahedronRestVolumeSigned"),
+# element maps of the cutting and heating kernels (model.py:207-255), optional
+MAP_ATTRS = (("edge_to_triangles", "mapping:edgeToTriangles"), ("triangle_to_tetrahedron", "mapping:triangleToTetrahedron"),
+             ("tetrahedron_to_triangles", "mapping:tetrahedronToTriangles"),
+             ("tetrahedron_neighbors", "mapping:tetrahedronNeighbors"))
+EXTRA_ATTRS = MAP_ATTRS + (("tetrahedron_rest_volume_signed", "ffsrl:tetrahedronRestVolumeSigned"),
                ("rest_vertex", "ffsrl:restVertex"), ("fixed", "ffsrl:fixed"))
 # connector prim (modelDO.py:751-770): ids local to its bodies
 CONNECTOR_ATTRS = (("connector_vertex_id", "pointId"), ("connector_triangle_id", "triIds"),
@@ -72,8 +79,10 @@ TEXTURE_ATTRS = (("texture", "material:diffuse_texture"), ("tex_coords", "primva
                  ("tex_indices", "primvars:st:indices"))
 SHAPES = {"vertex": (-1, 3), "tetrahedron": (-1, 4), "edge": (-1, 2), "triangle": (-1, 3), "vis_face": (-1, 3),
           "vis_point_color": (-1, 3), "point_to_vertex": (-1, 2), "tetrahedron_dm_inv": (-1, 9),
-          "rest_vertex": (-1, 3), "tex_coords": (-1, 2)}
-INT_KEYS = {"tetrahedron", "edge", "triangle", "vis_face", "point_to_vertex", "tex_indices"}
+          "rest_vertex": (-1, 3), "tex_coords": (-1, 2), "edge_to_triangles": (-1, 2),
+          "tetrahedron_to_triangles": (-1, 4), "tetrahedron_neighbors": (-1, 4)}
+INT_KEYS = {"tetrahedron", "edge", "triangle", "vis_face", "point_to_vertex", "tex_indices", "edge_to_triangles",
+            "triangle_to_tetrahedron", "tetrahedron_to_triangles", "tetrahedron_neighbors"}
 
 
 @dataclass
@@ -167,7 +176,8 @@ def _prims(z, flag):
 
 def merge_meshes(meshes) -> dict:
     """One soft body from several (disjoint) mesh dicts: ids offset, arrays concatenated
-    in order, as the reference concatenates an env's meshes."""
+    in order, as the reference concatenates an env's meshes.  The cutting maps are not
+    carried over (they are rebuilt from the merged topology when needed)."""
     if len(meshes) == 1:
         return meshes[0]
     out = {}

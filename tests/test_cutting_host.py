@@ -210,3 +210,15 @@ def test_active_values_fade_out_and_in(oracle_lib):
     assert (s[:, 3] == 1.0).all()          # a counter beyond the table is left alone
     assert s[0, 4] == 0.0                  # -5: the last step down, then done
     assert o.a["flipEdge"].tolist() == [0, 0, 0, 7, 0]
+
+
+def test_scene_files_carry_the_maps(tmp_path):
+    from ffsrl import scene
+    b = dict(mg.beam(3, 2, 2))
+    b.update(cu.topology_maps(b["tetrahedron"], b["triangle"], b["edge"]))
+    p = tmp_path / "cut.npz"
+    scene.write_scene(p, b)
+    m = scene.read_scene(p).mesh
+    for k in cu.MAP_KEYS:
+        assert np.array_equal(np.asarray(m[k]), b[k]), k
+    assert cu.mesh_maps(m)["edge_to_triangles"].shape == (len(b["edge"]), 2)
