@@ -61,9 +61,16 @@ __device__ __forceinline__ void refit_node(const ffsrl_bvh& b, const float* __re
         lo = vmin(l0, l1);
         hi = vmax(h0, h1);
         if (b.node_box) {
+            // the traversal's child order: the axis along which the children's centres lie
+            // farthest apart (bits 0-1) and whether the right child's centre is the higher
+            // one (bit 2)
+            const v3 d = (l1 + h1) - (l0 + h0);
+            const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+            const int axis = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
+            const float da = axis == 0 ? d.x : (axis == 1 ? d.y : d.z);
             float4* nb = reinterpret_cast<float4*>(b.node_box) + 2ll * (base + node);
             nb[0] = make_float4(lo.x, lo.y, lo.z, __int_as_float(left));
-            nb[1] = make_float4(hi.x, hi.y, hi.z, __int_as_float(0));
+            nb[1] = make_float4(hi.x, hi.y, hi.z, __int_as_float(axis | (da > 0.0f ? 4 : 0)));
         }
     }
     st3(b.aabb_min, base + node, lo);
@@ -240,16 +247,25 @@ __device__ __forceinline__ EnvView env_view(const ffsrl_bvh& b, int e) {
     return v;
 }
 
-// meshQueryRayManyEnvs (render.py:411-498): nearest hit with 0 < t < tMin, stack LIFO
-// with the right child popped first.  Returns the global face id or -1.
-// Traversal over the packed copies written by the refit: two 16-byte loads per node and
-// contiguous leaf triangles; the same node order, tests and hits as query().
+// meshQueryRayManyEnvs (render.py:411-498) over the packed copies written by the refit
+// (two 16-byte loads per node, contiguous leaf triangles), visiting the nearer child
+// first: the refit stores per inner node the axis along which its children's centres lie
+// farthest apart, and the ray's sign along it picks the order.  The result is the
+// reference's hit.  The reference visits nodes in a fixed pre-order (right child first),
+// prunes a node whose box entry is not nearer than the best hit so far, and keeps the
+// first of equally near hits.  Its pre-order visits leaves in descending tri-map position
+// (the build puts a node's left child's triangles first) and a leaf's triangles in
+// ascending order.  So here a hit is kept when it is nearer, or equally near and earlier
+// in that order.  With the same strict pruning, the triangle the reference keeps is never
+// pruned, whatever the visiting order: its boxes are entered before it is reached.
+// Returns the global face id or -1.
 __device__ int query_packed(const EnvView& ev, v3 ro, v3 rd, float& t_hit, v3& p_hit, int* err) {
     int stack[kStackCap];
     int count = 1;
     stack[0] = 0;
     float tMin = 1e6f;
     int hit_tri = -1;
+    int best_first = -1, best_k = 0;  // the kept hit's leaf and place in it
     int visits = 0;
     const v3 inv = mk(1.0f / rd.x, 1.0f / rd.y, 1.0f / rd.z);
     while (count) {
@@ -273,9 +289,12 @@ __device__ int query_packed(const EnvView& ev, v3 ro, v3 rd, float& t_hit, v3& p
                     v3 C = mk(q1.z, q1.w, q2.x);
                     v3 p;
                     float t = moller_trumbore(A, B, C, ro, rd, p);
-                    if (t < tMin && t > 0.0f) {
+                    if (t > 0.0f && (t < tMin || (t == tMin && hit_tri >= 0 &&
+                                                  (first > best_first || (first == best_first && k < best_k))))) {
                         tMin = t;
                         hit_tri = (int)(ev.fofs + ev.tri[first + k]);
+                        best_first = first;
+                        best_k = k;
                         t_hit = t;
                         p_hit = p;
                     }
@@ -289,8 +308,13 @@ __device__ int query_packed(const EnvView& ev, v3 ro, v3 rd, float& t_hit, v3& p
                     atomicExch(err, FFSRL_ERR_STACK_OVERFLOW);
                     return -1;
                 }
-                stack[count] = left;
-                stack[count + 1] = left + 1;
+                const int code = __float_as_int(c.w);
+                const int axis = code & 3;
+                const float da = axis == 0 ? rd.x : (axis == 1 ? rd.y : rd.z);
+                // nearer child: the left one when the ray runs towards the right child's side
+                const bool left_near = (da > 0.0f) == ((code & 4) != 0);
+                stack[count] = left_near ? left + 1 : left;
+                stack[count + 1] = left_near ? left : left + 1;
                 count += 2;
             }
         }
