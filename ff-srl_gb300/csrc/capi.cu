@@ -37,3 +37,48 @@ extern "C" int32_t ffsrl_device_info(int32_t* sm_count, int32_t* max_smem_per_bl
     if (cc_minor) { cudaDeviceGetAttribute(&v, cudaDevAttrComputeCapabilityMinor, dev); *cc_minor = v; }
     return FFSRL_OK;
 }
+
+// ---- CUDA graphs of library calls (the reference's wp.capture_begin / capture_end /
+// capture_launch, bvh.py:442-451, render.py:1108-1112) ----
+struct ffsrl_graph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" int32_t ffsrl_graph_begin(void* stream) {
+    if (!stream) return ffsrl::fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_graph_begin: the legacy default stream cannot be captured");
+    FFSRL_CUDA_TRY(cudaStreamBeginCapture((cudaStream_t)stream, cudaStreamCaptureModeThreadLocal));
+    return FFSRL_OK;
+}
+
+extern "C" int32_t ffsrl_graph_end(void* stream, ffsrl_graph** out) {
+    if (!stream || !out) return ffsrl::fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_graph_end");
+    *out = nullptr;
+    cudaGraph_t g = nullptr;
+    FFSRL_CUDA_TRY(cudaStreamEndCapture((cudaStream_t)stream, &g));
+    cudaGraphExec_t e = nullptr;
+    cudaError_t st = cudaGraphInstantiate(&e, g, 0);
+    if (st != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return ffsrl::cuda_fail(st, "ffsrl_graph_end: instantiate");
+    }
+    ffsrl_graph* h = new ffsrl_graph;
+    h->graph = g;
+    h->exec = e;
+    *out = h;
+    return FFSRL_OK;
+}
+
+extern "C" int32_t ffsrl_graph_launch(const ffsrl_graph* g, void* stream) {
+    if (!g || !g->exec) return ffsrl::fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_graph_launch");
+    FFSRL_CUDA_TRY(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
+    return FFSRL_OK;
+}
+
+extern "C" int32_t ffsrl_graph_destroy(ffsrl_graph* g) {
+    if (!g) return FFSRL_OK;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+    return FFSRL_OK;
+}

@@ -31,6 +31,7 @@ UNITS = {
     "render.cu": ["-fmad=false"],
     "instrument.cu": ["-fmad=false"],
     "cutting.cu": ["-fmad=false"],
+    "serve.cu": [],
     "bvh_build.cpp": [],
 }
 

@@ -100,6 +100,16 @@ class Render(C.Structure):
     ]
 
 
+class ServerConfig(C.Structure):
+    """ffsrl_server_config of include/ffsrl.h."""
+    _fields_ = [("num_slots", I32), ("slot_mesh", P), ("num_actors", I32), ("actor_mesh", P), ("lanes", I32),
+                ("plan", P), ("model", C.POINTER(Model)), ("initial_vertex", P), ("initial_base", P),
+                ("initial_tip", P), ("xform", P), ("initial_xform", P), ("height", P), ("grasp_cand_start", P),
+                ("grasp_cand", P), ("grasp_radius", F32), ("vis_point", P), ("point_to_vertex", P),
+                ("env_map_start", P), ("inst_local_point", P), ("inst_point_slot", P), ("inst_num_points", I32),
+                ("env_inst_first_point", P), ("bvh", C.POINTER(Bvh)), ("vis_face", P), ("render", C.POINTER(Render))]
+
+
 class BatchOptions(C.Structure):
     _fields_ = [("block_threads", I32), ("use_clusters", I32), ("deterministic", I32), ("reserved", I32 * 5)]
 
@@ -157,6 +167,18 @@ def lib() -> C.CDLL:
         "ffsrl_batch_class_envs": ([P, I32, P], I32),
         "ffsrl_batch_set_class_block": ([P, I32, I32], I32),
         "ffsrl_batch_set_class_prefetch": ([P, I32, I32], I32),
+        "ffsrl_server_create": ([C.POINTER(ServerConfig), C.POINTER(P)], I32),
+        "ffsrl_server_destroy": ([P], I32),
+        "ffsrl_server_submit": ([P, I32, P, I32, I32, C.c_int64], I32),
+        "ffsrl_server_launch": ([P, I32, C.POINTER(I32)], I32),
+        "ffsrl_server_poll": ([P, I32, P, P, P, C.POINTER(I32)], I32),
+        "ffsrl_server_admit": ([P, I32, C.POINTER(I32)], I32),
+        "ffsrl_server_evict": ([P, I32], I32),
+        "ffsrl_server_stats": ([P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(I32), C.POINTER(I32)], I32),
+        "ffsrl_graph_begin": ([P], I32),
+        "ffsrl_graph_end": ([P, C.POINTER(P)], I32),
+        "ffsrl_graph_launch": ([P, P], I32),
+        "ffsrl_graph_destroy": ([P], I32),
         "ffsrl_edge_breaker": ([P, P, P, P, P, I32, F32, F32, P], I32),
         "ffsrl_check_edge_breaker": ([P, P, P, P, I32, P, I32, P, P, P, P, F32, P, P, P], I32),
         "ffsrl_tetrahedron_breaker": ([P, P, P, P, P, I32, F32, P], I32),

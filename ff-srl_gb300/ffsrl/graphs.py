@@ -68,3 +68,59 @@ class Graph:
     def reset(self) -> None:
         self.graph = None
         self._kept = []
+
+
+class NativeGraph:
+    """The same capture through the C-ABI's graph calls (``ffsrl_graph_begin`` /
+    ``ffsrl_graph_end`` / ``ffsrl_graph_launch``), as a C caller would use them.  ``fn`` must
+    make library calls only: torch operations that allocate are not recorded by torch's
+    allocator here (use ``Graph`` for those)."""
+
+    def __init__(self, fn: Callable[[], None], prepare: Callable[[], None] | None = None):
+        self.fn = fn
+        self.prepare = prepare
+        self.handle = None
+        self._kept: list = []
+
+    def capture(self) -> None:
+        import ctypes as C
+        from ._lib import check, lib
+        if self.prepare is not None:
+            self.prepare()
+        torch.cuda.synchronize()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        h = C.c_void_p()
+        kept: list = []
+        _capturing.append(kept)
+        try:
+            with torch.cuda.stream(side):
+                check(lib().ffsrl_graph_begin(side.cuda_stream))
+                try:
+                    self.fn()
+                finally:
+                    check(lib().ffsrl_graph_end(side.cuda_stream, C.byref(h)))
+        finally:
+            _capturing.pop()
+        torch.cuda.current_stream().wait_stream(side)
+        self.handle = h
+        self._kept = kept
+
+    def __call__(self) -> None:
+        from ._lib import check, lib
+        if self.handle is None:
+            self.capture()
+        check(lib().ffsrl_graph_launch(self.handle, torch.cuda.current_stream().cuda_stream or None))
+
+    def close(self) -> None:
+        from ._lib import lib
+        if self.handle is not None and self.handle.value:
+            lib().ffsrl_graph_destroy(self.handle)
+        self.handle = None
+        self._kept = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -172,10 +172,13 @@ class EnvServer:
         self.free[int(self.slot_mesh[s])].append(s)
         self.evictions += 1
 
-    def _admit(self, a: int, stream) -> bool:
+    def _admit(self, a: int, stream, busy=()) -> bool:
+        """Give actor a a slot; ``busy`` holds the actors of the tick being formed, which
+        may not be evicted for it."""
         m = int(self.actor_mesh[a])
         if not self.free[m]:
-            idle = [int(x) for x in self.slot_actor[self.slot_mesh == m] if x >= 0 and not self.in_flight[x]]
+            idle = [int(x) for x in self.slot_actor[self.slot_mesh == m]
+                    if x >= 0 and not self.in_flight[x] and int(x) not in busy]
             if not idle:
                 return False
             self._evict(min(idle, key=lambda x: self.last_used[x]), stream)
@@ -246,7 +249,7 @@ class EnvServer:
             if self.in_flight[r.actor] or r.actor in seen or (max_batch and len(batch) >= max_batch):
                 rest.append(r)
                 continue
-            if self.actor_slot[r.actor] < 0 and not self._admit(r.actor, ln.stream):
+            if self.actor_slot[r.actor] < 0 and not self._admit(r.actor, ln.stream, seen):
                 rest.append(r)
                 continue
             seen.add(r.actor)
@@ -400,3 +403,113 @@ class EnvServer:
                 "slots": self.num_slots, "evictions": self.evictions, "budget_bytes_used": self.budget_used,
                 "episode_requests": episode, "env_status_nonzero": int((self.plan.env_status() != 0).sum()),
                 **({"tick_profile": prof} if prof else {})}
+
+
+class NativeEnvServer(EnvServer):
+    """``EnvServer`` with its ticks run by the library's C server (``ffsrl_server_*``): the
+    same slots, model, plan, BVH and renderer, with admission, eviction, the lanes and each
+    tick's launch sequence in native code.  Results equal ``EnvServer``'s for the same
+    requests (each env's result depends only on its own inputs)."""
+
+    def __init__(self, *args, **kw):
+        super().__init__(*args, **kw)
+        m = self.model
+        self._dm = m.device_model()
+        self._rd = self.renderer._desc(m)
+        self._slot_mesh = np.ascontiguousarray(self.slot_mesh, dtype=np.int32)
+        self._actor_mesh = np.ascontiguousarray(self.actor_mesh, dtype=np.int32)
+        c = L.ServerConfig()
+        c.num_slots, c.slot_mesh = self.num_slots, self._slot_mesh.ctypes.data
+        c.num_actors, c.actor_mesh = self.num_actors, self._actor_mesh.ctypes.data
+        c.lanes = len(self.lanes)
+        c.plan = self.plan.handle
+        c.model = C.pointer(self._dm)
+        c.initial_vertex = ptr(m.initialVertex)
+        c.initial_base, c.initial_tip = ptr(m.laparoscopeInitialBase), ptr(m.laparoscopeInitialTip)
+        if m.hasInstrumentKinematics:
+            c.xform, c.initial_xform = ptr(m.laparoscopeXForm), ptr(m.laparoscopeInitialXForm)
+            c.height = ptr(m.laparoscopeHeight)
+            if m.instrumentMesh is not None:
+                c.inst_local_point, c.inst_point_slot = ptr(m.laparoscopeVertex), ptr(m.laparoscopeVertexToXForm)
+                c.inst_num_points = int(m.laparoscopeVertexToXForm.numel())
+                c.env_inst_first_point = ptr(m.envInstrumentPointStartT)
+        c.grasp_cand_start, c.grasp_cand = ptr(m.graspCandStartT), ptr(m.graspCand)
+        c.grasp_radius = m.globalLaparoscopeDragLookupRadius
+        c.vis_point, c.point_to_vertex, c.env_map_start = ptr(m.allVisPoint), ptr(m.pointToVertex), ptr(m.envMapStartT)
+        c.bvh, c.vis_face, c.render = C.pointer(self.bvh.desc), ptr(m.allVisFace), C.pointer(self._rd)
+        self._cfg = c
+        h = C.c_void_p()
+        check(lib().ffsrl_server_create(C.byref(c), C.byref(h)))
+        self.handle = h
+        self._reqs: dict[int, Request] = {}
+        self._tag = 0
+        cap = self.num_slots * len(self.lanes)
+        self._tags = np.zeros(cap, dtype=np.int64)
+        self._actors = np.zeros(cap, dtype=np.int32)
+        self._res = np.zeros((cap, 4), dtype=np.float32)
+
+    def _stats(self):
+        a, e = C.c_int64(), C.c_int64()
+        p, f = C.c_int32(), C.c_int32()
+        check(lib().ffsrl_server_stats(self.handle, C.byref(a), C.byref(e), C.byref(p), C.byref(f)))
+        return int(a.value), int(e.value), int(p.value), int(f.value)
+
+    @property
+    def evictions(self) -> int:
+        return self._stats()[1] if getattr(self, "handle", None) is not None else 0
+
+    @evictions.setter
+    def evictions(self, _):  # EnvServer's own counter; the C server keeps the count here
+        pass
+
+    @property
+    def admissions(self) -> int:
+        return self._stats()[0] if getattr(self, "handle", None) is not None else 0
+
+    @admissions.setter
+    def admissions(self, _):
+        pass
+
+    def submit(self, req: Request) -> None:
+        d = np.ascontiguousarray(np.asarray(req.disp, dtype=np.float32).reshape(3))
+        self._tag += 1
+        self._reqs[self._tag] = req
+        check(lib().ffsrl_server_submit(self.handle, int(req.actor), d.ctypes.data, int(req.clamp), int(req.reset),
+                                        self._tag))
+
+    def launch(self, max_batch: int | None = None) -> int:
+        n = C.c_int32()
+        check(lib().ffsrl_server_launch(self.handle, int(max_batch or 0), C.byref(n)))
+        return int(n.value)
+
+    def poll(self) -> list[Request]:
+        n = C.c_int32()
+        check(lib().ffsrl_server_poll(self.handle, len(self._tags), self._tags.ctypes.data, self._actors.ctypes.data,
+                                      self._res.ctypes.data, C.byref(n)))
+        now = time.perf_counter()
+        done = []
+        for i in range(n.value):
+            r = self._reqs.pop(int(self._tags[i]))
+            r.t_done = now
+            r.result = self._res[i].copy()
+            done.append(r)
+        return done
+
+    def drain(self) -> list[Request]:
+        done = []
+        while self._stats()[3] > 0:
+            done += self.poll()
+            time.sleep(0.0002)
+        return done
+
+    def close(self) -> None:
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            torch.cuda.synchronize()
+            lib().ffsrl_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

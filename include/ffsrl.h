@@ -381,6 +381,77 @@ int32_t ffsrl_batch_state_f64(const ffsrl_batch* b, double* host_xvx);
 /* per-env status after a step: 0 ok, FFSRL_ERR_NONFINITE if the env's state went non-finite */
 int32_t ffsrl_batch_env_status(const ffsrl_batch* b, int32_t* host_status, int32_t num_envs);
 
+/* ---- CUDA graphs (the reference's wp.capture_begin / capture_end / capture_launch,
+   bvh.py:442-451, render.py:1108-1112, tests/testLiverRetraction.py:77-85) ----------
+   Every launch the library's calls make on `stream` between begin and end is recorded
+   (the batched step's class streams join the capture through its fork/join events);
+   launch replays them on any stream with the pointers and scalars they were recorded
+   with.  The legacy default stream (NULL) cannot be captured.  Calls that wait on the
+   host (ffsrl_batch_create, the staged env lists of ffsrl_batch_step_envs) do not belong
+   in a capture. */
+typedef struct ffsrl_graph ffsrl_graph;
+int32_t ffsrl_graph_begin(void* stream);
+int32_t ffsrl_graph_end(void* stream, ffsrl_graph** graph);
+int32_t ffsrl_graph_launch(const ffsrl_graph* graph, void* stream);
+int32_t ffsrl_graph_destroy(ffsrl_graph* graph);
+
+/* ---- serving: continuous batching of RL step requests (admit / evict / submit / poll) --
+   Each actor owns one env of a mesh type; envs live in the slots of one batched model,
+   slot s holding an env of mesh type slot_mesh[s].  A request is a tool displacement (3
+   floats), a clamp flag and a reset flag (the env returns to its rest state first).
+   ffsrl_server_launch starts a tick on a free lane with every ready request (its actor
+   not in flight; admitted into a free slot of its type, evicting the least recently used
+   idle actor of that type when there is none -- its state is kept in host memory and
+   restored when it returns).  A tick runs, for exactly those envs: resets, the tool move
+   (the kinematic chain when xform is given, else a rigid translation), grasp changes, one
+   batched step, the visual remap, the instrument's visual points, the BVH refit and the
+   ray-cast.  ffsrl_server_poll returns finished requests: their tags, actors and 4 floats
+   each (the drag point tip[4e+3] and the env's contact count).  A lane's tick is returned
+   whole, so capacity should be at least num_slots.  Host calls from one thread. */
+typedef struct ffsrl_server ffsrl_server;
+typedef struct {
+    int32_t num_slots;                  /* envs of the model */
+    const int32_t* slot_mesh;           /* host [num_slots] mesh type of each slot */
+    int32_t num_actors;
+    const int32_t* actor_mesh;          /* host [num_actors] mesh type of each actor's env */
+    int32_t lanes;                      /* ticks in flight at once: 1 or 2 (the plan's lanes) */
+    ffsrl_batch* plan;                  /* the model's batched plan */
+    const ffsrl_model* model;           /* device arrays of the model (copied at create) */
+    const float* initial_vertex;        /* [3V] rest state */
+    const float* initial_base;          /* [3*4N] */
+    const float* initial_tip;           /* [3*4N] */
+    float* xform;                       /* [112N] instrument transforms, or NULL */
+    const float* initial_xform;         /* [112N] (with xform) */
+    const float* height;                /* [4N] capsule heights (with xform) */
+    const int32_t* grasp_cand_start;    /* [N+1] grasp candidates of each env */
+    const int32_t* grasp_cand;
+    float grasp_radius;                 /* drag lookup radius */
+    float* vis_point;                   /* all visual points */
+    const int32_t* point_to_vertex;     /* remap pairs */
+    const int32_t* env_map_start;       /* [N+1] */
+    const float* inst_local_point;      /* instrument visual mesh (inst_num_points 0: none) */
+    const int32_t* inst_point_slot;
+    int32_t inst_num_points;
+    const int32_t* env_inst_first_point;/* [N] */
+    const ffsrl_bvh* bvh;               /* copied at create */
+    const int32_t* vis_face;
+    const ffsrl_render* render;         /* copied at create */
+} ffsrl_server_config;
+int32_t ffsrl_server_create(const ffsrl_server_config* config, ffsrl_server** server);
+int32_t ffsrl_server_destroy(ffsrl_server* server);
+int32_t ffsrl_server_submit(ffsrl_server* server, int32_t actor, const float* disp, int32_t clamp, int32_t reset,
+                            int64_t tag);
+/* starts a tick of at most max_batch requests (<= 0: no limit); *launched = its size */
+int32_t ffsrl_server_launch(ffsrl_server* server, int32_t max_batch, int32_t* launched);
+int32_t ffsrl_server_poll(ffsrl_server* server, int32_t capacity, int64_t* tags, int32_t* actors, float* results,
+                          int32_t* count);
+/* explicit admission (returns the slot; FFSRL_ERR_BUSY when every slot of the type is in
+   flight) and eviction (FFSRL_ERR_BUSY while the actor's tick is not polled) */
+int32_t ffsrl_server_admit(ffsrl_server* server, int32_t actor, int32_t* slot);
+int32_t ffsrl_server_evict(ffsrl_server* server, int32_t actor);
+int32_t ffsrl_server_stats(const ffsrl_server* server, int64_t* admissions, int64_t* evictions, int32_t* pending,
+                           int32_t* in_flight);
+
 /* ---- cutting and heating (integrator.py:700-918, 1153-1185, 1406-1518, 1583-1605) ----
    Library calls over the env-major arrays; the reference's DO step does not launch them.
    One thread per element.  Element maps use -1 for "none" (no neighbour, no surface

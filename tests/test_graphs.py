@@ -74,3 +74,28 @@ def test_rl_step_graph_with_changing_actions(gpu):
         out.append(_state(m, bvh, r) + [m.laparoscopeInCollision.cpu().numpy()])
     for a, b in zip(*out):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.gpu
+def test_native_graph_calls_replay_the_step_and_refit(gpu):
+    # ffsrl_graph_begin / end / launch (the C caller's capture) around library calls only
+    import torch
+    from ffsrl.graphs import NativeGraph
+    out = []
+    for use in (False, True):
+        m, bvh, r = _setup()
+        integ = SimIntegratorDO("cuda:0")
+
+        def step():
+            integ.stepModel(m, 2)
+            bvh.refitBVH()
+
+        g = NativeGraph(step, prepare=lambda: integ.plan(m)) if use else step
+        for _ in range(3):
+            g()
+        torch.cuda.synchronize()
+        out.append([t.cpu().numpy() for t in (m.vertex, m.velocity, m.allVisPoint, bvh.aabbMin, bvh.aabbMax)])
+        if use:
+            g.close()
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)

@@ -33,7 +33,7 @@ def test_abi_version(built_lib):
 
 
 STRUCTS = {"ffsrl_model": L.Model, "ffsrl_params": L.Params, "ffsrl_bvh": L.Bvh, "ffsrl_render": L.Render,
-           "ffsrl_batch_options": L.BatchOptions}
+           "ffsrl_batch_options": L.BatchOptions, "ffsrl_server_config": L.ServerConfig}
 
 
 def test_struct_layouts_match_header(tmp_path):
@@ -64,8 +64,23 @@ def test_argument_errors_need_no_gpu(built_lib):
     assert lib.ffsrl_bvh_refit_fused(None, None, None, None) == L.ERR_INVALID_ARGUMENT
     assert lib.ffsrl_render_fused(None, None, None) == L.ERR_INVALID_ARGUMENT
     assert lib.ffsrl_grasp_nearest(None, None, None, None, None, 0.0, None, 3, None) == L.ERR_INVALID_ARGUMENT
+    # serving, graphs and cutting check their arguments before touching a device
+    h = C.c_void_p()
+    assert lib.ffsrl_server_create(None, C.byref(h)) == L.ERR_INVALID_ARGUMENT and not h.value
+    assert lib.ffsrl_server_create(C.byref(L.ServerConfig()), C.byref(h)) == L.ERR_INVALID_ARGUMENT
+    assert lib.ffsrl_server_submit(None, 0, None, 1, 0, 7) == L.ERR_INVALID_ARGUMENT
+    assert lib.ffsrl_server_poll(None, 0, None, None, None, None) == L.ERR_INVALID_ARGUMENT
+    assert lib.ffsrl_server_destroy(None) == L.OK
+    assert lib.ffsrl_graph_begin(None) == L.ERR_INVALID_ARGUMENT
+    assert lib.ffsrl_graph_launch(None, None) == L.ERR_INVALID_ARGUMENT
+    assert lib.ffsrl_graph_destroy(None) == L.OK
+    assert lib.ffsrl_edge_breaker(None, None, None, None, None, 3, 1.0, 0.1, None) == L.ERR_INVALID_ARGUMENT
+    assert lib.ffsrl_update_active_values(None, None, None, 0, 5, None) == L.ERR_INVALID_ARGUMENT
+    assert lib.ffsrl_cut_edges(None, None, None, None, None, 2, None, 0, None, None, None, None, None, None,
+                               None) == L.ERR_INVALID_ARGUMENT
     # empty work is a no-op
     assert lib.ffsrl_remap(None, None, None, 0, None) == L.OK
+    assert lib.ffsrl_heat_propagation(None, None, None, None, 0, 0.1, 0.1, 0.1, None) == L.OK
     # out-of-range faces are rejected by the host BVH build
     pts = np.zeros((3, 3), dtype=np.float32)
     faces = np.array([[0, 1, 7]], dtype=np.int32)

@@ -124,3 +124,63 @@ def test_episode_reset_restarts_from_rest(gpu):
     res = {r.actor: r.result for r in done}
     assert np.array_equal(res[3], res[0])
     assert np.array_equal(_state(srv, 3), _state(srv, 0))
+
+
+def _run_native(srv, plan):
+    from ffsrl.serve import Request
+    out = {}
+    for reqs in plan:
+        for a, d, c, *rst in reqs:
+            srv.submit(Request(a, np.asarray(d, dtype=np.float32), c, 0.0, reset=bool(rst and rst[0])))
+        done = []
+        while srv._stats()[2] or srv._stats()[3]:
+            srv.launch()
+            done += srv.poll()
+        for r in done:
+            out.setdefault(r.actor, []).append(r.result.copy())
+    return out
+
+
+@pytest.mark.gpu
+def test_native_server_matches_the_python_server(gpu):
+    # the C server (ffsrl_server_*) against EnvServer on the same requests: a slot budget
+    # that forces evictions, episode resets and clamp changes; results and states bit-equal
+    from ffsrl.serve import EnvServer, NativeEnvServer
+    actors = [0, 0, 1, 1, 2, 2]
+    pool = _pool()
+    per = np.array([slot_bytes(m, 16) for m in pool])
+    kw = dict(hbm_budget_bytes=float(per.sum()) * 1.2, resolution=16)
+    py = EnvServer(pool, actors, "cuda:0", **kw)
+    nat = NativeEnvServer(pool, actors, "cuda:0", **kw)
+    assert nat.num_slots == py.num_slots == 3
+    rng = np.random.default_rng(5)
+    plan = []
+    for k in range(8):
+        acts = rng.permutation(6)[:3]
+        plan.append([(int(a), rng.uniform(-0.05, 0.05, 3).tolist(), int(k % 4 != 3), int(k == 5 and a % 2 == 0))
+                     for a in acts])
+    from ffsrl.serve import Request
+    rp = {}
+    for reqs in plan:
+        for a, d, c, rst in reqs:
+            py.submit(Request(a, np.asarray(d, dtype=np.float32), c, 0.0, reset=bool(rst)))
+        done = []
+        while py.pending or any(ln.batch for ln in py.lanes):
+            py.launch()
+            done += py.poll()
+        for r in done:
+            rp.setdefault(r.actor, []).append(r.result.copy())
+    rn = _run_native(nat, plan)
+    print(f"[serve] native: {nat.admissions} admissions, {nat.evictions} evictions; python: {py.admissions}, "
+          f"{py.evictions}")
+    assert nat.evictions == py.evictions >= 3 and nat.admissions == py.admissions
+    assert sorted(rp) == sorted(rn)
+    for a in rp:
+        assert len(rp[a]) == len(rn[a])
+        for x, y in zip(rp[a], rn[a]):
+            assert np.array_equal(x, y)
+    torch = pytest.importorskip("torch")
+    torch.cuda.synchronize()
+    assert np.array_equal(py.model.vertex.cpu().numpy(), nat.model.vertex.cpu().numpy())
+    assert np.array_equal(py.renderer.pixels.cpu().numpy(), nat.renderer.pixels.cpu().numpy())
+    nat.close()
