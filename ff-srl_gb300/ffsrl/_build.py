@@ -32,6 +32,7 @@ UNITS = {
     "instrument.cu": ["-fmad=false"],
     "cutting.cu": ["-fmad=false"],
     "serve.cu": [],
+    "handle.cu": [],
     "bvh_build.cpp": [],
 }
 

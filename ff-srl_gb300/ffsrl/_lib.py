@@ -167,6 +167,12 @@ def lib() -> C.CDLL:
         "ffsrl_batch_class_envs": ([P, I32, P], I32),
         "ffsrl_batch_set_class_block": ([P, I32, I32], I32),
         "ffsrl_batch_set_class_prefetch": ([P, I32, I32], I32),
+        "ffsrl_create": ([pm, pp, I32, C.POINTER(P)], I32),
+        "ffsrl_destroy": ([P], I32),
+        "ffsrl_step": ([P, I32, P], I32),
+        "ffsrl_get_device_model": ([P, pm, C.POINTER(P)], I32),
+        "ffsrl_set_tool": ([P, P, P, P, I32, P], I32),
+        "ffsrl_set_drag": ([P, P, I32, P], I32),
         "ffsrl_server_create": ([C.POINTER(ServerConfig), C.POINTER(P)], I32),
         "ffsrl_server_destroy": ([P], I32),
         "ffsrl_server_submit": ([P, I32, P, I32, I32, C.c_int64], I32),

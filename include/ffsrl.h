@@ -381,6 +381,26 @@ int32_t ffsrl_batch_state_f64(const ffsrl_batch* b, double* host_xvx);
 /* per-env status after a step: 0 ok, FFSRL_ERR_NONFINITE if the env's state went non-finite */
 int32_t ffsrl_batch_env_status(const ffsrl_batch* b, int32_t* host_status, int32_t num_envs);
 
+/* ---- owning handle over the batched step ------------------------------------------
+   ffsrl_create uploads a model given in HOST memory (an ffsrl_model whose pointers are
+   host arrays, sizes as the struct documents) into device arrays the handle owns, and
+   builds its batched plan (block_threads 0: automatic).  State and scratch arrays the
+   host model leaves NULL (predicted_vertex, velocity, dp, constraints_number,
+   collision_dp, lambdas, hole, active_drag_constraint, laparoscope_in_collision) start
+   zeroed.  ffsrl_get_device_model fills an ffsrl_model with the device pointers (and the
+   plan, for the ffsrl_batch_* calls): callers read and write state, tool and grasp arrays
+   there between steps.  ffsrl_set_tool / ffsrl_set_drag copy tool capsules [4N] and the
+   grasp mask [V] from host (from_host 1, waits for the copy) or device memory. */
+typedef struct ffsrl_handle ffsrl_handle;
+int32_t ffsrl_create(const ffsrl_model* host_model, const ffsrl_params* params, int32_t block_threads,
+                     ffsrl_handle** handle);
+int32_t ffsrl_destroy(ffsrl_handle* handle);
+int32_t ffsrl_step(ffsrl_handle* handle, int32_t n_steps, void* stream);
+int32_t ffsrl_get_device_model(const ffsrl_handle* handle, ffsrl_model* device_model, ffsrl_batch** plan);
+int32_t ffsrl_set_tool(ffsrl_handle* handle, const float* base, const float* tip, const float* radius,
+                       int32_t from_host, void* stream);
+int32_t ffsrl_set_drag(ffsrl_handle* handle, const float* drag, int32_t from_host, void* stream);
+
 /* ---- CUDA graphs (the reference's wp.capture_begin / capture_end / capture_launch,
    bvh.py:442-451, render.py:1108-1112, tests/testLiverRetraction.py:77-85) ----------
    Every launch the library's calls make on `stream` between begin and end is recorded

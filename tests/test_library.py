@@ -71,6 +71,10 @@ def test_argument_errors_need_no_gpu(built_lib):
     assert lib.ffsrl_server_submit(None, 0, None, 1, 0, 7) == L.ERR_INVALID_ARGUMENT
     assert lib.ffsrl_server_poll(None, 0, None, None, None, None) == L.ERR_INVALID_ARGUMENT
     assert lib.ffsrl_server_destroy(None) == L.OK
+    assert lib.ffsrl_create(None, None, 0, C.byref(h)) == L.ERR_INVALID_ARGUMENT and not h.value
+    assert lib.ffsrl_create(C.byref(L.Model()), C.byref(L.Params()), 0, C.byref(h)) == L.ERR_INVALID_ARGUMENT
+    assert lib.ffsrl_step(None, 1, None) == L.ERR_INVALID_ARGUMENT
+    assert lib.ffsrl_destroy(None) == L.OK
     assert lib.ffsrl_graph_begin(None) == L.ERR_INVALID_ARGUMENT
     assert lib.ffsrl_graph_launch(None, None) == L.ERR_INVALID_ARGUMENT
     assert lib.ffsrl_graph_destroy(None) == L.OK
