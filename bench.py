@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=5.0)
+    ap.add_argument("--serve-impl", choices=("native", "python"), default="native",
+                    help="serving loop: the library's C server (ffsrl_server_*) or the Python EnvServer")
     ap.add_argument("--no-graph", action="store_true", help="launch the env-step eagerly instead of a CUDA graph")
     return ap.parse_args()
 
@@ -370,12 +372,14 @@ def main():
     if args.serve_seconds > 0:
         # continuous-batching serving of the same pool: one closed-loop actor per env
         from ffsrl import scenarios as sc2
-        from ffsrl.serve import EnvServer
+        from ffsrl.serve import EnvServer, NativeEnvServer
         meshes_s, pool_s = sc2.mixed_meshes(envs, pool_size=POOL, seed=rank)
         ids = {id(mm): k for k, mm in enumerate(pool_s)}
-        srv = EnvServer(pool_s, [ids[id(mm)] for mm in meshes_s], device, hbm_budget_bytes=60e9, resolution=RES,
-                        autotune=True)
+        Server = NativeEnvServer if args.serve_impl == "native" else EnvServer
+        srv = Server(pool_s, [ids[id(mm)] for mm in meshes_s], device, hbm_budget_bytes=60e9, resolution=RES,
+                     autotune=True)
         serving = srv.run_closed_loop(args.serve_seconds, think_hz=60.0, seed=rank, warmup_s=1.0)
+        serving["server"] = args.serve_impl
         serving["what"] = ("closed-loop actors, Poisson think time at 60 Hz, each request = effector move + 8x10 step "
                            "+ refit + 128x128 ray-cast of its env; latency from arrival to result on the host")
         del srv
