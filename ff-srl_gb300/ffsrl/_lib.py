@@ -100,6 +100,14 @@ class Render(C.Structure):
     ]
 
 
+class RenderConfig(C.Structure):
+    """ffsrl_render_config of include/ffsrl.h."""
+    _fields_ = [("num_points", I32), ("num_faces", I32), ("points", P), ("faces", P), ("colors", P),
+                ("num_map", I32), ("point_to_vertex", P), ("env_point_start", P), ("env_face_start", P),
+                ("env_topology", P), ("resolution", I32), ("camera_tan", F32), ("camera_aspect", F32),
+                ("num_lights", I32), ("light_dir", P), ("light_intensity", P), ("render_mode", I32)]
+
+
 class ServerConfig(C.Structure):
     """ffsrl_server_config of include/ffsrl.h."""
     _fields_ = [("num_slots", I32), ("slot_mesh", P), ("num_actors", I32), ("actor_mesh", P), ("lanes", I32),
@@ -173,6 +181,8 @@ def lib() -> C.CDLL:
         "ffsrl_get_device_model": ([P, pm, C.POINTER(P)], I32),
         "ffsrl_set_tool": ([P, P, P, P, I32, P], I32),
         "ffsrl_set_drag": ([P, P, I32, P], I32),
+        "ffsrl_attach_render": ([P, C.POINTER(RenderConfig)], I32),
+        "ffsrl_render_handle": ([P, P, P, I32, P, P, P], I32),
         "ffsrl_server_create": ([C.POINTER(ServerConfig), C.POINTER(P)], I32),
         "ffsrl_server_destroy": ([P], I32),
         "ffsrl_server_submit": ([P, I32, P, I32, I32, C.c_int64], I32),

@@ -401,6 +401,36 @@ int32_t ffsrl_set_tool(ffsrl_handle* handle, const float* base, const float* tip
                        int32_t from_host, void* stream);
 int32_t ffsrl_set_drag(ffsrl_handle* handle, const float* drag, int32_t from_host, void* stream);
 
+/* Observation for the handle: the visual mesh of all envs in HOST memory (env-major;
+   faces hold global point ids within their env's range), remap pairs (visual point,
+   simulated vertex) and shading.  ffsrl_attach_render builds one BVH topology per
+   distinct env_topology id (NULL: one per env) on its first env's points (the
+   reference's binned SAH, 8 bins) and owns every device buffer of the refit and the
+   ray-cast.  Texture mode (1) needs texture tables and is not offered here.
+   ffsrl_render_handle remaps the visual points from the current vertices, refits and
+   ray-casts: color [N*R*R*3] and depth [N*R*R] are caller-owned device arrays; cameras
+   are device arrays of 1 or num_envs entries (position [3C], quaternion x,y,z,w [4C]). */
+typedef struct {
+    int32_t num_points, num_faces;
+    const float* points;            /* [3P] visual points, the BVH is built on these */
+    const int32_t* faces;           /* [3Fv] */
+    const float* colors;            /* [3P] */
+    int32_t num_map;
+    const int32_t* point_to_vertex; /* [2 * num_map] */
+    const int32_t* env_point_start; /* [N+1] */
+    const int32_t* env_face_start;  /* [N+1] */
+    const int32_t* env_topology;    /* [N] or NULL */
+    int32_t resolution;
+    float camera_tan, camera_aspect;
+    int32_t num_lights;
+    const float* light_dir;         /* [3L] */
+    const float* light_intensity;   /* [L] */
+    int32_t render_mode;            /* 0 grayscale, 2 normal map, 3 vertex colour, 4 depth map */
+} ffsrl_render_config;
+int32_t ffsrl_attach_render(ffsrl_handle* handle, const ffsrl_render_config* config);
+int32_t ffsrl_render_handle(ffsrl_handle* handle, const float* camera_pos, const float* camera_rot, int32_t num_cameras,
+                            float* color, float* depth, void* stream);
+
 /* ---- CUDA graphs (the reference's wp.capture_begin / capture_end / capture_launch,
    bvh.py:442-451, render.py:1108-1112, tests/testLiverRetraction.py:77-85) ----------
    Every launch the library's calls make on `stream` between begin and end is recorded

@@ -53,3 +53,59 @@ def test_handle_steps_like_the_python_layer(gpu):
           f"max |x_handle - x_python| = {np.abs(got - m.vertex.cpu().numpy()).max():.1e}")
     assert np.array_equal(got, m.vertex.cpu().numpy())
     assert np.array_equal(vel, m.velocity.cpu().numpy())
+
+
+@pytest.mark.gpu
+def test_handle_render_matches_the_python_renderer(gpu):
+    # ffsrl_attach_render / ffsrl_render_handle against SimBVH + WarpRaycastRendererDO on
+    # the same model state: same BVHs (built on the same rest points), same images
+    from ffsrl import SimBVH, WarpRaycastRendererDO
+    meshes, _ = sc.mixed_meshes(4, pool_size=2, seed=17, t_lo=300, t_hi=900)
+    m, meshes = sc.liver_model("cuda:0", 4, meshes=meshes, instrument_visual=False)
+    m.graspNearest(torch.ones(4, dtype=torch.int32, device="cuda:0"))
+    bvh = SimBVH("cuda:0", m)
+    ap = sc.fov_aperture(60.0)
+    r = WarpRaycastRendererDO("cuda:0", m, resolution=16, mode="headless", verticalAperture=ap,
+                              horizontalAperture=ap, render_mode=3)
+    r.setCameras(*sc.env_cameras(meshes, seed=4))
+    torch.cuda.synchronize()
+    hm, keep = m.host_model()
+    lib = L.lib()
+    h = C.c_void_p()
+    L.check(lib.ffsrl_create(C.byref(hm), C.byref(m.params()), 0, C.byref(h)))
+    try:
+        pts = np.ascontiguousarray(m.allVisPoint.cpu().numpy(), dtype=np.float32)
+        faces = np.ascontiguousarray(m.host["allVisFace"], dtype=np.int32)
+        cols = np.ascontiguousarray(m.allVisPointColor.cpu().numpy(), dtype=np.float32)
+        ptv = np.ascontiguousarray(m.host["pointToVertex"], dtype=np.int32)
+        ps = np.ascontiguousarray(m.envVisPointStart, dtype=np.int32)
+        fs = np.ascontiguousarray(m.envVisFaceStart, dtype=np.int32)
+        topo = np.ascontiguousarray(m.envMesh, dtype=np.int32)
+        ld = np.ascontiguousarray(r.lightDir.cpu().numpy(), dtype=np.float32)
+        li = np.ascontiguousarray(r.lightIntensity.cpu().numpy(), dtype=np.float32)
+        c = L.RenderConfig(num_points=len(pts), num_faces=len(faces) // 3 if faces.ndim == 1 else len(faces),
+                           points=pts.ctypes.data, faces=faces.ctypes.data, colors=cols.ctypes.data,
+                           num_map=len(ptv.reshape(-1)) // 2, point_to_vertex=ptv.ctypes.data,
+                           env_point_start=ps.ctypes.data, env_face_start=fs.ctypes.data,
+                           env_topology=topo.ctypes.data, resolution=16, camera_tan=r.camera_tan,
+                           camera_aspect=r.camera_aspect, num_lights=len(li), light_dir=ld.ctypes.data,
+                           light_intensity=li.ctypes.data, render_mode=3)
+        L.check(lib.ffsrl_attach_render(h, C.byref(c)))
+        L.check(lib.ffsrl_step(h, 2, None))
+        color = torch.zeros((4, 16, 16, 3), dtype=torch.float32, device="cuda:0")
+        depth = torch.zeros((4, 16, 16), dtype=torch.float32, device="cuda:0")
+        L.check(lib.ffsrl_render_handle(h, r.cameraPosT.data_ptr(), r.cameraRotT.data_ptr(), int(r.cameraPosT.shape[0]),
+                                        color.data_ptr(), depth.data_ptr(), None))
+        torch.cuda.synchronize()
+    finally:
+        lib.ffsrl_destroy(h)
+    SimIntegratorDO("cuda:0").stepModel(m, 2)
+    bvh.refitBVH()
+    r.renderNew(bvh, m)
+    torch.cuda.synchronize()
+    hit = float((depth > 0).float().mean())
+    print(f"[handle] render: {hit:.2f} of the pixels hit; max |color diff| "
+          f"{float((color - r.pixels.reshape(color.shape)).abs().max()):.1e}")
+    assert hit > 0.05
+    assert torch.equal(color, r.pixels.reshape(color.shape))
+    assert torch.equal(depth, r.depth.reshape(depth.shape))

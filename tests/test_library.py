@@ -33,7 +33,8 @@ def test_abi_version(built_lib):
 
 
 STRUCTS = {"ffsrl_model": L.Model, "ffsrl_params": L.Params, "ffsrl_bvh": L.Bvh, "ffsrl_render": L.Render,
-           "ffsrl_batch_options": L.BatchOptions, "ffsrl_server_config": L.ServerConfig}
+           "ffsrl_batch_options": L.BatchOptions, "ffsrl_server_config": L.ServerConfig,
+           "ffsrl_render_config": L.RenderConfig}
 
 
 def test_struct_layouts_match_header(tmp_path):
@@ -74,6 +75,8 @@ def test_argument_errors_need_no_gpu(built_lib):
     assert lib.ffsrl_create(None, None, 0, C.byref(h)) == L.ERR_INVALID_ARGUMENT and not h.value
     assert lib.ffsrl_create(C.byref(L.Model()), C.byref(L.Params()), 0, C.byref(h)) == L.ERR_INVALID_ARGUMENT
     assert lib.ffsrl_step(None, 1, None) == L.ERR_INVALID_ARGUMENT
+    assert lib.ffsrl_attach_render(None, None) == L.ERR_INVALID_ARGUMENT
+    assert lib.ffsrl_render_handle(None, None, None, 1, None, None, None) == L.ERR_INVALID_ARGUMENT
     assert lib.ffsrl_destroy(None) == L.OK
     assert lib.ffsrl_graph_begin(None) == L.ERR_INVALID_ARGUMENT
     assert lib.ffsrl_graph_launch(None, None) == L.ERR_INVALID_ARGUMENT
