@@ -16,7 +16,8 @@ kernels on it:
 
 They write the model's ``activeEdge``, ``activeTetrahedron`` and ``hole`` arrays, which the
 reference-shaped step reads live.  The batched step packs them into its plan, so a call
-that changes them bumps ``model.topologyVersion`` and the integrator rebuilds its plan.
+that changes them bumps ``model.topologyVersion`` and the integrator rebuilds its plan; a
+call that changes nothing (no edge broke, no tet overheated) leaves the plan as it is.
 
 The element maps the reference reads from its USD assets (``mapping:edgeToTriangles``,
 ``triangleToTetrahedron``, ``tetrahedronToTriangles``, ``tetrahedronNeighbors``) are taken
@@ -26,6 +27,8 @@ from a mesh dict when it carries them (``edge_to_triangles`` [E, 2],
 """
 
 from __future__ import annotations
+
+import contextlib
 
 import numpy as np
 import torch
@@ -175,8 +178,19 @@ class SimCutting:
         """The name the reference's launches use for ``flipEdge`` (integrator.py:2200)."""
         return self.flipEdge
 
-    def _touch(self) -> None:
-        self.model.topologyVersion += 1
+    @contextlib.contextmanager
+    def _topology_guard(self, stream=None):
+        """Bump ``model.topologyVersion`` when the enclosed calls (on ``stream``) change the
+        model's active values or holes, so the batched step rebuilds its plan only then."""
+        m = self.model
+        on = torch.cuda.stream(stream) if stream is not None else contextlib.nullcontext()
+        with on:
+            before = [t.clone() for t in (m.activeEdge, m.activeTetrahedron, m.hole)]
+        yield
+        with on:
+            after = (m.activeEdge, m.activeTetrahedron, m.hole)
+            if any(not torch.equal(a, b) for a, b in zip(before, after)):
+                m.topologyVersion += 1
 
     # ------------------------------------------------------------------ breaking
     def checkEdgeBreaking(self, breakFactor=None, breakThreshold=None, breakLimit: float = 1.0, stream=None):
@@ -186,6 +200,10 @@ class SimCutting:
         m, s = self.model, _lib.stream_handle(stream)
         bf = m.globalBreakFactor if breakFactor is None else breakFactor
         bt = m.globalBreakThreshold if breakThreshold is None else breakThreshold
+        with self._topology_guard(stream):
+            self._edge_breaking(m, s, bf, bt, breakLimit)
+
+    def _edge_breaking(self, m, s, bf, bt, breakLimit):
         check(lib().ffsrl_edge_breaker(ptr(m.predictedVertex), ptr(m.edge), ptr(m.edgeRestLength), ptr(m.activeEdge),
                                        ptr(self.edgeBreaker), m.numEdges, float(bf), float(bt), s))
         check(lib().ffsrl_check_edge_breaker(ptr(self.edgeBreaker), ptr(m.edge), ptr(m.activeEdge),
@@ -193,7 +211,6 @@ class SimCutting:
                                              ptr(m.activeTetrahedron), ptr(self.flipTetrahedron),
                                              ptr(self.edgesToTriangles), ptr(m.hole), float(breakLimit),
                                              ptr(self.edgeToEnv), ptr(m.envTetStartT), s))
-        self._touch()
 
     def checkTetrahedronBreaking(self, breakFactor=None, stream=None):
         """tetrahedronBreaker (integrator.py:777-818): accumulate each tet's overexpansion."""
@@ -223,11 +240,11 @@ class SimCutting:
         (integrator.py:874-918): overheated tets are flipped and open their surface."""
         m = self.model
         hl = m.globalHeatLimit if heatLimit is None else heatLimit
-        check(lib().ffsrl_check_heat(ptr(self.tetrahedronHeat), ptr(self.flipTetrahedron),
-                                     ptr(m.tetrahedronRestVolume) if volumeProportional else None,
-                                     ptr(self.tetrahedronToTriangle), ptr(m.hole), float(hl), m.numTetrahedrons,
-                                     _lib.stream_handle(stream)))
-        self._touch()
+        with self._topology_guard(stream):
+            check(lib().ffsrl_check_heat(ptr(self.tetrahedronHeat), ptr(self.flipTetrahedron),
+                                         ptr(m.tetrahedronRestVolume) if volumeProportional else None,
+                                         ptr(self.tetrahedronToTriangle), ptr(m.hole), float(hl), m.numTetrahedrons,
+                                         _lib.stream_handle(stream)))
 
     def heatLaparoscope(self, heatSphereRadius=None, heatQuantum=None, positions=None, stream=None):
         """heatLaparoscope (integrator.py:1153-1185): surface triangles near the midpoint of
@@ -248,18 +265,19 @@ class SimCutting:
         triangle are cut.  Positions default to the model's current vertices."""
         m = self.model
         x = m.vertex if positions is None else positions
-        check(lib().ffsrl_cut_edges(ptr(x), ptr(m.laparoscopeTip), ptr(m.edge), ptr(m.activeEdge), ptr(self.flipEdge),
-                                    m.numEdges, ptr(m.tetrahedron), m.numTetrahedrons, ptr(m.activeTetrahedron),
-                                    ptr(self.flipTetrahedron), ptr(self.edgesToTriangles), ptr(m.hole),
-                                    ptr(self.edgeToEnv), ptr(m.envTetStartT), _lib.stream_handle(stream)))
-        self._touch()
+        with self._topology_guard(stream):
+            check(lib().ffsrl_cut_edges(ptr(x), ptr(m.laparoscopeTip), ptr(m.edge), ptr(m.activeEdge),
+                                        ptr(self.flipEdge), m.numEdges, ptr(m.tetrahedron), m.numTetrahedrons,
+                                        ptr(m.activeTetrahedron), ptr(self.flipTetrahedron), ptr(self.edgesToTriangles),
+                                        ptr(m.hole), ptr(self.edgeToEnv), ptr(m.envTetStartT),
+                                        _lib.stream_handle(stream)))
 
     def updateActiveValues(self, stream=None):
         """inDeCreaseActiveValues (integrator.py:1583-1605) on the edges and the tets: flipped
         elements fade out (or in) over IN_DE_CREASE_STEPS calls."""
         m, s = self.model, _lib.stream_handle(stream)
-        check(lib().ffsrl_update_active_values(ptr(self.flipEdge), ptr(m.activeEdge), ptr(self.sqrtValues),
-                                               IN_DE_CREASE_STEPS, m.numEdges, s))
-        check(lib().ffsrl_update_active_values(ptr(self.flipTetrahedron), ptr(m.activeTetrahedron),
-                                               ptr(self.sqrtValues), IN_DE_CREASE_STEPS, m.numTetrahedrons, s))
-        self._touch()
+        with self._topology_guard(stream):
+            check(lib().ffsrl_update_active_values(ptr(self.flipEdge), ptr(m.activeEdge), ptr(self.sqrtValues),
+                                                   IN_DE_CREASE_STEPS, m.numEdges, s))
+            check(lib().ffsrl_update_active_values(ptr(self.flipTetrahedron), ptr(m.activeTetrahedron),
+                                                   ptr(self.sqrtValues), IN_DE_CREASE_STEPS, m.numTetrahedrons, s))

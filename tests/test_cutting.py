@@ -52,6 +52,10 @@ def test_breaking_and_fading_match_the_oracle(gpu, oracle_lib):
         c.checkTetrahedronBreaking(breakFactor=3.0)
         o.checkTetrahedronBreaking(breakFactor=3.0)
     _same(c, o, "breakers")
+    v = m.topologyVersion
+    c.checkEdgeBreaking(breakFactor=2.0, breakThreshold=1e9, breakLimit=1e9)  # nothing new breaks
+    assert m.topologyVersion == v
+    o.checkEdgeBreaking(breakFactor=2.0, breakThreshold=1e9, breakLimit=1e9)
     flipped = int((c.flipEdge == -1).sum())
     print(f"[cutting] {flipped} of {m.numEdges} edges broke, {int((c.flipTetrahedron == -1).sum())} tets, "
           f"{int(m.hole.sum())} holes")
