@@ -117,8 +117,7 @@ extern "C" int32_t ffsrl_create(const ffsrl_model* m, const ffsrl_params* p, int
     }
     h->params = *p;
     ffsrl_batch_options o{};
-    o.block_threads = block_threads;
-    o.deterministic = 1;
+    o.block_threads = block_threads;  // reference arithmetic, fixed-point sums
     if ((st = ffsrl_batch_create(m, &h->dev, &h->params, &o, &h->plan))) {
         std::string msg = ffsrl_last_error();
         h->plan = nullptr;
@@ -340,4 +339,17 @@ extern "C" int32_t ffsrl_render_handle(ffsrl_handle* h, const float* camera_pos,
     r.color = color;
     r.depth = depth;
     return ffsrl_render_fused(&r, &h->bvh, stream);
+}
+
+extern "C" int32_t ffsrl_render_handle_check(ffsrl_handle* h, void* stream) {
+    if (!h || !h->has_render) return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_render_handle_check: no render attached");
+    cudaStream_t s = (cudaStream_t)stream;
+    int32_t flag = 0;
+    FFSRL_CUDA_TRY(cudaMemcpyAsync(&flag, h->render.error_flag, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    FFSRL_CUDA_TRY(cudaStreamSynchronize(s));
+    if (flag == 0) return FFSRL_OK;
+    FFSRL_CUDA_TRY(cudaMemsetAsync(h->render.error_flag, 0, sizeof(int32_t), s));
+    FFSRL_CUDA_TRY(cudaStreamSynchronize(s));
+    return fail(flag == FFSRL_ERR_STACK_OVERFLOW ? FFSRL_ERR_STACK_OVERFLOW : FFSRL_ERR_CUDA,
+                "ffsrl_render_handle: a ray exhausted its BVH traversal stack since the last check");
 }

@@ -21,13 +21,16 @@ LIB = PKG / "libffsrl_cuda.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           f"-I{INCLUDE}", f"-I{CSRC}"]
-# per-unit extra flags: the reference-shaped step and the renderer round every product
-# as written (no fused multiply-add), like the CPU restatement; the batched step uses
-# the hardware's approximate division and square root (within 2 ulp)
+# per-unit extra flags: the reference-shaped step, the renderer and the reference-
+# arithmetic batched step round every product as written (no fused multiply-add), like
+# the CPU restatement; the fast batched step uses the hardware's approximate division and
+# square root (within 2 ulp)
 UNITS = {
     "capi.cu": [],
     "plain.cu": ["-fmad=false"],
     "batched.cu": ["-prec-div=false", "-prec-sqrt=false"],
+    "batched_ref.cu": ["-fmad=false"],
+    "batched_study.cu": ["-fmad=false"],
     "render.cu": ["-fmad=false"],
     "instrument.cu": ["-fmad=false"],
     "cutting.cu": ["-fmad=false"],

@@ -118,8 +118,17 @@ class ServerConfig(C.Structure):
                 ("env_inst_first_point", P), ("bvh", C.POINTER(Bvh)), ("vis_face", P), ("render", C.POINTER(Render))]
 
 
+# ffsrl_batch_options.arithmetic / .accumulation
+ARITH_REFERENCE = 0
+ARITH_FAST = 1
+ACC_FIXED = 0
+ACC_KAHAN = 1
+ACC_ATOMIC = 2
+
+
 class BatchOptions(C.Structure):
-    _fields_ = [("block_threads", I32), ("use_clusters", I32), ("deterministic", I32), ("reserved", I32 * 5)]
+    _fields_ = [("block_threads", I32), ("arithmetic", I32), ("accumulation", I32), ("precision", I32),
+                ("reserved", I32 * 4)]
 
 
 _lib = None
@@ -183,6 +192,7 @@ def lib() -> C.CDLL:
         "ffsrl_set_drag": ([P, P, I32, P], I32),
         "ffsrl_attach_render": ([P, C.POINTER(RenderConfig)], I32),
         "ffsrl_render_handle": ([P, P, P, I32, P, P, P], I32),
+        "ffsrl_render_handle_check": ([P, P], I32),
         "ffsrl_server_create": ([C.POINTER(ServerConfig), C.POINTER(P)], I32),
         "ffsrl_server_destroy": ([P], I32),
         "ffsrl_server_submit": ([P, I32, P, I32, I32, C.c_int64], I32),

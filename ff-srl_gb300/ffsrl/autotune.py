@@ -47,8 +47,9 @@ def _key(plan, cls) -> str:
     m = plan.model
     props = torch.cuda.get_device_properties(m.device)
     tets = int(sum(int(m.envTetStart[e + 1] - m.envTetStart[e]) for e in cls["envs"]))
-    sig = f"v3|{props.name}|{props.multi_processor_count}|{m.constraintFlags}|{m.simSubsteps}|{m.simConstraints}|" \
-          f"{cls['mode']}|{cls['max_nv']}|{len(cls['envs'])}|{tets}|{plan.precision}"
+    sig = f"v4|{props.name}|{props.multi_processor_count}|{m.constraintFlags}|{m.simSubsteps}|{m.simConstraints}|" \
+          f"{cls['mode']}|{cls['max_nv']}|{len(cls['envs'])}|{tets}|{plan.precision}|" \
+          f"{getattr(plan, 'arithmetic', '')}|{getattr(plan, 'accumulation', '')}"
     return hashlib.sha1(sig.encode()).hexdigest()[:16]
 
 

@@ -8,7 +8,12 @@ Two GPU forms with the same semantics:
 
 * ``batched=True`` (default): the env-resident batched kernel -- one persistent launch per
   mesh-size class, every substep and iteration of an environment on one SM, shared-memory
-  positions and deterministic fixed-point correction sums;
+  positions and deterministic fixed-point correction sums.  ``arithmetic="reference"``
+  (default) evaluates every constraint with the reference kernel's expressions (IEEE
+  division and square root, no fused multiply-add); ``"fast"`` uses hardware
+  reciprocals and a reformulated Neo-Hookean constraint.  ``accumulation`` selects
+  ``"fixed"`` (default), ``"kahan"`` (compensated float32) or ``"atomic"`` (float32
+  atomics, as the reference);
 * ``batched=False``: the reference-shaped form -- one kernel launch per reference kernel
   in the reference's launch order, float atomics.
 """
@@ -25,18 +30,27 @@ from . import _lib, graphs
 from ._lib import check, lib, ptr
 
 
+ARITHMETIC = {"reference": _lib.ARITH_REFERENCE, "fast": _lib.ARITH_FAST}
+ACCUMULATION = {"fixed": _lib.ACC_FIXED, "kahan": _lib.ACC_KAHAN, "atomic": _lib.ACC_ATOMIC}
+
+
 class BatchPlan:
     """Owner of an ffsrl_batch handle (packed constraint tables, work lists, streams)."""
 
-    def __init__(self, model, block_threads: int = 0, precision: int = 32):
+    def __init__(self, model, block_threads: int = 0, precision: int = 32, arithmetic: str = "reference",
+                 accumulation: str = "fixed"):
         model.require_cuda()
+        if arithmetic not in ARITHMETIC or accumulation not in ACCUMULATION:
+            raise ValueError(f"arithmetic in {list(ARITHMETIC)}, accumulation in {list(ACCUMULATION)}")
         hm, self._host_arrays = model.host_model()
         self._dm = model.device_model()
         self._params = model.params()
         opts = _lib.BatchOptions()
         opts.block_threads = int(block_threads)
-        opts.deterministic = 1
-        opts.reserved[0] = int(precision)
+        opts.arithmetic = ARITHMETIC[arithmetic]
+        opts.accumulation = ACCUMULATION[accumulation]
+        opts.precision = int(precision)
+        self.arithmetic, self.accumulation = arithmetic, accumulation
         h = C.c_void_p()
         check(lib().ffsrl_batch_create(C.byref(hm), C.byref(self._dm), C.byref(self._params), C.byref(opts),
                                        C.byref(h)))
@@ -92,9 +106,12 @@ class BatchPlan:
 class SimIntegratorDO:
     """Reference-compatible integrator: ``SimIntegratorDO(device).stepModel(simModel)``."""
 
-    def __init__(self, device="cuda:0", batched: bool = True, blockThreads: int = 0, autotune: bool = False) -> None:
+    def __init__(self, device="cuda:0", batched: bool = True, blockThreads: int = 0, autotune: bool = False,
+                 arithmetic: str = "reference", accumulation: str = "fixed") -> None:
         self.device = device
         self.batched = bool(batched)
+        self.arithmetic = arithmetic
+        self.accumulation = accumulation
         self.blockThreads = int(blockThreads)
         self.autotune = bool(autotune)
         self.tuning = None
@@ -108,7 +125,7 @@ class SimIntegratorDO:
         key = id(simModel)
         p = self._plans.get(key)
         if p is None or p.model is not simModel or p.version != simModel.topologyVersion:
-            p = BatchPlan(simModel, self.blockThreads)
+            p = BatchPlan(simModel, self.blockThreads, arithmetic=self.arithmetic, accumulation=self.accumulation)
             self._plans[key] = p
             if self.autotune and self.blockThreads == 0:
                 from .autotune import autotune

@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define FFSRL_ABI_VERSION 1
+#define FFSRL_ABI_VERSION 2
 
 typedef enum {
     FFSRL_OK = 0,
@@ -338,11 +338,27 @@ int32_t ffsrl_render_fused_envs(const ffsrl_render* r, const ffsrl_bvh* bvh, con
 
 /* ---- batched step ------------------------------------------------------------------ */
 typedef struct ffsrl_batch ffsrl_batch;
+/* Arithmetic of the batched step's constraint projections.  REFERENCE: each constraint
+   is evaluated with the reference kernel's expressions and association order, IEEE
+   division and square root, no fused multiply-add (per-constraint corrections equal the
+   serial restatement's).  FAST: one hardware reciprocal or reciprocal square root per
+   constraint, the Neo-Hookean constraint through M = Dm^-1 Dm^-T, multiply-add
+   contraction. */
+#define FFSRL_ARITH_REFERENCE 0
+#define FFSRL_ARITH_FAST      1
+/* Accumulation of per-vertex corrections.  FIXED: 32-bit fixed point per env scale with
+   an exact 64-bit side path (deterministic; the same bits alone or in any batch).
+   KAHAN: float32 (sum, compensation) pairs, compensated summation.  ATOMIC: plain
+   float32 atomics, as the reference accumulates. */
+#define FFSRL_ACC_FIXED  0
+#define FFSRL_ACC_KAHAN  1
+#define FFSRL_ACC_ATOMIC 2
 typedef struct {
-    int32_t block_threads;   /* 0 = autotuned */
-    int32_t use_clusters;    /* reserved */
-    int32_t deterministic;   /* 1 = fixed-point accumulation (default) */
-    int32_t reserved[5];
+    int32_t block_threads;   /* 0 = default per size class */
+    int32_t arithmetic;      /* FFSRL_ARITH_* (0 = reference) */
+    int32_t accumulation;    /* FFSRL_ACC_* (0 = fixed point) */
+    int32_t precision;       /* 32 (0 means 32) or 64: the float64 build, reference arithmetic */
+    int32_t reserved[4];
 } ffsrl_batch_options;
 
 /* Build the env-resident batch plan from HOST copies of the model arrays (host_model
@@ -430,6 +446,13 @@ typedef struct {
 int32_t ffsrl_attach_render(ffsrl_handle* handle, const ffsrl_render_config* config);
 int32_t ffsrl_render_handle(ffsrl_handle* handle, const float* camera_pos, const float* camera_rot, int32_t num_cameras,
                             float* color, float* depth, void* stream);
+/* Error state of the handle's ray-casts since the last check (the Python renderer's
+   checkErrors, which the reference lacks: its stack is unchecked, render.py:411-498).
+   Waits for `stream`, then returns FFSRL_ERR_STACK_OVERFLOW if a ray of a
+   ffsrl_render_handle call exhausted its traversal stack (its image then misses that
+   ray's hit), and clears the state; FFSRL_OK otherwise.  ffsrl_render_handle itself does
+   not wait for the GPU. */
+int32_t ffsrl_render_handle_check(ffsrl_handle* handle, void* stream);
 
 /* ---- CUDA graphs (the reference's wp.capture_begin / capture_end / capture_launch,
    bvh.py:442-451, render.py:1108-1112, tests/testLiverRetraction.py:77-85) ----------

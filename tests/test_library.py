@@ -29,7 +29,7 @@ def test_exports_every_declared_symbol(built_lib):
 
 
 def test_abi_version(built_lib):
-    assert L.lib().ffsrl_abi_version() == 1
+    assert L.lib().ffsrl_abi_version() == 2
 
 
 STRUCTS = {"ffsrl_model": L.Model, "ffsrl_params": L.Params, "ffsrl_bvh": L.Bvh, "ffsrl_render": L.Render,
