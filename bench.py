@@ -13,6 +13,12 @@ and a 128x128 (2x2 supersampled) depth + colour ray-cast per environment.
             per-env result (effector position + contact count, N x 4 float32)
   plain  -- the reference-shaped drop-in (one launch per reference kernel) on the same GPU
 
+Every env has a mesh of its own by default (config 2 draws a tet count per env);
+``--pool K`` draws the 4096 envs from K shared meshes instead.  ``--arithmetic`` picks the
+batched step's arithmetic for the headline (``fast``: hardware reciprocals; ``reference``:
+the reference kernels' own expressions, IEEE division and square root); the step kernel
+of the other form is timed beside it.
+
 `--impl reference` times the reference algorithm's CPU implementation (the C++
 restatement, all host threads) on a bounded sample of the same workload.
 """
@@ -37,7 +43,7 @@ sys.path.insert(0, str(ROOT / "ff-srl_gb300"))
 METRIC = "env-steps/s at 4096 envs"
 NUM_ENVS = 4096
 RES = 128
-POOL = 64
+POOL = 0  # 0: one mesh per env
 GRASP_RADIUS = 0.5  # cm: grasp the nearest surface vertex within this distance of the drag point
 EPISODE = 16  # RL episode length: every env returns to its rest state after this many steps
 
@@ -55,6 +61,10 @@ def parse():
     ap.add_argument("--serve-impl", choices=("native", "python"), default="native",
                     help="serving loop: the library's C server (ffsrl_server_*) or the Python EnvServer")
     ap.add_argument("--no-graph", action="store_true", help="launch the env-step eagerly instead of a CUDA graph")
+    ap.add_argument("--pool", type=int, default=POOL, help="distinct meshes the envs draw from (0: one per env)")
+    ap.add_argument("--arithmetic", choices=("fast", "reference"), default="fast",
+                    help="batched-step arithmetic of the headline")
+    ap.add_argument("--plain-steps", type=int, default=5)
     return ap.parse_args()
 
 
@@ -65,11 +75,12 @@ def dist_env():
     return rank, world, local
 
 
-def config(envs, n):
+def config(envs, n, pool=POOL, arithmetic="fast"):
     return {"workload": f"{envs} mixed-size ellipsoid envs (tets log-uniform 500-20000), 8 substeps x 10 iterations, "
                         f"Neo-Hookean+volume+distance+grasp+contact, kinematic instrument (rendered), BVH refit, "
                         f"{RES}x{RES} depth+colour ray-cast",
-            "envs_per_gpu": envs, "pool_meshes": POOL, "substeps": 8, "iterations": 10, "resolution": RES,
+            "envs_per_gpu": envs, "pool_meshes": pool if pool > 0 else envs, "substeps": 8, "iterations": 10,
+            "resolution": RES, "arithmetic": arithmetic,
             "parallelism": f"env-shard x{n}", "l2": "working set (GBs) exceeds the 129 MB L2; no flush needed",
             "episode_steps": EPISODE, "episode_reset": "all envs to rest state + grasp, inside the timed region"}
 
@@ -144,10 +155,10 @@ def algorithmic_bytes(model, substeps=8, iterations=10, nh=True):
     return substeps * (iterations * b_iter + V * 48)
 
 
-def build_workload(device, envs, seed):
+def build_workload(device, envs, seed, pool_size=POOL):
     import torch
     from ffsrl import SimBVH, SimIntegratorDO, WarpRaycastRendererDO, scenarios as sc
-    meshes, pool = sc.mixed_meshes(envs, pool_size=POOL, seed=seed)
+    meshes, pool = sc.mixed_meshes(envs, pool_size=pool_size, seed=seed)
     m, _ = sc.liver_model(device, envs, meshes=meshes)
     bvh = SimBVH(device, m)
     ap = sc.fov_aperture(60.0)
@@ -156,7 +167,7 @@ def build_workload(device, envs, seed):
     pos, rot = sc.env_cameras(meshes, seed=seed + 1)
     r.setCameras(pos, rot)
     m.graspNearest(torch.ones(envs, dtype=torch.int32, device=device), radius=GRASP_RADIUS)
-    return m, meshes, bvh, r
+    return m, meshes, pool, bvh, r
 
 
 def cpu_sample(meshes, threads, n_env=16):
@@ -180,13 +191,24 @@ def cpu_sample(meshes, threads, n_env=16):
     return n_env / dt, dt
 
 
+def warp_probe() -> str:
+    """Whether the reference's own kernels could run here: they need warp-lang 0.10.1
+    (FF_SRL/setup.py:24) for SimIntegratorDO.stepModel on device="cpu"."""
+    try:
+        import warp  # noqa: F401
+    except Exception as e:  # not installed on this image
+        return f"import warp failed: {type(e).__name__}: {e}"
+    return f"warp {getattr(warp, '__version__', '?')} imports"
+
+
 def reference_arm(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
+    probe = warp_probe()
     from ffsrl import scenarios as sc
     threads = os.cpu_count() or 1
-    meshes, _ = sc.mixed_meshes(args.envs, pool_size=POOL, seed=0)
+    meshes, _ = sc.mixed_meshes(args.envs, pool_size=args.pool, seed=0)
     sample = 32
     for _ in range(args.warmup):
         cpu_sample(meshes, threads, n_env=sample)
@@ -198,11 +220,14 @@ def reference_arm(args):
     line = {"metric": METRIC, "value": v, "unit": "env-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * sample / v, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-            "config": config(args.envs, world) | {"sample": f"{sample} envs x 1 step per timed step"},
+            "config": config(args.envs, world, args.pool, args.arithmetic) | {"sample": f"{sample} envs x 1 step per timed step"},
             "cpu_baseline": {"value": v, "unit": "env-steps/s", "cores": threads, "kind": "port",
                              "sample": f"{sample} envs of the same pool, 1 full env-step each (8x10 solve, refit, "
                                        f"{RES}x{RES} ray-cast), OpenMP over envs"},
-            "e2e": {"value": v, "unit": "env-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": v, "unit": "env-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "warp_probe": probe,
+            "reference_kind_reason": "the reference's Warp kernels need warp-lang 0.10.1, which this image lacks "
+                                     "(warp_probe); the arm times the C++ restatement of those kernels instead"}
     print(json.dumps(line))
 
 
@@ -219,11 +244,17 @@ def main():
     torch.cuda.set_device(local)
     device = f"cuda:{local}"
     envs = args.envs
-    m, meshes, bvh, r = build_workload(device, envs, seed=rank)
+    setup = {}
+    t_setup = time.perf_counter()
+    m, meshes, pool, bvh, r = build_workload(device, envs, seed=rank, pool_size=args.pool)
+    setup["workload_s"] = time.perf_counter() - t_setup
     from ffsrl import SimIntegratorDO, scenarios as sc, _lib as L
     from ffsrl.shard import max_over_ranks
-    integ = SimIntegratorDO(device, autotune=True)
+    t_setup = time.perf_counter()
+    integ = SimIntegratorDO(device, autotune=True, arithmetic=args.arithmetic)
     plan = integ.plan(m)
+    torch.cuda.synchronize()
+    setup["plan_and_autotune_s"] = time.perf_counter() - t_setup
     n_cls = plan.info()["num_classes"]
     K, W = args.steps, max(args.warmup, 3)
     walk = torch.as_tensor(sc.random_walk_steps(envs, K + W, seed=rank + 100), device=device)
@@ -310,6 +341,22 @@ def main():
     ks[1].record(stream)
     torch.cuda.synchronize()
     observe_ms = ks[0].elapsed_time(ks[1]) / kreps
+    # the step kernel in the other arithmetic form, same workload and episode phase
+    other = "reference" if args.arithmetic == "fast" else "fast"
+    t_other = time.perf_counter()
+    integ_o = SimIntegratorDO(device, autotune=True, arithmetic=other)
+    plan_o = integ_o.plan(m)
+    new_episode()
+    plan_o.step(1)
+    torch.cuda.synchronize()
+    ks[0].record(stream)
+    for _ in range(kreps):
+        plan_o.step(1)
+    ks[1].record(stream)
+    torch.cuda.synchronize()
+    other_kernel_ms = ks[0].elapsed_time(ks[1]) / kreps
+    setup["other_arithmetic_s"] = time.perf_counter() - t_other
+    del plan_o, integ_o
     alg = algorithmic_bytes(m)
     peak, peak_kind = peaks()
     achieved = alg / (step_kernel_ms / 1000.0) / 1e9
@@ -318,7 +365,9 @@ def main():
     if prof.exists():
         try:
             d = json.loads(prof.read_text())
-            traffic = d["dram_bytes_per_env_step"] * envs
+            rec = d.get(f"{args.arithmetic}|{'distinct' if args.pool <= 0 else 'pool' + str(args.pool)}")
+            if rec:
+                traffic = rec["dram_bytes_per_env_step"] * envs
         except Exception:
             traffic = None
 
@@ -359,7 +408,7 @@ def main():
         pint.stepModel(m, 1)
         torch.cuda.synchronize()
         pe = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-        pk = 2
+        pk = max(1, args.plain_steps)
         pe[0].record(stream)
         for k in range(pk):
             m.applyCartesianActionsInWorkspace(walk[k])
@@ -379,11 +428,11 @@ def main():
         # continuous-batching serving of the same pool: one closed-loop actor per env
         from ffsrl import scenarios as sc2
         from ffsrl.serve import EnvServer, NativeEnvServer
-        meshes_s, pool_s = sc2.mixed_meshes(envs, pool_size=POOL, seed=rank)
+        meshes_s, pool_s = meshes, pool
         ids = {id(mm): k for k, mm in enumerate(pool_s)}
         Server = NativeEnvServer if args.serve_impl == "native" else EnvServer
         srv = Server(pool_s, [ids[id(mm)] for mm in meshes_s], device, hbm_budget_bytes=60e9, resolution=RES,
-                     autotune=True)
+                     autotune=True, arithmetic=args.arithmetic)
         serving = srv.run_closed_loop(args.serve_seconds, think_hz=60.0, seed=rank, warmup_s=1.0)
         serving["server"] = args.serve_impl
         serving["what"] = ("closed-loop actors, Poisson think time at 60 Hz, each request = effector move + 8x10 step "
@@ -393,6 +442,7 @@ def main():
         cpu = None
         if not args.no_cpu:
             threads = os.cpu_count() or 1
+            cpu_sample(meshes[32:], threads, n_env=8)  # warm-up: page-in, thread pool, caches
             v, dt = cpu_sample(meshes, threads, n_env=32)
             cpu = {"value": v, "unit": "env-steps/s", "cores": threads, "kind": "port",
                    "sample": f"32 envs of the same pool, 1 full env-step (8x10 solve, refit, {RES}x{RES} ray-cast), "
@@ -403,14 +453,23 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": "env-steps/s", "n_gpus": world, "steps": K,
                 "warmup": W, "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded meshes and random-walk actions)",
-                "config": config(envs, world), "cuda_graph": not args.no_graph,
+                "config": config(envs, world, args.pool, args.arithmetic), "cuda_graph": not args.no_graph,
                 "latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99)),
                                "what": "full-batch step latency (all envs), per timed step"},
                 "e2e": {"value": e2e, "unit": "env-steps/s", "h2d_bytes_per_step": envs * 16,
                         "d2h_bytes_per_step": envs * 16},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                             "kernel": "k_batched (batched step, all size classes)", "kernel_ms": step_kernel_ms},
+                             "kernel": "k_batched (batched step, all size classes)", "kernel_ms": step_kernel_ms,
+                             "achieved_is": "algorithmic bytes of the step (every table and state byte of every "
+                                            "iteration) per second; the kernel keeps each env in shared memory "
+                                            "and L2, so DRAM moves a small fraction of them",
+                             "dram_gbs": (traffic / (step_kernel_ms / 1000.0) / 1e9) if traffic else None,
+                             "limiter": "instruction issue and the shared-memory pipe (profiles/k_batched_*.md)"},
+                "other_arithmetic": {"arithmetic": other, "kernel_ms": other_kernel_ms,
+                                     "what": "the batched step kernel of the other arithmetic form on the same "
+                                             "workload (autotuned), CUDA events"},
+                "setup_s": setup,
                 "observe_ms": {"value": observe_ms, "what": f"fused BVH refit + vertex normals + {RES}x{RES} "
                                                           "ray-cast of all envs, per step"},
                 "cpu_baseline": cpu, "plain": plain, "serving": serving, "gpu_launches": launches,

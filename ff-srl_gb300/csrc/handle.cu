@@ -179,6 +179,7 @@ extern "C" int32_t ffsrl_attach_render(ffsrl_handle* h, const ffsrl_render_confi
         return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_attach_render: missing arrays, bad sizes or mode");
     const int N = h->dev.num_envs;
     const int64_t P = c->num_points, Fv = c->num_faces;
+    const size_t owned0 = h->owned.size();  // buffers this call allocates come after these
     if (c->env_point_start[0] != 0 || c->env_point_start[N] != P || c->env_face_start[0] != 0 ||
         c->env_face_start[N] != Fv)
         return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_attach_render: env ranges do not cover the points and faces");
@@ -318,7 +319,16 @@ extern "C" int32_t ffsrl_attach_render(ffsrl_handle* h, const ffsrl_render_confi
     r.render_mode = c->render_mode;
     h->num_map = c->num_map;
     chk(upload_c(h, &h->point_to_vertex, c->point_to_vertex, 2ll * c->num_map, false));
-    if (st) return fail(st, std::string("ffsrl_attach_render: upload: ") + ffsrl_last_error());
+    if (st) {
+        // give back what this call allocated, so a retried attach does not accumulate them
+        for (size_t k = owned0; k < h->owned.size(); ++k) cudaFree(h->owned[k]);
+        h->owned.resize(owned0);
+        h->bvh = ffsrl_bvh{};
+        h->render = ffsrl_render{};
+        h->vis_point = nullptr;
+        h->point_to_vertex = nullptr;
+        return fail(st, std::string("ffsrl_attach_render: upload: ") + ffsrl_last_error());
+    }
     h->has_render = true;
     return FFSRL_OK;
 }

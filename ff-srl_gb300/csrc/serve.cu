@@ -335,9 +335,11 @@ extern "C" int32_t ffsrl_server_launch(ffsrl_server* S, int32_t max_batch, int32
         seen[r.actor] = 1;
         batch.push_back(r);
     }
-    S->pending.swap(rest);
     const int n = (int)batch.size();
-    if (!n) return FFSRL_OK;
+    if (!n) {
+        S->pending.swap(rest);
+        return FFSRL_OK;
+    }
     const ffsrl_server_config& c = S->cfg;
     const ffsrl_model& m = S->model;
     const int N = c.num_slots;
@@ -347,54 +349,66 @@ extern "C" int32_t ffsrl_server_launch(ffsrl_server* S, int32_t max_batch, int32
         const int s = S->actor_slot[r.actor];
         L.h_ids[i] = s;
         for (int k = 0; k < 3; ++k) L.h_disp[3 * i + k] = r.disp[k];
-        if (r.reset) {
-            L.h_rst[nr++] = s;
-            S->actor_clamp[r.actor] = 0;  // the grasp closes again below
-        }
+        if (r.reset) L.h_rst[nr++] = s;
     }
     for (int i = 0; i < n; ++i) {
         const Req& r = batch[i];
-        if (r.clamp != S->actor_clamp[r.actor]) {
+        // a reset opens the grasp; the clamp then closes again below if the request asks
+        const int cur = r.reset ? 0 : S->actor_clamp[r.actor];
+        if (r.clamp != cur) {
             L.h_gids[ng] = L.h_ids[i];
             L.h_gclamp[ng++] = r.clamp;
-            S->actor_clamp[r.actor] = r.clamp;
         }
     }
-    FFSRL_CUDA_TRY(cudaMemcpyAsync(L.d_ids, L.h_ids, sizeof(int) * n, cudaMemcpyHostToDevice, st));
-    FFSRL_CUDA_TRY(cudaMemcpyAsync(L.d_disp, L.h_disp, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, st));
-    int32_t e = FFSRL_OK;
-    if (nr) {
-        FFSRL_CUDA_TRY(cudaMemcpyAsync(L.d_rst, L.h_rst, sizeof(int) * nr, cudaMemcpyHostToDevice, st));
-        e = ffsrl_reset_envs(m.vertex, m.velocity, (float*)m.active_drag_constraint, c.initial_vertex,
-                             (float*)m.laparoscope_base, (float*)m.laparoscope_tip, c.initial_base, c.initial_tip,
-                             m.laparoscope_in_collision, c.xform, c.initial_xform, m.env_vertex_start, L.d_rst, nr, N, st);
+    // The queue and the clamp states change only once every launch of the tick has been
+    // issued: if one fails, the batch's requests stay queued in their order and the clamp
+    // states keep describing the device (launches already issued are not undone).
+    auto issue = [&]() -> int32_t {
+        FFSRL_CUDA_TRY(cudaMemcpyAsync(L.d_ids, L.h_ids, sizeof(int) * n, cudaMemcpyHostToDevice, st));
+        FFSRL_CUDA_TRY(cudaMemcpyAsync(L.d_disp, L.h_disp, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, st));
+        int32_t e = FFSRL_OK;
+        if (nr) {
+            FFSRL_CUDA_TRY(cudaMemcpyAsync(L.d_rst, L.h_rst, sizeof(int) * nr, cudaMemcpyHostToDevice, st));
+            e = ffsrl_reset_envs(m.vertex, m.velocity, (float*)m.active_drag_constraint, c.initial_vertex,
+                                 (float*)m.laparoscope_base, (float*)m.laparoscope_tip, c.initial_base, c.initial_tip,
+                                 m.laparoscope_in_collision, c.xform, c.initial_xform, m.env_vertex_start, L.d_rst, nr,
+                                 N, st);
+            if (e) return e;
+        }
+        if (c.xform)  // the effector moves through the instrument's kinematic chain
+            e = ffsrl_instrument_cartesian_envs(c.xform, L.d_disp, nullptr, nullptr, (float*)m.laparoscope_base,
+                                                (float*)m.laparoscope_tip, c.height, L.d_ids, n, N, st);
+        else
+            e = ffsrl_move_tool_envs((float*)m.laparoscope_base, (float*)m.laparoscope_tip, L.d_disp, L.d_ids, n, N,
+                                     st);
         if (e) return e;
-    }
-    if (c.xform)  // the effector moves through the instrument's kinematic chain
-        e = ffsrl_instrument_cartesian_envs(c.xform, L.d_disp, nullptr, nullptr, (float*)m.laparoscope_base,
-                                            (float*)m.laparoscope_tip, c.height, L.d_ids, n, N, st);
-    else
-        e = ffsrl_move_tool_envs((float*)m.laparoscope_base, (float*)m.laparoscope_tip, L.d_disp, L.d_ids, n, N, st);
-    if (e) return e;
-    if (ng) {
-        FFSRL_CUDA_TRY(cudaMemcpyAsync(L.d_gids, L.h_gids, sizeof(int) * ng, cudaMemcpyHostToDevice, st));
-        FFSRL_CUDA_TRY(cudaMemcpyAsync(L.d_gclamp, L.h_gclamp, sizeof(int) * ng, cudaMemcpyHostToDevice, st));
-        if ((e = ffsrl_grasp_nearest_envs(m.vertex, c.grasp_cand_start, c.grasp_cand, m.laparoscope_tip, L.d_gclamp,
-                                          c.grasp_radius, (float*)m.active_drag_constraint, L.d_gids, ng, N, st)))
+        if (ng) {
+            FFSRL_CUDA_TRY(cudaMemcpyAsync(L.d_gids, L.h_gids, sizeof(int) * ng, cudaMemcpyHostToDevice, st));
+            FFSRL_CUDA_TRY(cudaMemcpyAsync(L.d_gclamp, L.h_gclamp, sizeof(int) * ng, cudaMemcpyHostToDevice, st));
+            if ((e = ffsrl_grasp_nearest_envs(m.vertex, c.grasp_cand_start, c.grasp_cand, m.laparoscope_tip,
+                                              L.d_gclamp, c.grasp_radius, (float*)m.active_drag_constraint, L.d_gids,
+                                              ng, N, st)))
+                return e;
+        }
+        if ((e = ffsrl_batch_step_envs_lane(c.plan, li, L.h_ids, n, 1, st))) return e;
+        if ((e = ffsrl_remap_envs(c.vis_point, m.vertex, c.point_to_vertex, c.env_map_start, L.d_ids, n, N, st)))
             return e;
-    }
-    if ((e = ffsrl_batch_step_envs_lane(c.plan, li, L.h_ids, n, 1, st))) return e;
-    if ((e = ffsrl_remap_envs(c.vis_point, m.vertex, c.point_to_vertex, c.env_map_start, L.d_ids, n, N, st))) return e;
-    if (c.inst_num_points > 0 &&
-        (e = ffsrl_instrument_visual_update(c.xform, c.inst_local_point, c.inst_point_slot, c.inst_num_points,
-                                            c.vis_point, c.env_inst_first_point, L.d_ids, n, N, st)))
-        return e;
-    if ((e = ffsrl_bvh_refit_fused_envs(&S->bvh, c.vis_point, c.vis_face, L.d_ids, n, st))) return e;
-    if ((e = ffsrl_render_fused_envs(&S->render, &S->bvh, L.d_ids, n, st))) return e;
-    k_results<<<grid_for(n, 128), 128, 0, st>>>(m.laparoscope_tip, m.laparoscope_in_collision, L.d_ids, n, L.d_res);
-    FFSRL_LAUNCH_CHECK("ffsrl_server_launch: results");
-    FFSRL_CUDA_TRY(cudaMemcpyAsync(L.h_res, L.d_res, sizeof(float) * 4 * n, cudaMemcpyDeviceToHost, st));
-    FFSRL_CUDA_TRY(cudaEventRecord(L.done, st));
+        if (c.inst_num_points > 0 &&
+            (e = ffsrl_instrument_visual_update(c.xform, c.inst_local_point, c.inst_point_slot, c.inst_num_points,
+                                                c.vis_point, c.env_inst_first_point, L.d_ids, n, N, st)))
+            return e;
+        if ((e = ffsrl_bvh_refit_fused_envs(&S->bvh, c.vis_point, c.vis_face, L.d_ids, n, st))) return e;
+        if ((e = ffsrl_render_fused_envs(&S->render, &S->bvh, L.d_ids, n, st))) return e;
+        k_results<<<grid_for(n, 128), 128, 0, st>>>(m.laparoscope_tip, m.laparoscope_in_collision, L.d_ids, n,
+                                                    L.d_res);
+        FFSRL_LAUNCH_CHECK("ffsrl_server_launch: results");
+        FFSRL_CUDA_TRY(cudaMemcpyAsync(L.h_res, L.d_res, sizeof(float) * 4 * n, cudaMemcpyDeviceToHost, st));
+        FFSRL_CUDA_TRY(cudaEventRecord(L.done, st));
+        return FFSRL_OK;
+    };
+    if (int32_t e = issue()) return e;
+    S->pending.swap(rest);
+    for (const Req& r : batch) S->actor_clamp[r.actor] = r.clamp;
     ++S->clock;
     for (const Req& r : batch) {
         S->in_flight[r.actor] = 1;

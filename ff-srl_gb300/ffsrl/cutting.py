@@ -181,15 +181,22 @@ class SimCutting:
     @contextlib.contextmanager
     def _topology_guard(self, stream=None):
         """Bump ``model.topologyVersion`` when the enclosed calls (on ``stream``) change the
-        model's active values or holes, so the batched step rebuilds its plan only then."""
+        model's active values or holes, so the batched step rebuilds its plan only then.
+
+        The arrays are copied on the device before the calls and compared after them on
+        the device, reduced to one flag that is read back once: each guarded call waits for
+        its stream once, so it cannot be recorded into a CUDA graph."""
         m = self.model
         on = torch.cuda.stream(stream) if stream is not None else contextlib.nullcontext()
         with on:
             before = [t.clone() for t in (m.activeEdge, m.activeTetrahedron, m.hole)]
         yield
         with on:
-            after = (m.activeEdge, m.activeTetrahedron, m.hole)
-            if any(not torch.equal(a, b) for a, b in zip(before, after)):
+            changed = torch.zeros((), dtype=torch.bool, device=m.activeEdge.device)
+            for a, b in zip(before, (m.activeEdge, m.activeTetrahedron, m.hole)):
+                if a.numel():
+                    changed |= (a != b).any()
+            if bool(changed):
                 m.topologyVersion += 1
 
     # ------------------------------------------------------------------ breaking

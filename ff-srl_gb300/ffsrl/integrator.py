@@ -132,11 +132,20 @@ class SimIntegratorDO:
                 self.tuning = autotune(p)
         return p
 
-    def stepModel(self, simModel, steps: int = 1, stream=None, useGraph: bool = False) -> None:
+    def stepModel(self, simModel, steps: int = 1, stream=None, useGraph: bool = False,
+                  checkStatus: bool = False) -> None:
         """integrator.py:1640-1744: ``steps`` env-steps, then the visual points.  With
         ``useGraph`` the launches are captured into a CUDA graph on the first call and the
         graph is replayed afterwards (the reference RL loop's ``wp.capture_launch``,
-        ``tests/testLiverRetraction.py:77-85``); one graph per model and step count."""
+        ``tests/testLiverRetraction.py:77-85``); one graph per model and step count.
+        ``checkStatus`` waits for the step and raises if an env's state became non-finite
+        (the reference has no such check; without it, poll ``envStatus``)."""
+        if checkStatus:
+            self.stepModel(simModel, steps, stream, useGraph)
+            if stream is not None:
+                stream.synchronize()
+            self.checkStatus(simModel)
+            return
         simModel.require_cuda()
         if useGraph:
             from .graphs import Graph
@@ -152,8 +161,27 @@ class SimIntegratorDO:
             return
         self._step(simModel, steps, stream)
 
+    MAX_BATCHED_ENV_VERTICES = 65535  # env-local vertex ids of the batched tables are 16-bit
+
+    def routesToPlain(self, simModel) -> bool:
+        """True when the batched step cannot hold the model (an env with more than 65,535
+        vertices): stepModel then runs the reference-shaped step, which has no such limit."""
+        sizes = np.diff(np.asarray(simModel.envVertexStart, dtype=np.int64))
+        return bool(self.batched and len(sizes) and sizes.max() > self.MAX_BATCHED_ENV_VERTICES)
+
     def _step(self, simModel, steps, stream) -> None:
-        if self.batched:
+        if self.batched and self.routesToPlain(simModel):
+            if not getattr(self, "_warned_plain", False):
+                import warnings
+                warnings.warn("an env has more than 65,535 vertices: stepping this model with the reference-shaped "
+                              "step instead of the batched one")
+                self._warned_plain = True
+            m = simModel.device_model()
+            prm = simModel.params()
+            s = _lib.stream_handle(stream)
+            for _ in range(int(steps)):
+                check(lib().ffsrl_step_model(C.byref(m), C.byref(prm), s))
+        elif self.batched:
             self.plan(simModel).step(steps, stream)
         else:
             m = simModel.device_model()
@@ -165,5 +193,18 @@ class SimIntegratorDO:
         simModel.transformSimLaparoscopeMeshData(stream)
 
     def envStatus(self, simModel) -> np.ndarray:
-        """Per-env status of the last batched step (0 ok, 7 non-finite state)."""
+        """Per-env status of the last batched step (0 ok, 7 non-finite state); zeros for a
+        model the batched step routes to the reference-shaped step."""
+        if self.routesToPlain(simModel):
+            return np.zeros(simModel.numEnvs, dtype=np.int32)
         return self.plan(simModel).env_status()
+
+    def checkStatus(self, simModel) -> None:
+        """Raises FFSRLError (ERR_NONFINITE) naming the envs whose state the last batched
+        step left non-finite.  It reads the per-env status back from the device, so it
+        waits for the step; stepModel(checkStatus=True) calls it after every step."""
+        st = self.envStatus(simModel)
+        bad = np.nonzero(st)[0]
+        if len(bad):
+            raise _lib.FFSRLError(int(st[bad[0]]), f"non-finite state in envs {bad[:16].tolist()}"
+                                                   f"{' ...' if len(bad) > 16 else ''}")

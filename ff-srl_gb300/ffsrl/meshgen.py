@@ -97,16 +97,18 @@ def finalize_mesh(points: np.ndarray, tets: np.ndarray, density: float, fixed: n
     np.add.at(mass, tets.ravel(), np.repeat(rest_vol * density / 4.0, 4))
     inv_mass = np.where(fixed | (mass <= 0), 0.0, 1.0 / np.maximum(mass, 1e-300))
 
-    # unique edges
+    # unique edges (sorted id pairs, lexicographic; one int64 key per pair)
     e = np.sort(tets[:, _TET_EDGES].reshape(-1, 2), axis=1)
-    edges = np.unique(e, axis=0)
+    ekey = np.unique(e[:, 0] * nv + e[:, 1])
+    edges = np.stack([ekey // nv, ekey % nv], axis=1)
     rest_len = np.linalg.norm(rest[edges[:, 1]] - rest[edges[:, 0]], axis=1)
 
-    # boundary faces, oriented away from the opposite vertex
+    # boundary faces (used by one tet), oriented away from the opposite vertex
     faces = tets[:, _TET_FACES].reshape(-1, 3)
     opp = tets[:, _TET_FACE_OPP].reshape(-1)
     key = np.sort(faces, axis=1)
-    _, inv, cnt = np.unique(key, axis=0, return_inverse=True, return_counts=True)
+    fkey = (key[:, 0] * nv + key[:, 1]) * nv + key[:, 2]
+    _, inv, cnt = np.unique(fkey, return_inverse=True, return_counts=True)
     bnd = cnt[inv.ravel()] == 1
     faces, opp = faces[bnd], opp[bnd]
     a, b, c = rest[faces[:, 0]], rest[faces[:, 1]], rest[faces[:, 2]]
@@ -218,11 +220,46 @@ def ellipsoid_for_tets(target_tets: int, seed: int = 0, h: float = 0.6, **kw) ->
     return ellipsoid(semi_axes=tuple(base * best), h=h, seed=seed, **kw)
 
 
-def mixed_pool(num_meshes: int, seed: int = 0, t_lo: int = 500, t_hi: int = 20000) -> list[dict]:
-    """``num_meshes`` ellipsoids with tet targets drawn log-uniform in [t_lo, t_hi]."""
+_WORKER_MODULE = "_ffsrl_meshgen_worker"
+
+
+def _load_standalone():
+    """This file as a module of its own (numpy only): what the pool workers run, so that
+    they import neither torch nor the CUDA library."""
+    import importlib.util
+    import sys
+    mod = sys.modules.get(_WORKER_MODULE)
+    if mod is None:
+        spec = importlib.util.spec_from_file_location(_WORKER_MODULE, __file__)
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[_WORKER_MODULE] = mod
+        spec.loader.exec_module(mod)
+    return mod
+
+
+def _ellipsoid_job(args):
+    target, seed = args
+    return ellipsoid_for_tets(target, seed=seed)
+
+
+def mixed_pool(num_meshes: int, seed: int = 0, t_lo: int = 500, t_hi: int = 20000, workers: int = 0) -> list[dict]:
+    """``num_meshes`` ellipsoids with tet targets drawn log-uniform in [t_lo, t_hi].
+
+    ``workers`` > 1 builds them in that many spawned processes (0: one per host core for
+    pools of 256 meshes or more); the meshes are the same either way."""
     rng = np.random.Generator(np.random.PCG64(seed))
     targets = np.exp(rng.uniform(np.log(t_lo), np.log(t_hi), size=num_meshes))
-    return [ellipsoid_for_tets(int(t), seed=seed * 1000 + i) for i, t in enumerate(targets)]
+    jobs = [(int(t), seed * 1000 + i) for i, t in enumerate(targets)]
+    if workers == 0:
+        import os
+        workers = (os.cpu_count() or 1) if num_meshes >= 256 else 1
+    if workers <= 1:
+        return [_ellipsoid_job(j) for j in jobs]
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    mod = _load_standalone()
+    with ProcessPoolExecutor(workers, mp_context=mp.get_context("spawn"), initializer=_load_standalone) as ex:
+        return list(ex.map(mod._ellipsoid_job, jobs, chunksize=max(1, len(jobs) // (4 * workers))))
 
 
 def gravity_force(meshes, g: float = -981.0) -> tuple[float, float, float]:

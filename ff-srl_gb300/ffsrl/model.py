@@ -292,12 +292,13 @@ class SimModelDO:
         # all envs alike in their object face counts: the reference's layout assumption
         self.uniformVisLayout = bool(np.all(nvf == nvf[0]) and np.all(ng == ng[0]))
 
-        # synthetic instrument: 3 capsules + drag point per env, parked far above
+        # synthetic instrument: 3 capsules + drag point per env, parked far above the
+        # scene (out of reach of any mesh until a caller places it)
         r = np.asarray(toolRadius, dtype=np.float32)
         base = np.zeros((4 * N, 3), dtype=np.float32)
         tip = np.zeros((4 * N, 3), dtype=np.float32)
-        tip[:, 1] = 10.0
-        base[:, 1] = 10.1
+        tip[:, 1] = 1000.0
+        base[:, 1] = 1000.1
         rad = np.tile(np.array([r[0], r[1], r[2], 0.0], dtype=np.float32), N)
         self.toolHost = {"base": base, "tip": tip, "radius": rad}
 

@@ -192,7 +192,11 @@ def liver_model(device, num_envs, meshes=None, E=NH_E, nu=NH_NU, substeps=8, ite
 
 def mixed_meshes(num_envs: int, pool_size: int = 64, seed: int = 0, t_lo: int = 500, t_hi: int = 20000):
     """Config 2 pool: ``pool_size`` ellipsoids with tet targets log-uniform in [t_lo, t_hi],
-    each env drawing one (seeded)."""
+    each env drawing one (seeded).  ``pool_size`` 0 (or the env count) gives every env a
+    mesh of its own, as config 2 draws a tet count per env."""
+    if pool_size <= 0 or pool_size == num_envs:
+        pool = mg.mixed_pool(num_envs, seed=seed, t_lo=t_lo, t_hi=t_hi)
+        return list(pool), pool
     pool = mg.mixed_pool(pool_size, seed=seed, t_lo=t_lo, t_hi=t_hi)
     rng = np.random.Generator(np.random.PCG64(seed + 17))
     pick = rng.integers(0, pool_size, size=num_envs)

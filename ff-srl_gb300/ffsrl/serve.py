@@ -97,7 +97,8 @@ class _Lane:
 
 class EnvServer:
     def __init__(self, pool: list, actor_mesh, device="cuda:0", hbm_budget_bytes: float = 60e9, resolution: int = 128,
-                 lanes: int = 2, seed: int = 0, autotune: bool = False, block_threads: int = 0, **model_kw):
+                 lanes: int = 2, seed: int = 0, autotune: bool = False, block_threads: int = 0,
+                 arithmetic: str = "reference", **model_kw):
         self.device = torch.device(device)
         self.pool = pool
         self.actor_mesh = np.asarray(actor_mesh, dtype=np.int64)
@@ -112,7 +113,7 @@ class EnvServer:
         self.budget_used = float((k * per).sum())
         meshes = [pool[m] for m in self.slot_mesh]
         self.model, _ = sc.liver_model(device, self.num_slots, meshes=meshes, **model_kw)
-        self.integ = SimIntegratorDO(device, blockThreads=block_threads, autotune=autotune)
+        self.integ = SimIntegratorDO(device, blockThreads=block_threads, autotune=autotune, arithmetic=arithmetic)
         self.plan = self.integ.plan(self.model)
         self.bvh = SimBVH(device, self.model)
         ap = sc.fov_aperture(60.0)

@@ -55,15 +55,33 @@ def test_env_too_large_for_the_batched_step(gpu, oracle_lib):
     big = mg.beam(40, 40, 40)  # 41^3 = 68,921 vertices: more than 16-bit env-local ids hold
     assert len(big["vertex"]) > 65535
     m = SimModelDO(big, 1, "cuda:0", simSubsteps=1, simConstraintsSteps=1, environmentGroundLevel=-100.0)
+    from ffsrl.integrator import BatchPlan
     with pytest.raises(L.FFSRLError) as err:
-        SimIntegratorDO("cuda:0").stepModel(m)
+        BatchPlan(m)  # the batched tables cannot hold it
     assert err.value.code == L.ERR_UNSUPPORTED
+    # the integrator routes the model to the reference-shaped step instead
+    integ = SimIntegratorDO("cuda:0")
+    assert integ.routesToPlain(m)
     o = oracle.OracleSim(m)
-    SimIntegratorDO("cuda:0", batched=False).stepModel(m)
+    with pytest.warns(UserWarning, match="65,535"):
+        integ.stepModel(m)
     o.step(1)
     torch.cuda.synchronize()
     x = m.vertex.cpu().numpy()
     assert np.abs(x - o.a["vertex"]).max() / np.abs(o.a["vertex"]).max() < 1e-5
+    assert integ.envStatus(m).tolist() == [0]
+
+
+def test_check_status_raises_on_a_non_finite_env(gpu):
+    mesh = mg.ellipsoid_for_tets(600, seed=1)
+    from ffsrl import scenarios as sc
+    m, _ = sc.liver_model("cuda:0", 3, meshes=[mesh] * 3)
+    integ = SimIntegratorDO("cuda:0")
+    integ.stepModel(m, 1, checkStatus=True)  # finite: no error
+    m.vertex[m.envSlice(2).start + 3, 1] = float("inf")
+    with pytest.raises(L.FFSRLError) as err:
+        integ.stepModel(m, 1, checkStatus=True)
+    assert err.value.code == L.ERR_NONFINITE and "[2]" in str(err.value)
 
 
 def test_zero_steps_and_unreachable_grasp(gpu):

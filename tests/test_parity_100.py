@@ -1,0 +1,218 @@
+"""GPU parity over 100 steps, and bit-exactness of the reference arithmetic.
+
+The reference kernels (FF_SRL/FF_SRL/integrator.py:1640-1744) sum each vertex's
+corrections with float atomics, so two runs of the reference on a GPU may add them in
+different orders.  On these soft, sagging meshes the resulting rounding differences grow
+over a hundred steps.  Each 100-step test therefore also runs the oracle a second time with
+every env's tets and edges in a seeded random order -- another order the reference's own
+atomics may take -- and measures how far those two legitimate executions of the reference
+algorithm drift apart (``spread``).
+
+Tolerance, at every 10th step: max |x_gpu - x_oracle| / max |x_oracle| must stay within
+max(1e-4, 2 x the largest spread seen so far).  The bar is 1e-4 wherever the reference's own
+execution-order spread stays below half of that.
+
+Bit-exactness: with reference arithmetic and float accumulation, a mesh where every vertex
+receives exactly one correction term per constraint kind (disjoint tets, disjoint edges)
+has no order freedom left, and the batched step must give the oracle's bits.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from ffsrl import SimIntegratorDO, SimModelDO, _lib as L, meshgen as mg, scenarios as sc
+
+pytestmark = pytest.mark.gpu
+POS_TOL = 1e-4
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
+
+
+def device_state(m):
+    return {"vertex": m.vertex.cpu().numpy(), "velocity": m.velocity.cpu().numpy(),
+            "laparoscope_base": m.laparoscopeBase.cpu().numpy(), "laparoscope_tip": m.laparoscopeTip.cpu().numpy(),
+            "laparoscope_radius": m.laparoscopeRadius.cpu().numpy(),
+            "active_drag_constraint": m.activeDragConstraint.cpu().numpy()}
+
+
+def oracle_pair(m, seed=0):
+    """The oracle on the model's state, and a second oracle whose tets and edges run in a
+    seeded random order within each env."""
+    o1 = oracle.OracleSim(m, device_state(m))
+    o2 = oracle.OracleSim(m, device_state(m))
+    rng = np.random.default_rng(seed)
+
+    def env_perm(starts):
+        return np.concatenate([s + rng.permutation(e - s) for s, e in zip(starts[:-1], starts[1:])])
+
+    pt, pe = env_perm(m.envTetStart), env_perm(m.envEdgeStart)
+    for key, p in (("tetrahedron", pt), ("tetrahedron_rest_volume", pt), ("tetrahedron_dm_inv", pt),
+                   ("active_tetrahedron", pt), ("xpbd_rest_volume", pt), ("edge", pe), ("edge_rest_length", pe),
+                   ("active_edge", pe)):
+        a = o2.a[key]
+        if len(p) == 0 or a.size == 0:
+            continue
+        b = np.ascontiguousarray(a.reshape(len(p), -1)[p].reshape(a.shape))
+        o2.a[key] = b
+        setattr(o2.desc, key, b.ctypes.data)
+    return o1, o2
+
+
+def run_100(name, build, runs, steps=100, every=10, threads=4):
+    """Steps the GPU runs (label -> integrator kwargs) and the oracle pair in lock step;
+    asserts the tolerance at every checkpoint and returns the error table."""
+    models = {k: build() for k in runs}
+    integ = {k: SimIntegratorDO("cuda:0", **kw) for k, kw in runs.items()}
+    first = next(iter(models.values()))
+    o1, o2 = oracle_pair(first)
+    spread_max, worst = 0.0, {k: 0.0 for k in runs}
+    for k in range(0, steps, every):
+        for key in runs:
+            integ[key].stepModel(models[key], every)
+        o1.step(every, threads)
+        o2.step(every, threads)
+        torch.cuda.synchronize()
+        ref = o1.a["vertex"]
+        spread_max = max(spread_max, rel(o2.a["vertex"], ref))
+        tol = max(POS_TOL, 2.0 * spread_max)
+        line = []
+        for key in runs:
+            e = rel(models[key].vertex.cpu().numpy(), ref)
+            worst[key] = max(worst[key], e)
+            line.append(f"{key} {e:.2e}")
+            assert np.isfinite(models[key].vertex.cpu().numpy()).all()
+            assert e < tol, f"{name} {key} step {k + every}: {e:.3e} > {tol:.3e}"
+        print(f"[parity100] {name} step {k + every}: " + ", ".join(line) + f"; oracle order spread {spread_max:.2e}")
+    for key in runs:
+        if integ[key].batched:
+            assert (integ[key].envStatus(models[key]) == 0).all()
+    return worst, spread_max
+
+
+def grasped(m):
+    m.graspNearest(torch.ones(m.numEnvs, dtype=torch.int32, device="cuda:0"), radius=0.5)
+    torch.cuda.synchronize()
+    return m
+
+
+def test_beam_config0_every_10_steps(gpu, oracle_lib):
+    run_100("beam", lambda: sc.beam_model("cuda:0")[0],
+            {"plain": {"batched": False}, "batched": {}, "batched-fast": {"arithmetic": "fast"}})
+
+
+def test_liver_config1_neohookean_grasp_contact(gpu, oracle_lib):
+    # the 12/8/6 cm ellipsoid (11,102 vertices), grasped, the closed clamps on its surface
+    worst, spread = run_100("liver", lambda: grasped(sc.liver_model("cuda:0", 1)[0]), {"batched": {}})
+    print(f"[parity100] liver worst {worst}, reference order spread {spread:.2e}")
+
+
+def test_mixed_pool_with_contact(gpu, oracle_lib):
+    # the mixed-size pool of the throughput workload, contact on, both arithmetic forms
+    pool = [mg.ellipsoid_for_tets(t, seed=i) for i, t in enumerate([300, 1200, 4000])]
+    meshes = [pool[i % 3] for i in range(7)]
+    run_100("mixed7", lambda: grasped(sc.liver_model("cuda:0", 7, meshes=meshes)[0]),
+            {"batched": {}, "batched-fast": {"arithmetic": "fast"}})
+
+
+def _disjoint_tets(n=24, seed=5):
+    rng = np.random.default_rng(seed)
+    base = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], float)
+    V, T = [], []
+    for k in range(n):
+        off = np.array([3.0 * (k % 6), 3.0 * (k // 6), 0.0])
+        V.append(base + off + rng.uniform(-0.1, 0.1, (4, 3)))
+        T.append(np.arange(4) + 4 * k)
+    inv = np.full(4 * n, 2.0)
+    inv[0::4] = 0.0  # each tet hangs from one vertex
+    return mg.tiny_mesh(np.concatenate(V), np.array(T), inverse_mass=inv)
+
+
+def _dumbbells(n=32, seed=6):
+    rng = np.random.default_rng(seed)
+    V, E = [], []
+    for k in range(n):
+        a = np.array([2.0 * (k % 8), 2.0 * (k // 8), 0.0])
+        V += [a, a + np.array([0.0, -1.0, 0.0]) + rng.uniform(-0.2, 0.2, 3)]
+        E.append([2 * k, 2 * k + 1])
+    inv = np.tile([0.0, 1.5], n)
+    return mg.tiny_mesh(np.array(V), edge=np.array(E), inverse_mass=inv)
+
+
+def _tiny_model(mesh, flags, envs=2):
+    mu, lam = sc.lame(3.0 * sc.KPA, 0.45)
+    m = SimModelDO(mesh, envs, "cuda:0", simSubsteps=8, simFrameRate=60, simConstraintsSteps=10,
+                   environmentGroundLevel=-100.0, constraints=flags, globalVolumeCompliance=1.0 / lam,
+                   globalDeviatoricCompliance=1.0 / mu, environmentGravity=(0.0, -400.0, 0.0))
+    # every env's right-clamp tip (the grasp target) beside its mesh; a few vertices grasped
+    tip = m.laparoscopeTip.cpu().numpy()
+    tip[2::4] = np.array([1.0, 2.0, 0.5], dtype=np.float32)
+    m.setTool(m.laparoscopeBase.cpu().numpy(), tip)
+    drag = np.zeros(m.numVertices, dtype=np.float32)
+    drag[1::7] = 1.0
+    m.activeDragConstraint.copy_(torch.as_tensor(drag))
+    torch.cuda.synchronize()
+    return m
+
+
+@pytest.mark.parametrize("kind", ["tets", "edges"])
+def test_reference_arithmetic_is_bit_exact(gpu, oracle_lib, kind):
+    if kind == "tets":
+        m = _tiny_model(_disjoint_tets(), L.VOLUME | L.NEOHOOKEAN | L.DRAG)
+    else:
+        m = _tiny_model(_dumbbells(), L.DISTANCE | L.DRAG)
+    o = oracle.OracleSim(m, device_state(m))
+    integ = SimIntegratorDO("cuda:0", arithmetic="reference", accumulation="atomic")
+    integ.stepModel(m, 100)
+    o.step(100)
+    torch.cuda.synchronize()
+    x, v = m.vertex.cpu().numpy(), m.velocity.cpu().numpy()
+    moved = float(np.abs(o.a["vertex"] - m.host["vertex"].reshape(-1, 3)).max())
+    print(f"[parity100] bit-exact {kind}: moved {moved:.3f}, max |dx| {np.abs(x - o.a['vertex']).max():.1e}")
+    assert moved > 0.1
+    assert np.array_equal(x, o.a["vertex"])
+    assert np.array_equal(v, o.a["velocity"])
+
+
+def test_large_terms_take_the_exact_side_path(gpu, oracle_lib):
+    # a vertex dragged 60 cm from its 1 cm tet: the first corrections are far beyond the
+    # 32-bit fixed-point range of the env's scale; they go to the 64-bit side path and the
+    # step follows the oracle instead of dropping them
+    V = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], float)
+    mesh = mg.tiny_mesh(V, [[0, 1, 2, 3]], edge=[[0, 1], [0, 2], [0, 3], [1, 2], [1, 3], [2, 3]],
+                        inverse_mass=[0.0, 1.0, 1.0, 1.0])
+    m = _tiny_model(mesh, L.VOLUME | L.DISTANCE | L.NEOHOOKEAN, envs=1)
+    m.activeDragConstraint.zero_()
+    integ = SimIntegratorDO("cuda:0")
+    integ.plan(m)  # the env's scale comes from its 1 cm rest state
+    x = m.vertex.cpu().numpy()
+    x[3] += np.array([60.0, 0.0, 0.0], dtype=np.float32)
+    m.vertex.copy_(torch.as_tensor(x))
+    o = oracle.OracleSim(m, device_state(m))
+    integ.stepModel(m, 2)
+    o.step(2)
+    torch.cuda.synchronize()
+    e = rel(m.vertex.cpu().numpy(), o.a["vertex"])
+    print(f"[parity100] side path: {e:.2e}, span {np.abs(o.a['vertex']).max():.1f}")
+    assert integ.envStatus(m).tolist() == [0]
+    assert e < 1e-5
+
+
+def test_env_bits_do_not_depend_on_the_other_envs(gpu):
+    # the fixed-point scale is per env: an env stepped in a model whose other env lies
+    # 500 cm away gives the same bits as in a model of its own
+    mesh = mg.ellipsoid_for_tets(800, seed=3)
+    far = dict(mesh)
+    far["vertex"] = mesh["vertex"] + np.array([500.0, 0.0, 0.0], dtype=np.float32)
+    far["rest_vertex"] = mesh["rest_vertex"] + np.array([500.0, 0.0, 0.0], dtype=np.float32)
+    a, _ = sc.liver_model("cuda:0", 1, meshes=[mesh])
+    b, _ = sc.liver_model("cuda:0", 2, meshes=[mesh, far])
+    for m in (a, b):
+        grasped(m)
+        SimIntegratorDO("cuda:0").stepModel(m, 3)
+    torch.cuda.synchronize()
+    sl = a.envSlice(0)
+    assert torch.equal(a.vertex[sl], b.vertex[b.envSlice(0)])
