@@ -28,6 +28,11 @@ kern_f pick_fast_fixed(int block, int mode, int prefetch, unsigned flags) {
         if (block == 768) return k_batched<AccFixed, 768, 0, false, kLiverFlags, false>;
         if (block == 1024) return k_batched<AccFixed, 1024, 0, false, kLiverFlags, false>;
     }
+    if (flags == kLiverFlags && mode == 0 && prefetch == 2) {
+        if (block == 512) return k_batched<AccFixed, 512, 0, true, kLiverFlags, false>;
+        if (block == 640) return k_batched<AccFixed, 640, 0, true, kLiverFlags, false>;
+        return nullptr;
+    }
     if (prefetch == 2) {
         if (mode == 0 && block == 512) return k_batched<AccFixed, 512, 0, true, 0, false>;
         if (mode == 0 && block == 640) return k_batched<AccFixed, 640, 0, true, 0, false>;
@@ -55,6 +60,8 @@ struct ffsrl_batch {
     EnvRec* d_env = nullptr;
     uint2* d_tet_idx = nullptr; float2* d_tet_va = nullptr;
     float4* d_nh0 = nullptr; float4* d_nh1 = nullptr; float* d_tet_vs = nullptr; float4* d_tet_ed = nullptr;
+    float2* d_tet_ed2 = nullptr;  // compact fast-form folded edges
+    int compact = 0;              // compact fast-form tet records (48 bytes a tet)
     unsigned* d_edge_idx = nullptr; float2* d_edge_la = nullptr; uint2* d_tri_idx = nullptr;
     int* d_work = nullptr; int* d_counters = nullptr; int* d_status = nullptr;
     unsigned char* d_scratch = nullptr;
@@ -122,7 +129,7 @@ void free_batch(ffsrl_batch* b) {
     cudaFree(b->d_state64); cudaFree(b->d_cnt0); cudaFree(b->d_tet_orig);
     cudaFree(b->d_edge_orig);
     cudaFree(b->d_conn_idx); cudaFree(b->d_conn_bar); cudaFree(b->d_conn_vert); cudaFree(b->d_pend); cudaFree(b->d_pcnt);
-    cudaFree(b->d_wide); cudaFree(b->d_nhd);
+    cudaFree(b->d_wide); cudaFree(b->d_nhd); cudaFree(b->d_tet_ed2);
     for (auto& l : b->lanes) {
         for (auto s : l.streams) if (s) cudaStreamDestroy(s);
         for (auto e : l.done) if (e) cudaEventDestroy(e);
@@ -185,7 +192,8 @@ Dev<float> make_dev_f(ffsrl_batch* b) {
     D.env_status = b->d_status;
     D.cnt0 = b->d_cnt0; D.tet_orig = b->d_tet_orig; D.edge_orig = b->d_edge_orig;
     D.nhd = b->d_nhd; D.wide = b->d_wide; D.bound = b->bound;
-    D.tet_ed = b->d_tet_ed; D.fold = b->d_tet_ed != nullptr;
+    D.tet_ed = b->d_tet_ed; D.tet_ed2 = b->d_tet_ed2; D.compact = b->compact;
+    D.fold = b->d_tet_ed != nullptr || b->d_tet_ed2 != nullptr;
     D.conn_idx = b->d_conn_idx; D.conn_bar = b->d_conn_bar; D.conn_vert = b->d_conn_vert;
     D.pend = b->d_pend; D.pcnt = b->d_pcnt;
     D.conn_w = p.connector_mass_weight_ratio; D.conn_ks = p.connector_ks; D.conn_mul = p.connector_rest_length_mul;
@@ -229,7 +237,7 @@ template <> int32_t launch_class<double>(ffsrl_batch* b, const ffsrl_batch::Clas
     D.cnt0 = F.cnt0; D.tet_orig = F.tet_orig; D.edge_orig = F.edge_orig;
     D.nhd = F.nhd; D.wide = F.wide; D.bound = F.bound; D.pend = nullptr; D.pcnt = nullptr;
     D.conn_idx = nullptr; D.conn_bar = nullptr; D.conn_vert = nullptr;
-    D.tet_ed = F.tet_ed; D.fold = F.fold;
+    D.tet_ed = F.tet_ed; D.tet_ed2 = nullptr; D.compact = 0; D.fold = F.fold;
     D.iterations = F.iterations; D.dt = F.dt; D.gx = F.gx; D.gy = F.gy; D.gz = F.gz; D.damping = F.damping;
     D.ground = F.ground; D.ks_distance = F.ks_distance; D.ks_volume = F.ks_volume; D.ks_contact = F.ks_contact;
     D.ks_drag = F.ks_drag; D.vol_c = F.vol_c; D.dev_c = F.dev_c; D.a_dist = F.a_dist; D.a_vol = F.a_vol;
@@ -643,6 +651,9 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
     std::vector<unsigned char> tet_cls(T, 0);
     const bool fold = (fl & FFSRL_DISTANCE) && !(fl & FFSRL_DISTANCE_XPBD) &&
                       (fl & (FFSRL_VOLUME | FFSRL_VOLUME_XPBD | FFSRL_NEOHOOKEAN)) && T > 0 && E > 0;
+    // fast form with Neo-Hookean and folded edges: 48-byte tet records (see below)
+    const bool compact = !ex && nh && fold;
+    b->compact = compact ? 1 : 0;
     if (fold) {
         tet_ed.assign(T, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
         std::vector<unsigned> n_edge_idx;
@@ -695,6 +706,11 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
                 const float2 la = edge_la[k];
                 const float w = hm->inverse_mass[r.v0 + a] + hm->inverse_mass[r.v0 + c];
                 if (la.y == 0.0f || la.x < feps || w < feps) continue;  // never contributes or counts
+                if (compact && la.y != 1.0f) {  // compact records fold fully active edges only
+                    n_edge_idx.push_back(edge_idx[k]);
+                    n_edge_la.push_back(la);
+                    continue;
+                }
                 int best = -1, best_slot = 0;
                 for (int j = adj_start[a]; j < adj_start[a + 1]; ++j) {
                     const int t = adj[j];
@@ -917,6 +933,24 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
         permute(tet_vs, tet_orig); permute(tet_ed, tet_orig); permute(edge_idx, edge_orig); permute(edge_la, edge_orig);
     }
 
+    // ---- compact fast-form records: the rest volume carries the volume constraint's
+    // activity in its sign (the constraint runs only for activity 1, and then multiplies by
+    // it exactly), so nh1.w holds +-|V0| and the tet needs no (V0, active) pair; 1/|V0| is
+    // formed in the kernel.  Folded edges are all fully active, so their slots hold the
+    // rest lengths alone, 0 for none. ----
+    std::vector<float2> tet_ed2;
+    if (compact) {
+        tet_ed2.resize(T);
+        for (int64_t t = 0; t < T; ++t) {
+            const float v0 = std::fabs(tet_va[t].x);
+            nh1[t].w = tet_va[t].y == 1.0f ? v0 : -v0;
+            const float4 ed = tet_ed[t];
+            tet_ed2[t] = make_float2(ed.y != 0.0f ? ed.x : 0.0f, ed.w != 0.0f ? ed.z : 0.0f);
+        }
+        std::vector<float2>().swap(tet_va);
+        std::vector<float4>().swap(tet_ed);
+    }
+
     // ---- share identical constraint tables: envs of one mesh read the same records ----
     {
         for (int e = 0; e < N; ++e) {
@@ -936,6 +970,7 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
             };
             return a.nv == c.nv && a.nt == c.nt && a.ne == c.ne && a.nf == c.nf &&
                    eq(tet_idx, a.t0, c.t0, a.nt) && eq(tet_va, a.t0, c.t0, a.nt) && eq(nh0, a.t0, c.t0, a.nt) &&
+                   eq(tet_ed2, a.t0, c.t0, a.nt) &&
                    eq(nhd, 3 * a.t0, 3 * c.t0, 3 * a.nt) &&
                    eq(nh1, a.t0, c.t0, a.nt) && eq(tet_vs, a.t0, c.t0, a.nt) && eq(tet_ed, a.t0, c.t0, a.nt) &&
                    eq(tet_orig, a.t0, c.t0, a.nt) && eq(edge_idx, a.e0, c.e0, a.ne) && eq(edge_la, a.e0, c.e0, a.ne) &&
@@ -943,6 +978,7 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
         };
         std::vector<uint2> c_tet_idx; std::vector<float2> c_tet_va; std::vector<float4> c_nh0, c_nh1, c_nhd;
         std::vector<float> c_tet_vs; std::vector<float4> c_tet_ed; std::vector<int> c_tet_orig, c_edge_orig;
+        std::vector<float2> c_tet_ed2;
         std::vector<unsigned> c_edge_idx; std::vector<float2> c_edge_la; std::vector<uint2> c_tri_idx;
         std::unordered_map<uint64_t, std::vector<int>> seen;
         std::vector<EnvRec> out = env;
@@ -966,6 +1002,7 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
             out[e].t0 = (int)c_tet_idx.size(); out[e].e0 = (int)c_edge_idx.size(); out[e].f0 = (int)c_tri_idx.size();
             app(c_tet_idx, tet_idx, r.t0, r.nt); app(c_tet_va, tet_va, r.t0, r.nt); app(c_nh0, nh0, r.t0, r.nt);
             app(c_nhd, nhd, 3 * r.t0, 3 * r.nt);
+            app(c_tet_ed2, tet_ed2, r.t0, r.nt);
             app(c_nh1, nh1, r.t0, r.nt); app(c_tet_vs, tet_vs, r.t0, r.nt); app(c_tet_ed, tet_ed, r.t0, r.nt);
             app(c_tet_orig, tet_orig, r.t0, r.nt); app(c_edge_idx, edge_idx, r.e0, r.ne);
             app(c_edge_la, edge_la, r.e0, r.ne); app(c_edge_orig, edge_orig, r.e0, r.ne);
@@ -973,6 +1010,7 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
         }
         env = out;
         tet_idx.swap(c_tet_idx); tet_va.swap(c_tet_va); nh0.swap(c_nh0); nh1.swap(c_nh1); nhd.swap(c_nhd);
+        tet_ed2.swap(c_tet_ed2);
         tet_vs.swap(c_tet_vs); tet_ed.swap(c_tet_ed); tet_orig.swap(c_tet_orig); edge_idx.swap(c_edge_idx); edge_la.swap(c_edge_la);
         edge_orig.swap(c_edge_orig); tri_idx.swap(c_tri_idx);
     }
@@ -1051,6 +1089,7 @@ extern "C" int32_t ffsrl_batch_create(const ffsrl_model* hm, const ffsrl_model* 
         (st = dalloc(b, &b->d_wide, (precision == 32 && accum == FFSRL_ACC_FIXED) ? 3 * (size_t)V : 0)) ||
         (st = dalloc(b, &b->d_tet_vs, tet_vs.size())) || (st = upload(b->d_tet_vs, tet_vs)) ||
         (st = dalloc(b, &b->d_tet_ed, tet_ed.size())) || (st = upload(b->d_tet_ed, tet_ed)) ||
+        (st = dalloc(b, &b->d_tet_ed2, tet_ed2.size())) || (st = upload(b->d_tet_ed2, tet_ed2)) ||
         (st = dalloc(b, &b->d_edge_idx, edge_idx.size())) || (st = upload(b->d_edge_idx, edge_idx)) ||
         (st = dalloc(b, &b->d_edge_la, edge_la.size())) || (st = upload(b->d_edge_la, edge_la)) ||
         (st = dalloc(b, &b->d_tri_idx, tri_idx.size())) || (st = upload(b->d_tri_idx, tri_idx)) ||

@@ -207,15 +207,22 @@ template <class S> __device__ __forceinline__ t3<typename S::R> take3(typename S
     typedef typename S::R R;
     t3<R> r;
     if constexpr (S::kFixed) {
-        long long s[3];
-        for (int k = 0; k < 3; ++k) s[k] = (long long)(int)acc[3 * i + k];
-        if (wide_on) {
-            unsigned long long* w = wd.w + 3 * (wd.v0 + i);
-            for (int k = 0; k < 3; ++k) { s[k] += (long long)w[k]; w[k] = 0ull; }
+        if (!wide_on && !extra) {
+            // the common case: the 32-bit sum alone (int32 -> float, the same rounding as the
+            // 64-bit conversion below, which runs on the slow float64 unit)
+            r = T3<R>(__int2float_rn((int)acc[3 * i]) * inv, __int2float_rn((int)acc[3 * i + 1]) * inv,
+                      __int2float_rn((int)acc[3 * i + 2]) * inv);
+        } else {
+            long long s[3];
+            for (int k = 0; k < 3; ++k) s[k] = (long long)(int)acc[3 * i + k];
+            if (wide_on) {
+                unsigned long long* w = wd.w + 3 * (wd.v0 + i);
+                for (int k = 0; k < 3; ++k) { s[k] += (long long)w[k]; w[k] = 0ull; }
+            }
+            if (extra)
+                for (int k = 0; k < 3; ++k) s[k] += extra[k];
+            r = T3<R>(__ll2float_rn(s[0]) * inv, __ll2float_rn(s[1]) * inv, __ll2float_rn(s[2]) * inv);
         }
-        if (extra)
-            for (int k = 0; k < 3; ++k) s[k] += extra[k];
-        r = T3<R>(__ll2float_rn(s[0]) * inv, __ll2float_rn(s[1]) * inv, __ll2float_rn(s[2]) * inv);
     } else if constexpr (S::kKahan) {
         r = T3<R>(acc_value(acc[3 * i]), acc_value(acc[3 * i + 1]), acc_value(acc[3 * i + 2]));
     } else {
@@ -251,7 +258,10 @@ template <class R> struct Dev {
     const int* cnt0;           // per-vertex static contribution count (global vertex index)
     const float4* tet_ed;      // distance constraints solved by the tet: (L0 of A-B, active, +-L0, active);
                                // the second is C-D for +L0 and A-C for -L0; active 0 = none
+    const float2* tet_ed2;     // compact records: (L0 of A-B, +-L0 of C-D / A-C), 0 = none, active 1
     int fold;                  // distance constraints folded into the tet records
+    int compact;               // compact fast-form records: no tet_va, nh1.w = +-|V0| (sign: active),
+                               // folded edges in tet_ed2
     const uint2* conn_idx;     // connectors: (point | triangle a << 16, b | c << 16), env-local ids
     const float4* conn_bar;    // (barycentric 0, 1, 2, rest distance)
     const unsigned char* conn_vert;  // per vertex (global id): 1 when a connector holds it
@@ -434,8 +444,20 @@ template <bool EX, bool NH, bool FOLD, class R>
 __device__ __forceinline__ TetRec load_tet(const Dev<R>& D, long long g) {
     TetRec r;
     r.ix = __ldg(D.tet_idx + g);
-    r.va = __ldg(D.tet_va + g);
     r.n0 = r.n1 = r.n2 = r.ed = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (!EX && NH && FOLD && D.compact) {
+        // 48 bytes a tet instead of 64: |V0| and the volume constraint's activity ride in
+        // the sign of nh1.w, 1/|V0| is formed here, folded edges are always active
+        r.n0 = __ldg(D.nh0 + g);
+        r.n1 = __ldg(D.nh1 + g);
+        const float2 e = __ldg(D.tet_ed2 + g);
+        const float v0 = fabsf(r.n1.w);
+        r.va = make_float2(v0, signbit(r.n1.w) ? 0.0f : 1.0f);
+        r.n1.w = rcp(v0);
+        r.ed = make_float4(e.x, e.x != 0.0f ? 1.0f : 0.0f, e.y, e.y != 0.0f ? 1.0f : 0.0f);
+        return r;
+    }
+    r.va = __ldg(D.tet_va + g);
     if (NH) {
         if (EX) { r.n0 = __ldg(D.nhd + 3 * g); r.n1 = __ldg(D.nhd + 3 * g + 1); r.n2 = __ldg(D.nhd + 3 * g + 2); }
         else { r.n0 = __ldg(D.nh0 + g); r.n1 = __ldg(D.nh1 + g); }
@@ -626,12 +648,15 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK <= 256 ? 768 / BLOCK : 1))
                                 if (prefetch && t + BLOCK < nt) {  // this thread's next record, into L1
                                     const long long gn = gt + BLOCK;
                                     prefetch_l1(D.tet_idx + gn);
-                                    prefetch_l1(D.tet_va + gn);
+                                    if (EX || !D.compact) prefetch_l1(D.tet_va + gn);
                                     if (nhf) {
                                         if (EX) { prefetch_l1(D.nhd + 3 * gn); prefetch_l1(D.nhd + 3 * gn + 2); }
                                         else { prefetch_l1(D.nh0 + gn); prefetch_l1(D.nh1 + gn); }
                                     }
-                                    if (fold) prefetch_l1(D.tet_ed + gn);
+                                    if (fold) {
+                                        if (!EX && D.compact) prefetch_l1(D.tet_ed2 + gn);
+                                        else prefetch_l1(D.tet_ed + gn);
+                                    }
                                 }
                                 // every record of the tet is requested up front, so its loads are in
                                 // flight together

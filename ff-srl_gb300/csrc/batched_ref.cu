@@ -16,6 +16,11 @@ kern_f pick_ref_fixed(int block, int mode, int prefetch, unsigned flags) {
         if (block == 768) return k_batched<AccFixed, 768, 0, false, kLiverFlags, true>;
         if (block == 1024) return k_batched<AccFixed, 1024, 0, false, kLiverFlags, true>;
     }
+    if (flags == kLiverFlags && mode == 0 && prefetch == 2) {
+        if (block == 512) return k_batched<AccFixed, 512, 0, true, kLiverFlags, true>;
+        if (block == 640) return k_batched<AccFixed, 640, 0, true, kLiverFlags, true>;
+        return nullptr;
+    }
     if (prefetch == 2) {
         if (mode == 0 && block == 512) return k_batched<AccFixed, 512, 0, true, 0, true>;
         if (mode == 0 && block == 640) return k_batched<AccFixed, 640, 0, true, 0, true>;

@@ -31,14 +31,19 @@ from . import scenarios as sc
 
 
 def step_mixed(envs: int = 512, arithmetic: str = "fast", pool: int = 0, device: str = "cuda:0") -> None:
+    """The autotuned batched step; the step after tuning runs inside the NVTX range
+    ``profiled_step`` (capture it with ``ncu --nvtx --nvtx-include profiled_step/``)."""
     meshes, _ = sc.mixed_meshes(envs, pool_size=pool, seed=0)
     m, _ = sc.liver_model(device, envs, meshes=meshes)
     m.graspNearest(torch.ones(envs, dtype=torch.int32, device=device), radius=0.5)
-    integ = SimIntegratorDO(device, arithmetic=arithmetic)  # default blocks: one launch per class
+    integ = SimIntegratorDO(device, autotune=True, arithmetic=arithmetic)
     p = integ.plan(m)
-    print(p.info())
+    print(p.info(), integ.tuning)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("profiled_step")
     p.step(1)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
 
 
 def step_big(device: str = "cuda:0") -> None:

@@ -357,8 +357,11 @@ class EnvServer:
         t_end = t_meas + duration_s
         ticks, batch_sizes = 0, []
         sent = np.zeros(A, dtype=np.int64)
+        ev_meas = None  # evictions when the measured window opens
         while True:
             now = time.perf_counter()
+            if ev_meas is None and now >= t_meas:
+                ev_meas = self.evictions
             if now >= t_end:
                 break
             due = np.nonzero((~waiting) & (nxt <= now))[0]
@@ -401,7 +404,9 @@ class EnvServer:
                 "p99_ms": float(np.percentile(lat_ms, 99)) if len(lat_ms) else None,
                 "served_env_steps_per_s": served / duration_s, "requests": served, "ticks": ticks,
                 "mean_batch": float(np.mean(batch_sizes)) if batch_sizes else 0.0, "actors": A,
-                "slots": self.num_slots, "evictions": self.evictions, "budget_bytes_used": self.budget_used,
+                "slots": self.num_slots, "evictions": self.evictions,
+                "evictions_measured": self.evictions - (ev_meas if ev_meas is not None else self.evictions),
+                "budget_bytes_used": self.budget_used,
                 "episode_requests": episode, "env_status_nonzero": int((self.plan.env_status() != 0).sum()),
                 **({"tick_profile": prof} if prof else {})}
 

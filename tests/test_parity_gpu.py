@@ -229,12 +229,15 @@ def test_liver_config1_mesh_global_accumulators(gpu, oracle_lib):
 
 def test_precision_float32_vs_float64(gpu):
     # config 3's stiff variant (nu 0.49, 16 substeps x 50 iterations) on the full liver
-    # mesh: float32 (mode 1) against the float64 build of the same kernel (mode 2)
-    from ffsrl.precision import precision_report
-    rep = precision_report([mg.ellipsoid()], steps=3)
+    # mesh: float32 with each accumulation (fixed point, Kahan, float atomics) against the
+    # float64 build of the same kernel
+    from ffsrl.precision import config3
+    rep = config3(envs=1, steps=10)
     print("[precision]", rep)
     assert rep["finite"]
-    assert rep["max_pos_err_rel"] < POS_TOL
+    for acc in ("fixed", "kahan", "atomic"):
+        assert rep[acc]["max_pos_err_rel"] < POS_TOL, acc
+        assert rep[acc]["status_nonzero"] == 0
     assert rep["volume_err_f64"]["max"] < 0.5
 
 

@@ -79,6 +79,23 @@ def test_alone_equals_mix(gpu):
 
 
 @pytest.mark.gpu
+def test_alone_equals_mix_across_server_models(gpu):
+    # an actor served by a model of its own mesh alone gives the same bits as in a model
+    # built from a whole pool and stepped with other actors: each env's fixed-point scale
+    # comes from its own coordinates
+    from ffsrl.serve import EnvServer
+    pool = _pool()
+    alone = EnvServer([pool[1]], [0], "cuda:0", resolution=16)
+    mix = EnvServer(pool, [0, 1, 2, 0, 1, 2], "cuda:0", resolution=16)
+    d = [[0.05, 0.02, -0.01], [-0.03, 0.04, 0.0], [0.0, -0.05, 0.02]]
+    ra = _run(alone, [[(0, d[k], 1)] for k in range(3)])
+    rm = _run(mix, [[(a, d[k] if a == 4 else d[(k + a) % 3], 1) for a in range(6)] for k in range(3)])
+    for k in range(3):
+        assert np.array_equal(ra[0][k], rm[4][k])
+    assert np.array_equal(_state(alone, 0), _state(mix, 4))
+
+
+@pytest.mark.gpu
 def test_eviction_restores_state(gpu):
     actors = [0, 0, 1, 1, 2, 2]
     pool = _pool()
