@@ -62,9 +62,10 @@ def oracle_pair(m, seed=0):
     return o1, o2
 
 
-def run_100(name, build, runs, steps=100, every=10, threads=4):
+def run_100(name, build, runs, steps=100, every=10, threads=4, report_only=()):
     """Steps the GPU runs (label -> integrator kwargs) and the oracle pair in lock step;
-    asserts the tolerance at every checkpoint and returns the error table."""
+    asserts the tolerance at every checkpoint (except for the labels in ``report_only``,
+    which are printed only) and returns the error table."""
     models = {k: build() for k in runs}
     integ = {k: SimIntegratorDO("cuda:0", **kw) for k, kw in runs.items()}
     first = next(iter(models.values()))
@@ -85,7 +86,8 @@ def run_100(name, build, runs, steps=100, every=10, threads=4):
             worst[key] = max(worst[key], e)
             line.append(f"{key} {e:.2e}")
             assert np.isfinite(models[key].vertex.cpu().numpy()).all()
-            assert e < tol, f"{name} {key} step {k + every}: {e:.3e} > {tol:.3e}"
+            if key not in report_only:
+                assert e < tol, f"{name} {key} step {k + every}: {e:.3e} > {tol:.3e}"
         print(f"[parity100] {name} step {k + every}: " + ", ".join(line) + f"; oracle order spread {spread_max:.2e}")
     for key in runs:
         if integ[key].batched:
@@ -106,7 +108,11 @@ def test_beam_config0_every_10_steps(gpu, oracle_lib):
 
 def test_liver_config1_neohookean_grasp_contact(gpu, oracle_lib):
     # the 12/8/6 cm ellipsoid (11,102 vertices), grasped, the closed clamps on its surface
-    worst, spread = run_100("liver", lambda: grasped(sc.liver_model("cuda:0", 1)[0]), {"batched": {}})
+    # reported without a bar: the reference-shaped form (its float atomics change their
+    # order from run to run) and the fast arithmetic
+    worst, spread = run_100("liver", lambda: grasped(sc.liver_model("cuda:0", 1)[0]),
+                            {"batched": {}, "batched-fast": {"arithmetic": "fast"}, "plain": {"batched": False}},
+                            report_only=("plain", "batched-fast"))
     print(f"[parity100] liver worst {worst}, reference order spread {spread:.2e}")
 
 
@@ -115,7 +121,8 @@ def test_mixed_pool_with_contact(gpu, oracle_lib):
     pool = [mg.ellipsoid_for_tets(t, seed=i) for i, t in enumerate([300, 1200, 4000])]
     meshes = [pool[i % 3] for i in range(7)]
     run_100("mixed7", lambda: grasped(sc.liver_model("cuda:0", 7, meshes=meshes)[0]),
-            {"batched": {}, "batched-fast": {"arithmetic": "fast"}})
+            {"batched": {}, "batched-fast": {"arithmetic": "fast"}, "plain": {"batched": False}},
+            report_only=("plain",))
 
 
 def _disjoint_tets(n=24, seed=5):
