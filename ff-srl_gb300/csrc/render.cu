@@ -5,9 +5,7 @@
 // with IEEE division and square root the images and boxes equal the CPU restatement's
 // bit for bit whenever the summation order is the same (the fused paths).
 #include <cuda_runtime.h>
-#include <algorithm>
 #include <cstdint>
-#include <string>
 #include "ffsrl_internal.h"
 #include "vecmath.cuh"
 
@@ -415,17 +413,14 @@ __device__ __forceinline__ v3 texel(const ffsrl_render& r, const int* ob, int lf
     return (1.0f - ay) * lower + ay * upper;
 }
 
-// The ray through sub-pixel (x, y) of a W x H ray grid (drawSimBVHKernelManyEnvs,
-// render.py:299-330): s = 2x/W - 1 per axis, direction rotate(q, (sx tan aspect, sy tan, -1))
-// normalised
-__device__ __forceinline__ v3 ray_dir(const ffsrl_render& r, float4 q, int x, int y, int W, int H) {
+__device__ __forceinline__ Shade trace(const ffsrl_render& r, const EnvView& ev, int e, v3 ro, float4 q, int x, int y,
+                                       int W, int H) {
     float sx = 2.0f * float(x) / float(W) - 1.0f;
     float sy = 2.0f * float(y) / float(H) - 1.0f;
-    return normalize(quat_rotate(q, mk(sx * r.camera_tan * r.camera_aspect, sy * r.camera_tan, -1.0f)));
-}
-
-// shading of the kept hit: face `tri` (global id) at distance t, hit point p
-__device__ __forceinline__ Shade shade(const ffsrl_render& r, const EnvView& ev, int e, int tri, float t, v3 p) {
+    v3 rd = normalize(quat_rotate(q, mk(sx * r.camera_tan * r.camera_aspect, sy * r.camera_tan, -1.0f)));
+    float t = 0.0f;
+    v3 p = mk(0.0f, 0.0f, 0.0f);
+    int tri = query(ev, r.vis_point, r.vis_face, ro, rd, t, p, r.error_flag);
     Shade s;
     s.color = mk(0.0f, 0.0f, 0.0f);
     s.depth = 0.0f;
@@ -472,15 +467,6 @@ __device__ __forceinline__ Shade shade(const ffsrl_render& r, const EnvView& ev,
         s.depth = d;
     }
     return s;
-}
-
-__device__ __forceinline__ Shade trace(const ffsrl_render& r, const EnvView& ev, int e, v3 ro, float4 q, int x, int y,
-                                       int W, int H) {
-    v3 rd = ray_dir(r, q, x, y, W, H);
-    float t = 0.0f;
-    v3 p = mk(0.0f, 0.0f, 0.0f);
-    int tri = query(ev, r.vis_point, r.vis_face, ro, rd, t, p, r.error_flag);
-    return shade(r, ev, e, tri, t, p);
 }
 
 // drawSimBVHKernelManyEnvs (render.py:276-409): one thread per ray, into scratch
@@ -562,178 +548,6 @@ __global__ void __launch_bounds__(256) k_rays(ffsrl_render r, ffsrl_bvh b, const
     if (valid && q == 0) {
         v3 c = mk(cx, cy, cz);
         for (int k = 0; k < 3; ++k) c = mk(c.x + ax[k], c.y + ay[k], c.z + az[k]);
-        float dd = ((d + ad[0]) + ad[1]) + ad[2];
-        float nsq = float(2 * 2);
-        long long o = (long long)e * R * R + (long long)py * R + px;
-        if (r.color) st3(r.color, o, mk(c.x / nsq, c.y / nsq, c.z / nsq));
-        if (r.depth) r.depth[o] = dd / nsq;
-    }
-}
-
-// ---- triangle-parallel ray-cast ---------------------------------------------------------
-// The kept hit of a ray is the reference's: the nearest accepted hit, and among equally near
-// ones the first in the reference's visiting order (leaves in descending tri-map position, a
-// leaf's triangles ascending; see query_packed).  Key = the distance's bits above the
-// triangle's rank in that order, so the smallest key is the kept hit whatever order the
-// triangles arrive in, and a 64-bit atomicMin per ray keeps it.  Each triangle tests the
-// rays its projection can reach; the hit test (moller_trumbore) and the ray directions
-// are the traversal's own expressions, so keys -- and images -- are the same bits.
-constexpr unsigned long long kNoHit = ~0ull;
-
-__device__ __forceinline__ v3 camera_frame(float4 q, v3 x) {
-    return quat_rotate(make_float4(-q.x, -q.y, -q.z, q.w), x);  // the inverse rotation
-}
-
-// Grid rays (x in [0, W), y in [1, H], as the traversal numbers them) whose direction the
-// hit test (moller_trumbore) can accept for triangle (a, b, c).
-//
-// The test accepts when its computed barycentrics u, v >= 0 and u + v <= 1.  Their rounding
-// error is below E = 16 eps S L / |det| (eps = 2^-24; S bounds the coordinates and the
-// distance |ro - a| the test subtracts; L the longest edge; det = -rd.N with N = ab x ac,
-// which the test requires >= 1e-4 in magnitude): each bound comes from a dot product of
-// vectors of those lengths, and the factor holds twice the sum of their terms.  So every
-// accepted ray meets the triangle scaled by (1 + 6E) about its centroid.  |det| over the
-// rays near the triangle is at least |dc.N| - |N| alpha (dc: the direction to the centroid,
-// alpha: the angle the scaled triangle spans) and at least 1e-4 (a triangle seen edge-on
-// takes that bound, a scale of up to 16; its projection stays a sliver).  The rectangle is the
-// scaled triangle's projection, a quarter ray spacing wider on each side for the rounding of
-// the projection and of the ray directions (below 1e-3 of a spacing for a unit quaternion,
-// checked to 1e-6; otherwise the whole grid).  A triangle with every corner behind the
-// camera cannot be hit (t > 0); one reaching the camera plane takes the whole grid.
-__device__ __forceinline__ bool ray_rect(const ffsrl_render& r, v3 ro, float4 q, v3 a, v3 b, v3 c, int W, int H,
-                                         int& x0, int& x1, int& y0, int& y1) {
-    auto whole = [&]() { x0 = 0; x1 = W - 1; y0 = 1; y1 = H; return true; };
-    if (!(fabsf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w - 1.0f) < 1e-6f)) return whole();
-    const v3 ab = b - a, ac = c - a, bc = c - b;
-    const v3 N = cross(ab, ac);
-    const float L = fmaxf(length(ab), fmaxf(length(ac), length(bc)));
-    const v3 g = (a + b + c) / 3.0f;
-    const v3 gc = g - ro;
-    const float dg = length(gc);
-    const float nN = length(N);
-    const float S = fmaxf(fabsf(ro.x), fmaxf(fabsf(ro.y), fabsf(ro.z))) + fmaxf(fabsf(a.x), fmaxf(fabsf(a.y), fabsf(a.z))) +
-                    dg + 2.0f * L;
-    // far from the camera (dg > 4 L) and for a scale below 1.5, the rays in question lie
-    // within alpha of dc: the triangle's angular radius L / dg, doubled, plus a ray spacing
-    float det_lo = 1e-4f;
-    if (dg > 4.0f * L && nN > 0.0f) {
-        const float alpha = 2.0f * L / dg + 4.0f * fmaxf(r.camera_tan * r.camera_aspect, r.camera_tan) / float(min(W, H));
-        det_lo = fmaxf(det_lo, fabsf(dot(gc, N)) / dg - nN * alpha);
-    }
-    float E = 16.0f * 5.9604645e-8f * S * L / det_lo;
-    // alpha assumed the scaled triangle within 2 L of its centroid (scale <= 2); beyond
-    // that, the test's threshold alone bounds |det| (a triangle seen nearly edge-on: its
-    // scaled projection stays a thin sliver)
-    if (1.0f + 6.0f * E > 2.0f) E = 16.0f * 5.9604645e-8f * S * L / 1e-4f;
-    if (!(E < 2.5f)) return whole();
-    const float k = 1.0f + 6.0f * E;
-    const v3 sa = g + (a - g) * k, sb = g + (b - g) * k, sc = g + (c - g) * k;
-    const v3 P0 = camera_frame(q, sa - ro), P1 = camera_frame(q, sb - ro), P2 = camera_frame(q, sc - ro);
-    if (P0.z > 0.0f && P1.z > 0.0f && P2.z > 0.0f) return false;
-    if (!(P0.z < 0.0f && P1.z < 0.0f && P2.z < 0.0f)) return whole();
-    const float kx = 1.0f / (r.camera_tan * r.camera_aspect), ky = 1.0f / r.camera_tan;
-    const float s0x = P0.x / -P0.z * kx, s0y = P0.y / -P0.z * ky;
-    const float s1x = P1.x / -P1.z * kx, s1y = P1.y / -P1.z * ky;
-    const float s2x = P2.x / -P2.z * kx, s2y = P2.y / -P2.z * ky;
-    const float lx = fminf(s0x, fminf(s1x, s2x)), hx = fmaxf(s0x, fmaxf(s1x, s2x));
-    const float ly = fminf(s0y, fminf(s1y, s2y)), hy = fmaxf(s0y, fmaxf(s1y, s2y));
-    if (!(lx == lx && hx == hx && ly == ly && hy == hy)) return whole();  // non-finite corner
-    // s = 2x/W - 1  <=>  x = (s + 1) W / 2; clamp in float before the integer conversion
-    const float fw = 0.5f * float(W), fh = 0.5f * float(H);
-    const float ax = fminf(fmaxf((lx + 1.0f) * fw - 0.25f, -1.0f), float(W));
-    const float bx = fminf(fmaxf((hx + 1.0f) * fw + 0.25f, -1.0f), float(W));
-    const float ay = fminf(fmaxf((ly + 1.0f) * fh - 0.25f, 0.0f), float(H + 1));
-    const float by = fminf(fmaxf((hy + 1.0f) * fh + 0.25f, 0.0f), float(H + 1));
-    x0 = max((int)ceilf(ax), 0); x1 = min((int)floorf(bx), W - 1);
-    y0 = max((int)ceilf(ay), 1); y1 = min((int)floorf(by), H);
-    return x0 <= x1 && y0 <= y1;
-}
-
-__device__ __forceinline__ void raster_tri(const ffsrl_render& r, const ffsrl_bvh& b, int e, int tpos) {
-    const int W = 2 * r.resolution, H = 2 * r.resolution;
-    const int cam = r.num_cameras > 1 ? e : 0;
-    const v3 ro = ld3(r.camera_pos, cam);
-    const float4 q = reinterpret_cast<const float4*>(r.camera_rot)[cam];
-    const long long f = (long long)b.env_face_offset[e] + b.tri_id[tpos];
-    const v3 A = ld3(r.vis_point, r.vis_face[3 * f]), B = ld3(r.vis_point, r.vis_face[3 * f + 1]),
-             C = ld3(r.vis_point, r.vis_face[3 * f + 2]);
-    int x0, x1, y0, y1;
-    if (!ray_rect(r, ro, q, A, B, C, W, H, x0, x1, y0, y1)) return;
-    const unsigned long long rank = (unsigned)b.tri_rank[tpos];
-    unsigned long long* key = r.ray_key + (long long)e * W * H;
-    for (int y = y0; y <= y1; ++y)
-        for (int x = x0; x <= x1; ++x) {
-            const v3 rd = ray_dir(r, q, x, y, W, H);
-            v3 p;
-            const float t = moller_trumbore(A, B, C, ro, rd, p);
-            if (t > 0.0f && t < 1e6f)
-                atomicMin(key + (long long)(H - y) * W + x, ((unsigned long long)__float_as_uint(t) << 32) | rank);
-        }
-}
-
-// One thread per tri-map position of an env (blockIdx.y strides over the envs, or the
-// listed envs): the triangle's rays, each hit into the ray's key
-__global__ void __launch_bounds__(256) k_raster(ffsrl_render r, ffsrl_bvh b, const int* __restrict__ ids, int n_ids) {
-    const int count = ids ? n_ids : r.num_envs;
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    for (int k = blockIdx.y; k < count; k += gridDim.y) {
-        const int e = ids ? ids[k] : k;
-        if (e < 0 || e >= r.num_envs) continue;
-        const int topo = b.env_topology[e];
-        const int t0 = b.topo_tri_offset[topo], nt = b.topo_tri_offset[topo + 1] - t0;
-        if (j < nt) raster_tri(r, b, e, t0 + j);
-    }
-}
-
-// The rays' kept hits shaded and averaged 2x2 per pixel (the layout of k_rays: a block per
-// 8x8-pixel tile, the four rays of a pixel in consecutive lanes); each key is reset for the
-// next call
-__global__ void __launch_bounds__(256) k_resolve(ffsrl_render r, ffsrl_bvh b, const int* __restrict__ ids, int n_ids) {
-    const int R = r.resolution, W = 2 * R, H = 2 * R;
-    const int tiles_x = (R + 7) / 8;
-    const int tiles = tiles_x * ((R + 7) / 8);
-    const int k = blockIdx.x / tiles;
-    const int e = ids ? (k < n_ids ? ids[k] : r.num_envs) : k;
-    const int tile = blockIdx.x % tiles;
-    const int pix = threadIdx.x >> 2, qd = threadIdx.x & 3;
-    const int wp = pix >> 3, jj = pix & 7;
-    const int px = (tile % tiles_x) * 8 + (wp & 1) * 4 + (jj & 3);
-    const int py = (tile / tiles_x) * 8 + (wp >> 1) * 2 + (jj >> 2);
-    const bool valid = e >= 0 && e < r.num_envs && px < R && py < R;
-    Shade s;
-    s.color = mk(0.0f, 0.0f, 0.0f);
-    s.depth = 0.0f;
-    if (valid) {
-        const int et = (2 * py + (qd >> 1)) * W + 2 * px + (qd & 1);
-        unsigned long long* kp = r.ray_key + (long long)e * W * H + et;
-        const unsigned long long key = *kp;
-        if (key != kNoHit) {
-            *kp = kNoHit;
-            const int cam = r.num_cameras > 1 ? e : 0;
-            const v3 ro = ld3(r.camera_pos, cam);
-            const float4 q = reinterpret_cast<const float4*>(r.camera_rot)[cam];
-            const EnvView ev = env_view(b, e);
-            const v3 rd = ray_dir(r, q, et % W, H - et / W, W, H);
-            const float t = __uint_as_float((unsigned)(key >> 32));
-            const unsigned rank = (unsigned)(key & 0xffffffffull);
-            const int first = 0x1FFFF - (int)(rank >> 15), kk = (int)(rank & 0x7FFFu);
-            const int tri = (int)(ev.fofs + ev.tri[first + kk]);
-            const v3 p = ro + t * rd;
-            s = shade(r, ev, e, tri, t, p);
-        }
-    }
-    float cx = s.color.x, cy = s.color.y, cz = s.color.z, d = s.depth;
-    float ax[3], ay[3], az[3], ad[3];
-#pragma unroll
-    for (int m = 1; m <= 3; ++m) {
-        ax[m - 1] = __shfl_down_sync(0xffffffffu, cx, m);
-        ay[m - 1] = __shfl_down_sync(0xffffffffu, cy, m);
-        az[m - 1] = __shfl_down_sync(0xffffffffu, cz, m);
-        ad[m - 1] = __shfl_down_sync(0xffffffffu, d, m);
-    }
-    if (valid && qd == 0) {
-        v3 c = mk(cx, cy, cz);
-        for (int m = 0; m < 3; ++m) c = mk(c.x + ax[m], c.y + ay[m], c.z + az[m]);
         float dd = ((d + ad[0]) + ad[1]) + ad[2];
         float nsq = float(2 * 2);
         long long o = (long long)e * R * R + (long long)py * R + px;
@@ -851,49 +665,5 @@ extern "C" int32_t ffsrl_render_fused_envs(const ffsrl_render* r, const ffsrl_bv
     const int tiles = ((r->resolution + 7) / 8) * ((r->resolution + 7) / 8);
     k_rays<<<(unsigned)((long long)tiles * n), 256, 0, s>>>(*r, *b, env_ids, n);
     FFSRL_LAUNCH_CHECK("ffsrl_render_fused_envs");
-    return FFSRL_OK;
-}
-
-namespace {
-int32_t check_binned(const ffsrl_render* r, const ffsrl_bvh* b, const char* who) {
-    if (!r->ray_key || !b->tri_rank || !r->point_face_start || !r->point_face)
-        return fail(FFSRL_ERR_INVALID_ARGUMENT, std::string(who) + ": needs ray_key, tri_rank and the point->face CSR");
-    if (((uintptr_t)r->ray_key) & 7) return fail(FFSRL_ERR_INVALID_ARGUMENT, std::string(who) + ": ray_key alignment");
-    return FFSRL_OK;
-}
-}  // namespace
-
-extern "C" int32_t ffsrl_render_binned(const ffsrl_render* r, const ffsrl_bvh* b, int32_t max_topology_tris,
-                                       void* stream) {
-    if (int32_t st = check_render(r)) return st;
-    if (int32_t st = check_bvh(b)) return st;
-    if (int32_t st = check_binned(r, b, "ffsrl_render_binned")) return st;
-    if (max_topology_tris <= 0) return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_render_binned: max_topology_tris");
-    cudaStream_t s = (cudaStream_t)stream;
-    const int P = r->num_vis_points;
-    k_normal_gather<<<grid_for(P, 256), 256, 0, s>>>(r->vis_point, r->vis_face, r->point_face_start, r->point_face,
-                                                     r->vertex_normal, P);
-    k_raster<<<dim3(grid_for(max_topology_tris, 256), std::min(r->num_envs, 65535)), 256, 0, s>>>(*r, *b, nullptr, 0);
-    const int tiles = ((r->resolution + 7) / 8) * ((r->resolution + 7) / 8);
-    k_resolve<<<(unsigned)((long long)tiles * r->num_envs), 256, 0, s>>>(*r, *b, nullptr, 0);
-    FFSRL_LAUNCH_CHECK("ffsrl_render_binned");
-    return FFSRL_OK;
-}
-
-extern "C" int32_t ffsrl_render_binned_envs(const ffsrl_render* r, const ffsrl_bvh* b, int32_t max_topology_tris,
-                                            const int32_t* env_ids, int32_t n, void* stream) {
-    if (int32_t st = check_render(r)) return st;
-    if (int32_t st = check_bvh(b)) return st;
-    if (int32_t st = check_binned(r, b, "ffsrl_render_binned_envs")) return st;
-    if (n < 0 || (n > 0 && (!env_ids || !r->env_point_start)) || max_topology_tris <= 0)
-        return fail(FFSRL_ERR_INVALID_ARGUMENT, "ffsrl_render_binned_envs: env ids, env point ranges, tri count");
-    if (n == 0) return FFSRL_OK;
-    cudaStream_t s = (cudaStream_t)stream;
-    k_normal_gather_envs<<<n, 256, 0, s>>>(r->vis_point, r->vis_face, r->point_face_start, r->point_face,
-                                           r->vertex_normal, r->env_point_start, env_ids, r->num_envs);
-    k_raster<<<dim3(grid_for(max_topology_tris, 256), std::min(n, 65535)), 256, 0, s>>>(*r, *b, env_ids, n);
-    const int tiles = ((r->resolution + 7) / 8) * ((r->resolution + 7) / 8);
-    k_resolve<<<(unsigned)((long long)tiles * n), 256, 0, s>>>(*r, *b, env_ids, n);
-    FFSRL_LAUNCH_CHECK("ffsrl_render_binned_envs");
     return FFSRL_OK;
 }

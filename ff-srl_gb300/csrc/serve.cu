@@ -398,10 +398,7 @@ extern "C" int32_t ffsrl_server_launch(ffsrl_server* S, int32_t max_batch, int32
                                                 c.vis_point, c.env_inst_first_point, L.d_ids, n, N, st)))
             return e;
         if ((e = ffsrl_bvh_refit_fused_envs(&S->bvh, c.vis_point, c.vis_face, L.d_ids, n, st))) return e;
-        if ((e = c.max_topology_tris > 0
-                     ? ffsrl_render_binned_envs(&S->render, &S->bvh, c.max_topology_tris, L.d_ids, n, st)
-                     : ffsrl_render_fused_envs(&S->render, &S->bvh, L.d_ids, n, st)))
-            return e;
+        if ((e = ffsrl_render_fused_envs(&S->render, &S->bvh, L.d_ids, n, st))) return e;
         k_results<<<grid_for(n, 128), 128, 0, st>>>(m.laparoscope_tip, m.laparoscope_in_collision, L.d_ids, n,
                                                     L.d_res);
         FFSRL_LAUNCH_CHECK("ffsrl_server_launch: results");

@@ -83,7 +83,7 @@ class Bvh(C.Structure):
         ("aabb_min", P), ("aabb_max", P),
         ("total_env_nodes", I32), ("total_topology_nodes", I32), ("max_level", I32),
         ("level_node", P), ("level_start", P), ("topo_level_offset", P), ("node_box", P), ("tri_pos", P),
-        ("refit_source", P), ("tri_rank", P),
+        ("refit_source", P),
     ]
 
 
@@ -96,7 +96,7 @@ class Render(C.Structure):
         ("num_lights", I32), ("light_dir", P), ("light_intensity", P),
         ("color", P), ("depth", P), ("rays", P), ("ray_depth", P), ("error_flag", P), ("env_point_start", P),
         ("render_mode", I32), ("texture", P), ("env_objects", P), ("object_texture", P), ("tex_coords", P),
-        ("tex_indices", P), ("ray_key", P),
+        ("tex_indices", P),
     ]
 
 
@@ -115,8 +115,7 @@ class ServerConfig(C.Structure):
                 ("initial_tip", P), ("xform", P), ("initial_xform", P), ("height", P), ("grasp_cand_start", P),
                 ("grasp_cand", P), ("grasp_radius", F32), ("vis_point", P), ("point_to_vertex", P),
                 ("env_map_start", P), ("inst_local_point", P), ("inst_point_slot", P), ("inst_num_points", I32),
-                ("env_inst_first_point", P), ("bvh", C.POINTER(Bvh)), ("vis_face", P), ("render", C.POINTER(Render)),
-                ("max_topology_tris", I32)]
+                ("env_inst_first_point", P), ("bvh", C.POINTER(Bvh)), ("vis_face", P), ("render", C.POINTER(Render))]
 
 
 # ffsrl_batch_options.arithmetic / .accumulation
@@ -194,8 +193,6 @@ def lib() -> C.CDLL:
         "ffsrl_attach_render": ([P, C.POINTER(RenderConfig)], I32),
         "ffsrl_render_handle": ([P, P, P, I32, P, P, P], I32),
         "ffsrl_render_handle_check": ([P, P], I32),
-        "ffsrl_render_binned": ([P, P, I32, P], I32),
-        "ffsrl_render_binned_envs": ([P, P, I32, P, I32, P], I32),
         "ffsrl_server_create": ([C.POINTER(ServerConfig), C.POINTER(P)], I32),
         "ffsrl_server_destroy": ([P], I32),
         "ffsrl_server_submit": ([P, I32, P, I32, I32, C.c_int64], I32),

@@ -46,24 +46,6 @@ def build_topology(points: np.ndarray, faces: np.ndarray, bins: int = 8) -> dict
     return out
 
 
-def tri_rank(t: dict) -> np.ndarray:
-    """Per tri-map position of one topology: ``((0x1FFFF - first) << 15) | k`` for the leaf
-    starting at position ``first`` and the position ``k`` inside it.  The reference
-    traverses right children first, so its pre-order meets leaves in descending ``first``
-    and a leaf's triangles in ascending ``k``; among equally near hits it keeps the first
-    it meets, which is the smallest rank."""
-    left, first, cnt = t["left_node"], t["first_tri_id"], t["tri_count"]
-    out = np.full(len(t["tri_id"]), -1, dtype=np.int64)
-    for n in np.nonzero(left == -1)[0]:
-        f0, c = int(first[n]), int(cnt[n])
-        if f0 > 0x1FFFF or c > 0x7FFF:
-            raise ValueError("tri_rank: a topology beyond 2^17 tri-map positions or a leaf beyond 2^15 triangles")
-        out[f0:f0 + c] = ((0x1FFFF - f0) << 15) | np.arange(c)
-    if (out < 0).any():
-        raise ValueError("tri_rank: tri-map positions outside every leaf")
-    return out.astype(np.int32)
-
-
 def reference_refit_source(simModel) -> np.ndarray | None:
     """The face whose box the reference's refit takes for each visual face, or None where
     it takes the face itself everywhere.
@@ -182,10 +164,6 @@ class SimBVH:
         self.triCount = T(np.concatenate([t["tri_count"] for t in topos]))
         self.level = T(np.concatenate([t["level"] for t in topos]))
         self.triId = T(np.concatenate([t["tri_id"] for t in topos]))
-        # each tri-map position's rank in the reference's visiting order among equally near
-        # hits (the triangle-parallel ray-cast keeps the smallest)
-        self.triRank = T(np.concatenate([tri_rank(t) for t in topos]))
-        self.maxTopologyTris = int(nt.max())
         self.envTopology = T(env_topo)
         self.envNodeOffset = T(env_node_off)
         self.envFaceOffset = T(m.envVisFaceStart[:-1])
@@ -223,7 +201,6 @@ class SimBVH:
         src = reference_refit_source(m) if self.referenceRefitShift else None
         self.refitSource = None if src is None else T(src)
         d.refit_source = None if src is None else ptr(self.refitSource)
-        d.tri_rank = ptr(self.triRank)
 
     # ------------------------------------------------------------- npz files
     def saveBVH(self, path: str) -> None:

@@ -67,7 +67,7 @@ class WarpRaycastRendererDO:
     def __init__(self, device, simModel, cameraPos=(3.0, 3.0, 3.0), cameraRot=(0.0, 0.0, 0.0),
                  lightPos=(3.0, 0.0, 0.0), lightIntensity=0.3, resolution: int = 512, mode: str = "human",
                  horizontalAperture: float = 19.2, verticalAperture: float = 19.2, fused: bool = True,
-                 render_mode: int = RenderMode.texture, method: str = "binned"):
+                 render_mode: int = RenderMode.texture):
         if mode not in ("headless", "gpuless"):
             warnings.warn(f"render mode {mode!r}: no display back-end here, rendering headless")
         self.device = torch.device(device)
@@ -75,11 +75,6 @@ class WarpRaycastRendererDO:
         self.simModel = simModel
         self.numEnvs = simModel.numEnvs
         self.fused = bool(fused)
-        # the fused images: "binned" (triangle by triangle, no traversal) or "bvh" (ray by
-        # ray, nearer-child-first traversal); both are the reference's images
-        if method not in ("binned", "bvh"):
-            raise ValueError(f"method {method!r}: 'binned' or 'bvh'")
-        self.method = method
         if int(render_mode) not in range(5):
             raise ValueError(f"render_mode {render_mode!r}: expected a RenderMode value 0..4")
         self.render_mode = int(render_mode)  # the reference's default is RenderMode.texture (render.py:852)
@@ -108,7 +103,6 @@ class WarpRaycastRendererDO:
         self.errorFlag = torch.zeros(1, dtype=torch.int32, device=self.device)
         self.rays = None
         self.rayDepth = None
-        self.rayKey = None  # binned ray-cast scratch: all bits set between calls
         # point -> incident faces (ascending face id) for the deterministic normal gather
         faces = simModel.host["allVisFace"].reshape(-1, 3).astype(np.int64)
         P = simModel.numAllVisPoints
@@ -151,10 +145,6 @@ class WarpRaycastRendererDO:
                 self.rays = torch.zeros((self.numEnvs * self.num_rays, 3), dtype=torch.float32, device=self.device)
                 self.rayDepth = torch.zeros(self.numEnvs * self.num_rays, dtype=torch.float32, device=self.device)
             r.rays, r.ray_depth = ptr(self.rays), ptr(self.rayDepth)
-        if self.fused and self.method == "binned":
-            if self.rayKey is None:
-                self.rayKey = torch.full((self.numEnvs * self.num_rays,), -1, dtype=torch.int64, device=self.device)
-            r.ray_key = ptr(self.rayKey)
         r.error_flag = ptr(self.errorFlag)
         r.env_point_start = ptr(simModel.envVisPointStartT)
         r.render_mode = int(self.render_mode)
@@ -167,10 +157,6 @@ class WarpRaycastRendererDO:
     def renderFunctionNew(self, simBVH, stream=None) -> None:
         self.simModel.require_cuda()
         r = self._desc(self.simModel)
-        if self.fused and self.method == "binned":
-            check(lib().ffsrl_render_binned(C.byref(r), C.byref(simBVH.desc), simBVH.maxTopologyTris,
-                                            _lib.stream_handle(stream)))
-            return
         fn = lib().ffsrl_render_fused if self.fused else lib().ffsrl_render_reference
         check(fn(C.byref(r), C.byref(simBVH.desc), _lib.stream_handle(stream)))
 
@@ -181,8 +167,8 @@ class WarpRaycastRendererDO:
         tensors change."""
         if useGraph:
             from .graphs import Graph
-            key = (id(simBVH), self.render_mode, self.fused, self.method, self.cameraPosT.data_ptr(),
-                   self.cameraRotT.data_ptr(), self.lightDir.data_ptr())
+            key = (id(simBVH), self.render_mode, self.fused, self.cameraPosT.data_ptr(), self.cameraRotT.data_ptr(),
+                   self.lightDir.data_ptr())
             if self.renderGraph is None or self.renderGraph[0] != key:
                 self.renderGraph = (key, Graph(lambda: self.renderFunctionNew(simBVH),
                                                prepare=lambda: self._desc(self.simModel)))

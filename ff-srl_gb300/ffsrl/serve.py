@@ -314,11 +314,7 @@ class EnvServer:
             check(lib().ffsrl_bvh_refit_fused_envs(C.byref(self.bvh.desc), ptr(m.allVisPoint), ptr(m.allVisFace),
                                                    ptr(ln.ids_d), n, s))
             rd = self.renderer._desc(m)
-            if self.renderer.method == "binned":
-                check(lib().ffsrl_render_binned_envs(C.byref(rd), C.byref(self.bvh.desc), self.bvh.maxTopologyTris,
-                                                     ptr(ln.ids_d), n, s))
-            else:
-                check(lib().ffsrl_render_fused_envs(C.byref(rd), C.byref(self.bvh.desc), ptr(ln.ids_d), n, s))
+            check(lib().ffsrl_render_fused_envs(C.byref(rd), C.byref(self.bvh.desc), ptr(ln.ids_d), n, s))
             idl = ln.ids_d[:n].long()
             ln.res_d[:n, :3] = m.laparoscopeTip[4 * idl + 3]
             ln.res_d[:n, 3] = m.laparoscopeInCollision[idl].float()
@@ -447,7 +443,6 @@ class NativeEnvServer(EnvServer):
         c.grasp_radius = m.globalLaparoscopeDragLookupRadius
         c.vis_point, c.point_to_vertex, c.env_map_start = ptr(m.allVisPoint), ptr(m.pointToVertex), ptr(m.envMapStartT)
         c.bvh, c.vis_face, c.render = C.pointer(self.bvh.desc), ptr(m.allVisFace), C.pointer(self._rd)
-        c.max_topology_tris = self.bvh.maxTopologyTris if self.renderer.method == "binned" else 0
         self._cfg = c
         h = C.c_void_p()
         check(lib().ffsrl_server_create(C.byref(c), C.byref(h)))

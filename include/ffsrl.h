@@ -150,11 +150,6 @@ typedef struct {
        the object boundaries (bvh.py:66-74 uses `>` where render.py:462-470 uses `>=`);
        the traversal and tri_pos always use f.  Every entry must be a valid face id. */
     const int32_t* refit_source;
-    /* optional [tris], for the triangle-parallel ray-cast: per tri-map position of each
-       topology, ((0x1FFFF - first) << 15) | k for the leaf's first position `first` and the
-       position k inside the leaf -- the reference's visiting order among equally near hits
-       (smaller is earlier).  Needs first < 2^17 and leaves below 2^15 triangles. */
-    const int32_t* tri_rank;
 } ffsrl_bvh;
 
 /* ---- ray-cast renderer (render.py:826-1196) ------------------------------------ */
@@ -199,9 +194,6 @@ typedef struct {
                                         (0 = no texture: vertex colour), first tex coord, first tex index */
     const float* tex_coords;         /* [2T] (u, v) */
     const int32_t* tex_indices;      /* 3 per object-local face: tex coords relative to the object's first */
-    /* [N*(2R)^2] triangle-parallel ray-cast scratch, one 64-bit key per ray; every bit set
-       before the first call (each call leaves it so) */
-    unsigned long long* ray_key;
 } ffsrl_render;
 
 /* ---- library ---------------------------------------------------------------- */
@@ -338,18 +330,6 @@ int32_t ffsrl_render_reference(const ffsrl_render* r, const ffsrl_bvh* bvh, void
 /* Same images: normals by CSR gather in face order, one thread per ray with a register
    stack, the 2x2 downsample fused through warp shuffles. */
 int32_t ffsrl_render_fused(const ffsrl_render* r, const ffsrl_bvh* bvh, void* stream);
-
-/* Same images again, computed triangle by triangle instead of ray by ray: each triangle
-   of each env projects its bounding rectangle onto the (2R)^2 ray grid and runs the
-   traversal's ray-triangle test for those rays; every hit goes into its ray's 64-bit key
-   (distance bits above the triangle's rank in the reference's visiting order) by an
-   atomic minimum, which keeps the hit the reference keeps; a second pass shades the kept
-   hits and averages 2x2 rays per pixel.  Needs bvh->tri_rank, r->ray_key and the
-   point->face CSR; max_topology_tris = the most triangles of any topology.  No traversal
-   stack, so no overflow to report. */
-int32_t ffsrl_render_binned(const ffsrl_render* r, const ffsrl_bvh* bvh, int32_t max_topology_tris, void* stream);
-int32_t ffsrl_render_binned_envs(const ffsrl_render* r, const ffsrl_bvh* bvh, int32_t max_topology_tris,
-                                 const int32_t* env_ids, int32_t n, void* stream);
 
 /* ffsrl_render_fused for the listed envs only (device array of env ids): their vertex
    normals (needs r->env_point_start) and images; other envs are not touched. */
@@ -529,8 +509,6 @@ typedef struct {
     const ffsrl_bvh* bvh;               /* copied at create */
     const int32_t* vis_face;
     const ffsrl_render* render;         /* copied at create */
-    int32_t max_topology_tris;          /* > 0: ray-cast triangle by triangle (ffsrl_render_binned_envs;
-                                           needs render->ray_key and bvh->tri_rank); 0: by BVH traversal */
 } ffsrl_server_config;
 int32_t ffsrl_server_create(const ffsrl_server_config* config, ffsrl_server** server);
 int32_t ffsrl_server_destroy(ffsrl_server* server);

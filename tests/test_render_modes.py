@@ -186,53 +186,3 @@ def test_render_mode_bad_value_is_rejected(gpu):
     from ffsrl._lib import FFSRLError
     with pytest.raises(FFSRLError):
         r.renderNew(bvh, m)
-
-
-@pytest.mark.gpu
-@pytest.mark.parametrize("where", ["outside", "close", "inside"])
-def test_binned_ray_cast_equals_traversal(gpu, oracle_lib, where):
-    # the triangle-by-triangle ray-cast against the ray-by-ray traversal and the oracle:
-    # cameras around the meshes, close enough that triangles cross the camera plane, and
-    # inside a mesh
-    import torch
-    import oracle
-    from ffsrl import SimBVH, SimIntegratorDO, WarpRaycastRendererDO, meshgen as mg, scenarios as sc
-    from ffsrl.render import look_at_rotation
-    meshes = [mg.ellipsoid_for_tets(t, seed=i) for i, t in enumerate([900, 2500, 600])]
-    m, _ = sc.liver_model("cuda:0", 3, meshes=meshes)
-    SimIntegratorDO("cuda:0").stepModel(m, 2)
-    bvh = SimBVH("cuda:0", m)
-    bvh.refitBVH()
-    rng = np.random.default_rng({"outside": 1, "close": 2, "inside": 3}[where])
-    pos, rot = [], []
-    for mesh in meshes:
-        c = mesh["vertex"].mean(axis=0).astype(np.float64)
-        rad = float(np.linalg.norm(mesh["vertex"] - c, axis=1).max())
-        d = rng.normal(size=3)
-        d /= np.linalg.norm(d)
-        dist = {"outside": 2.5 * rad, "close": 1.02 * rad, "inside": 0.3 * rad}[where]
-        p = c + d * dist
-        pos.append(p)
-        rot.append(look_at_rotation(p, c + rng.normal(size=3) * 0.2 * rad))
-    imgs = {}
-    for method in ("binned", "bvh"):
-        r = WarpRaycastRendererDO("cuda:0", m, resolution=24, mode="headless", render_mode=3, method=method,
-                                  lightPos=(0.3, 1.0, 0.5), lightIntensity=0.8)
-        r.setCameras(np.asarray(pos, np.float32), np.asarray(rot, np.float32))
-        col = r.renderNew(bvh, m).clone()
-        torch.cuda.synchronize()
-        imgs[method] = (col.cpu().numpy(), r.depthImages().cpu().numpy())
-        if method == "binned":
-            # a second call: the keys were reset, the same images come out
-            col2 = r.renderNew(bvh, m)
-            torch.cuda.synchronize()
-            assert torch.equal(col2, col)
-        rr = r
-    ocol, odep, _ = oracle.render(rr, bvh, m.allVisPoint.cpu().numpy(),
-                                  aabb=(bvh.aabbMin.cpu().numpy(), bvh.aabbMax.cpu().numpy()))
-    hit = float((odep > 0).mean())
-    print(f"[render] binned vs traversal, camera {where}: {hit:.2f} of the pixels hit")
-    assert hit > 0.02
-    for method in ("binned", "bvh"):
-        assert np.array_equal(imgs[method][1], odep), method
-        assert np.array_equal(imgs[method][0], ocol), method

@@ -60,8 +60,7 @@ def _camera():
 def test_python_renderer_reports_the_overflow(gpu):
     m = _model("cuda:0")
     bvh = SimBVH("cuda:0", m)
-    # the traversal-stack check belongs to the ray-by-ray path ("bvh")
-    r = WarpRaycastRendererDO("cuda:0", m, resolution=8, mode="headless", render_mode=4, method="bvh")
+    r = WarpRaycastRendererDO("cuda:0", m, resolution=8, mode="headless", render_mode=4)
     r.setCameras(*_camera())
     bvh.refitBVH()
     r.renderNew(bvh, m)
