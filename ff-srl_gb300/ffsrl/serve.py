@@ -29,6 +29,7 @@ import numpy as np
 import torch
 
 from . import _lib as L
+from . import meshgen as mg
 from . import scenarios as sc
 from ._lib import check, lib, ptr
 from .bvh import SimBVH
@@ -112,6 +113,9 @@ class EnvServer:
         self.num_slots = int(len(self.slot_mesh))
         self.budget_used = float((k * per).sum())
         meshes = [pool[m] for m in self.slot_mesh]
+        # one gravity force for the model (the reference's per-model vector), from the
+        # whole pool, so that it does not depend on which mesh takes the first slot
+        model_kw.setdefault("environmentGravity", mg.gravity_force(pool))
         self.model, _ = sc.liver_model(device, self.num_slots, meshes=meshes, **model_kw)
         self.integ = SimIntegratorDO(device, blockThreads=block_threads, autotune=autotune, arithmetic=arithmetic)
         self.plan = self.integ.plan(self.model)

@@ -82,11 +82,14 @@ def test_alone_equals_mix(gpu):
 def test_alone_equals_mix_across_server_models(gpu):
     # an actor served by a model of its own mesh alone gives the same bits as in a model
     # built from a whole pool and stepped with other actors: each env's fixed-point scale
-    # comes from its own coordinates
+    # comes from its own coordinates.  Both models get the same gravity force (the
+    # reference's gravity is one vector per model, applied times each vertex's inverse
+    # mass; by default a server takes it from the mean vertex mass of its own pool)
     from ffsrl.serve import EnvServer
     pool = _pool()
-    alone = EnvServer([pool[1]], [0], "cuda:0", resolution=16)
-    mix = EnvServer(pool, [0, 1, 2, 0, 1, 2], "cuda:0", resolution=16)
+    g = mg.gravity_force(pool)
+    alone = EnvServer([pool[1]], [0], "cuda:0", resolution=16, environmentGravity=g)
+    mix = EnvServer(pool, [0, 1, 2, 0, 1, 2], "cuda:0", resolution=16, environmentGravity=g)
     d = [[0.05, 0.02, -0.01], [-0.03, 0.04, 0.0], [0.0, -0.05, 0.02]]
     ra = _run(alone, [[(0, d[k], 1)] for k in range(3)])
     rm = _run(mix, [[(a, d[k] if a == 4 else d[(k + a) % 3], 1) for a in range(6)] for k in range(3)])
