@@ -146,10 +146,17 @@ template <> __device__ __forceinline__ void acc_add<AccFixed>(unsigned* acc, int
 template <> __device__ __forceinline__ void acc_add<AccAtomic>(float* acc, int k, float v) { atomicAdd(acc + k, v); }
 template <> __device__ __forceinline__ void acc_add<AccF64>(double* acc, int k, double v) { atomicAdd(acc + k, v); }
 // Kahan step on the (sum, compensation) pair of word k: y = v - c; t = s + y;
-// c' = (t - s) - y; s' = t, retried until no other thread changed the pair in between
+// c' = (t - s) - y; s' = t, retried until no other thread changed the pair in between.
+// The retries are capped: a pair still contended after 2^20 tries is set to NaN, which the
+// step reports as a non-finite env instead of waiting on.
 template <> __device__ __forceinline__ void acc_add<AccKahan>(unsigned long long* acc, int k, float v) {
     unsigned long long old = acc[k], assumed;
+    int tries = 0;
     do {
+        if (++tries > (1 << 20)) {
+            atomicExch(acc + k, 0x7fc000007fc00000ull);
+            return;
+        }
         assumed = old;
         const float s = __uint_as_float((unsigned)(assumed & 0xffffffffull));
         const float c = __uint_as_float((unsigned)(assumed >> 32));

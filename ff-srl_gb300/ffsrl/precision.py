@@ -84,35 +84,37 @@ def config3(envs: int = 4, steps: int = 300, device: str = "cuda:0", accumulatio
     return {"config": "3 ellipsoid, nu 0.49, 16 x 50"} | compare(make, steps, accumulations) | {"nu": 0.49}
 
 
-def all_configs(device: str = "cuda:0", steps: int = 100, steps3: int = 300, envs3: int = 4) -> list[dict]:
-    """The float32-vs-float64 report for each workload: the beam (config 0, reference
-    step), the 12/8/6 cm ellipsoid (config 1, Neo-Hookean, grasp, contact), 16 envs of the
-    one-mesh-per-env pool shared by the throughput and serving workloads (configs 2 and
-    4), all ``steps`` steps, and the nearly incompressible ellipsoid (config 3, ``steps3``
-    steps)."""
+def all_configs(device: str = "cuda:0", steps: int = 100, steps3: int = 300, envs3: int = 4, which=(0, 1, 2, 3)):
+    """The float32-vs-float64 report for each workload, one row per workload as it
+    finishes: the beam (config 0, reference step), the 12/8/6 cm ellipsoid (config 1,
+    Neo-Hookean, grasp, contact), 16 envs with one mesh each from the generator shared by
+    the throughput and serving workloads (configs 2 and 4), all ``steps`` steps, and the
+    nearly incompressible ellipsoid (config 3, ``steps3`` steps)."""
     import torch
     from . import meshgen as mg
-    out = []
-    out.append({"config": "0 beam, reference step"} | compare(lambda: sc.beam_model(device, 1)[0], steps))
 
     def liver(meshes):
         m, _ = sc.liver_model(device, len(meshes), meshes=meshes)
         m.graspNearest(torch.ones(len(meshes), dtype=torch.int32, device=device), radius=0.5)
         return m
 
-    ell = [mg.ellipsoid()]
-    out.append({"config": "1 ellipsoid, Neo-Hookean + grasp + contact"} | compare(lambda: liver(ell), steps))
-    pool, _ = sc.mixed_meshes(16, pool_size=0, seed=0)
-    out.append({"config": "2/4 mixed-size pool, 16 envs"} | compare(lambda: liver(pool), steps))
-    out.append(config3(envs3, steps3, device))
-    return out
+    if 0 in which:
+        yield {"config": "0 beam, reference step"} | compare(lambda: sc.beam_model(device, 1)[0], steps)
+    if 1 in which:
+        ell = [mg.ellipsoid()]
+        yield {"config": "1 ellipsoid, Neo-Hookean + grasp + contact"} | compare(lambda: liver(ell), steps)
+    if 2 in which:
+        pool, _ = sc.mixed_meshes(16, pool_size=0, seed=0)
+        yield {"config": "2/4 one mesh per env, 16 envs"} | compare(lambda: liver(pool), steps)
+    if 3 in which:
+        yield config3(envs3, steps3, device)
 
 
 if __name__ == "__main__":
+    # python -m ffsrl.precision [configs, e.g. 012 or 3] [steps for config 3]
     import json
     import sys
-    if len(sys.argv) > 1 and sys.argv[1] == "config3":
-        print(json.dumps(config3(steps=int(sys.argv[2]) if len(sys.argv) > 2 else 300)))
-    else:
-        for row in all_configs():
-            print(json.dumps(row), flush=True)
+    which = tuple(int(c) for c in sys.argv[1]) if len(sys.argv) > 1 else (0, 1, 2, 3)
+    steps3 = int(sys.argv[2]) if len(sys.argv) > 2 else 300
+    for row in all_configs(which=which, steps3=steps3):
+        print(json.dumps(row), flush=True)
