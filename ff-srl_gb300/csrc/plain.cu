@@ -47,10 +47,10 @@ __global__ void k_volume(const float* __restrict__ xp, float* dp, int* cnt, cons
     if (fabsf(w) < FFSRL_FLOAT_EPS) return;
     float C = rv - vol;
     float dl = -ks * active * C / w;
-    atomic_add3(dp, id.x, q0 * dl * mA);
-    atomic_add3(dp, id.y, q1 * dl * mB);
-    atomic_add3(dp, id.z, q2 * dl * mC);
-    atomic_add3(dp, id.w, q3 * dl * mD);
+    atomic_add3_pair(dp, id.x, q0 * dl * mA);
+    atomic_add3_pair(dp, id.y, q1 * dl * mB);
+    atomic_add3_pair(dp, id.z, q2 * dl * mC);
+    atomic_add3_pair(dp, id.w, q3 * dl * mD);
     atomicAdd(cnt + id.x, 1); atomicAdd(cnt + id.y, 1); atomicAdd(cnt + id.z, 1); atomicAdd(cnt + id.w, 1);
 }
 
@@ -76,10 +76,10 @@ __global__ void k_volume_xpbd(const float* __restrict__ xp, float* dp, int* cnt,
     float C = vol - rv;
     float dl = -(C + alpha * l0) / (w + alpha);
     lam[t] = l0 + dl;
-    atomic_add3(dp, id.x, q0 * dl * mA);
-    atomic_add3(dp, id.y, q1 * dl * mB);
-    atomic_add3(dp, id.z, q2 * dl * mC);
-    atomic_add3(dp, id.w, q3 * dl * mD);
+    atomic_add3_pair(dp, id.x, q0 * dl * mA);
+    atomic_add3_pair(dp, id.y, q1 * dl * mB);
+    atomic_add3_pair(dp, id.z, q2 * dl * mC);
+    atomic_add3_pair(dp, id.w, q3 * dl * mD);
     atomicAdd(cnt + id.x, 1); atomicAdd(cnt + id.y, 1); atomicAdd(cnt + id.z, 1); atomicAdd(cnt + id.w, 1);
 }
 
@@ -135,7 +135,7 @@ __global__ void k_neohookean(const float* __restrict__ xp, float* dp, int* cnt, 
     alpha = dev_c / dt / dt / rv;
     dl = -C / (w + alpha);
     dA = dA + g0 * dl * mA; dB = dB + g1 * dl * mB; dC = dC + g2 * dl * mC; dD = dD + g3 * dl * mD;
-    atomic_add3(dp, id.x, dA); atomic_add3(dp, id.y, dB); atomic_add3(dp, id.z, dC); atomic_add3(dp, id.w, dD);
+    atomic_add3_pair(dp, id.x, dA); atomic_add3_pair(dp, id.y, dB); atomic_add3_pair(dp, id.z, dC); atomic_add3_pair(dp, id.w, dD);
     atomicAdd(cnt + id.x, 1); atomicAdd(cnt + id.y, 1); atomicAdd(cnt + id.z, 1); atomicAdd(cnt + id.w, 1);
 }
 
@@ -159,8 +159,8 @@ __global__ void k_distance(const float* __restrict__ xp, float* dp, int* cnt, co
     if (w < FFSRL_FLOAT_EPS) return;
     float C = len - L0;
     v3 d = -C * (dir / len) * ks * active / w;
-    atomic_add3(dp, id.x, -(d * mA));
-    atomic_add3(dp, id.y, d * mB);
+    atomic_add3_pair(dp, id.x, -(d * mA));
+    atomic_add3_pair(dp, id.y, d * mB);
     atomicAdd(cnt + id.x, 1); atomicAdd(cnt + id.y, 1);
 }
 
@@ -187,8 +187,8 @@ __global__ void k_distance_xpbd(const float* __restrict__ xp, float* dp, int* cn
     float dl = -(C + alpha * l0) / (w + alpha);
     lam[e] = l0 + dl;
     v3 d = dl * normalize(dir);
-    atomic_add3(dp, id.x, -(d * mA));
-    atomic_add3(dp, id.y, d * mB);
+    atomic_add3_pair(dp, id.x, -(d * mA));
+    atomic_add3_pair(dp, id.y, d * mB);
     atomicAdd(cnt + id.x, 1); atomicAdd(cnt + id.y, 1);
 }
 
@@ -243,10 +243,10 @@ __global__ void k_connector(const float* __restrict__ xp, float* dp, int* cnt, c
     float C = len - rd * rmul;
     float s = wratio + wt * (b.x * b.x + b.y * b.y + b.z * b.z);
     v3 delta = (C / s) * (dir / len) * ks;
-    atomic_add3(dp, pid, -(delta * wratio));
-    atomic_add3(dp, ta, delta * wt * b.x);
-    atomic_add3(dp, tb, delta * wt * b.y);
-    atomic_add3(dp, tc, delta * wt * b.z);
+    atomic_add3_pair(dp, pid, -(delta * wratio));
+    atomic_add3_pair(dp, ta, delta * wt * b.x);
+    atomic_add3_pair(dp, tb, delta * wt * b.y);
+    atomic_add3_pair(dp, tc, delta * wt * b.z);
     atomicAdd(cnt + pid, 1); atomicAdd(cnt + ta, 1); atomicAdd(cnt + tb, 1); atomicAdd(cnt + tc, 1);
 }
 
@@ -276,9 +276,9 @@ __global__ void k_collide(const float* __restrict__ xp, float* cdp, const int* _
         tl = tl + length(rA) + length(rB) + length(rC);
     }
     if (tl > 0.0f) atomicAdd(in_collision + env, 1);
-    if (inv_mass[a] > 0.0f) atomic_add3(cdp, a, tA);
-    if (inv_mass[b] > 0.0f) atomic_add3(cdp, b, tB);
-    if (inv_mass[c] > 0.0f) atomic_add3(cdp, c, tC);
+    if (inv_mass[a] > 0.0f) atomic_add3_pair(cdp, a, tA);
+    if (inv_mass[b] > 0.0f) atomic_add3_pair(cdp, b, tB);
+    if (inv_mass[c] > 0.0f) atomic_add3_pair(cdp, c, tC);
 }
 
 __global__ void k_collide_apply(float* __restrict__ xp, float* __restrict__ cdp, int n) {

@@ -4,6 +4,7 @@
 // their mathematics: length = sqrt(dot), dot = (x*x' + y*y') + z*z',
 // normalize(v) = v/|v| for |v| > 0 else 0, min/max = a<b?a:b / a>b?a:b.
 #pragma once
+#include <cstdint>
 #include <cuda_runtime.h>
 
 namespace ffsrl {
@@ -40,6 +41,23 @@ __device__ __forceinline__ void st3(float* __restrict__ p, long long i, v3 v) {
 }
 __device__ __forceinline__ void atomic_add3(float* p, long long i, v3 v) {
     atomicAdd(p + 3 * i, v.x); atomicAdd(p + 3 * i + 1, v.y); atomicAdd(p + 3 * i + 2, v.z);
+}
+
+// The same three float additions in two atomic instructions: the 8-byte-aligned pair of
+// the entry (x, y for an even i, y, z for an odd one) as one float2 atomic (global memory,
+// sm_90 and later), the other component alone.  Each component is still added by one
+// float atomic, so the sums are those of atomic_add3 in some order.  Falls back to
+// atomic_add3 when p is not 8-byte aligned.
+__device__ __forceinline__ void atomic_add3_pair(float* p, long long i, v3 v) {
+    if (reinterpret_cast<uintptr_t>(p) & 7) {
+        atomic_add3(p, i, v);
+    } else if ((i & 1) == 0) {
+        atomicAdd(reinterpret_cast<float2*>(p + 3 * i), make_float2(v.x, v.y));
+        atomicAdd(p + 3 * i + 2, v.z);
+    } else {
+        atomicAdd(p + 3 * i, v.x);
+        atomicAdd(reinterpret_cast<float2*>(p + 3 * i + 1), make_float2(v.y, v.z));
+    }
 }
 
 // closestPointOnEdge (integrator.py:1520-1534)
