@@ -180,22 +180,41 @@ __device__ __forceinline__ bool slab(v3 ro, v3 rd, v3 lo, v3 hi, float& tnear) {
 }
 
 // Node test of the traversal: intersectAABB's hit && tmin < tMin (render.py:452-454).
-// The slab distances are first formed with the ray's reciprocal direction; when every
-// part of the decision is farther from its threshold than the rounding of that form can
-// move it (8 float ulps of the summed distances), the decision equals the reference's.
-// Otherwise -- and for non-finite distances -- the reference's divisions decide.
-__device__ __forceinline__ bool node_hit(v3 ro, v3 rd, v3 inv, v3 lo, v3 hi, float tMin) {
-    float t1 = (lo.x - ro.x) * inv.x, t2 = (hi.x - ro.x) * inv.x;
-    float t3 = (lo.y - ro.y) * inv.y, t4 = (hi.y - ro.y) * inv.y;
-    float t5 = (lo.z - ro.z) * inv.z, t6 = (hi.z - ro.z) * inv.z;
+// The slab distances are first formed as fma(lo, inv, -ro inv) with the ray's reciprocal
+// direction inv and the per-ray products ro inv.  Against the reference's
+// (lo - ro) / rd each differs by at most 4.01 u |t| + 1.02 u |ro inv| (u = 2^-24: the
+// reciprocal, the product ro inv and the fma each round once; the reference rounds the
+// difference and the quotient).  When every part of the decision is farther from its
+// threshold than that -- g = 8 u m + 4 u R below, m the sum of the six |t|, R the sum
+// of the three |ro inv| -- the decision equals the reference's.  Otherwise, and for
+// non-finite distances, the reference's divisions decide.
+struct RaySlab {
+    v3 inv;    // 1 / rd per axis
+    v3 roinv;  // ro * inv per axis
+    float g0;  // 4 u (|ro inv|.x + .y + .z)
+};
+
+__device__ __forceinline__ RaySlab ray_slab(v3 ro, v3 rd) {
+    RaySlab r;
+    r.inv = mk(1.0f / rd.x, 1.0f / rd.y, 1.0f / rd.z);
+    r.roinv = mk(ro.x * r.inv.x, ro.y * r.inv.y, ro.z * r.inv.z);
+    r.g0 = 2.38418579e-7f * ((fabsf(r.roinv.x) + fabsf(r.roinv.y)) + fabsf(r.roinv.z));  // 4 * 2^-24
+    return r;
+}
+
+__device__ __forceinline__ bool node_hit(v3 ro, v3 rd, const RaySlab& rs, v3 lo, v3 hi, float tMin) {
+    float t1 = fmaf(lo.x, rs.inv.x, -rs.roinv.x), t2 = fmaf(hi.x, rs.inv.x, -rs.roinv.x);
+    float t3 = fmaf(lo.y, rs.inv.y, -rs.roinv.y), t4 = fmaf(hi.y, rs.inv.y, -rs.roinv.y);
+    float t5 = fmaf(lo.z, rs.inv.z, -rs.roinv.z), t6 = fmaf(hi.z, rs.inv.z, -rs.roinv.z);
     // the sum of magnitudes bounds every distance and is infinite or NaN when any of them
-    // is, so the fast path only sees finite values, where fminf/fmaxf pick what the
-    // reference's comparisons pick (up to the sign of a zero, which no test below sees)
+    // is (or when the per-ray products are), so the fast path only sees finite values,
+    // where fminf/fmaxf pick what the reference's comparisons pick (up to the sign of a
+    // zero, which no test below sees)
     float m = ((fabsf(t1) + fabsf(t2)) + (fabsf(t3) + fabsf(t4))) + (fabsf(t5) + fabsf(t6));
-    if (m < 3.0e37f) {
+    if (m < 3.0e37f && rs.g0 < 3.0e37f) {
         float tmin = fmaxf(fmaxf(fminf(t1, t2), fminf(t3, t4)), fminf(t5, t6));
         float tmax = fminf(fminf(fmaxf(t1, t2), fmaxf(t3, t4)), fmaxf(t5, t6));
-        float g = m * 4.76837158e-7f;  // 8 * 2^-24 * m
+        float g = fmaf(m, 4.76837158e-7f, rs.g0);  // 8 u m + 4 u R
         // a certainly-false part decides a miss; all parts certainly true decide a hit
         if (tmax < -g || tmax - tmin < -2.0f * g || tmin > tMin + g) return false;
         if (tmax > g && tmax - tmin > 2.0f * g && tmin < tMin - g) return true;
@@ -267,7 +286,7 @@ __device__ int query_packed(const EnvView& ev, v3 ro, v3 rd, float& t_hit, v3& p
     int hit_tri = -1;
     int best_first = -1, best_k = 0;  // the kept hit's leaf and place in it
     int visits = 0;
-    const v3 inv = mk(1.0f / rd.x, 1.0f / rd.y, 1.0f / rd.z);
+    const RaySlab rs = ray_slab(ro, rd);
     while (count) {
         int node = stack[--count];
         if (++visits > ev.nn) {
@@ -275,7 +294,7 @@ __device__ int query_packed(const EnvView& ev, v3 ro, v3 rd, float& t_hit, v3& p
             return -1;
         }
         const float4 a = __ldg(ev.box + 2 * node), c = __ldg(ev.box + 2 * node + 1);
-        if (node_hit(ro, rd, inv, mk(a.x, a.y, a.z), mk(c.x, c.y, c.z), tMin)) {
+        if (node_hit(ro, rd, rs, mk(a.x, a.y, a.z), mk(c.x, c.y, c.z), tMin)) {
             int left = __float_as_int(a.w);
             if (left == -1) {
                 int fc = __float_as_int(c.w);
@@ -332,14 +351,14 @@ __device__ int query(const EnvView& ev, const float* __restrict__ pts, const int
     float tMin = 1e6f;
     int hit_tri = -1;
     int visits = 0;
-    const v3 inv = mk(1.0f / rd.x, 1.0f / rd.y, 1.0f / rd.z);
+    const RaySlab rs = ray_slab(ro, rd);
     while (count) {
         int node = stack[--count];
         if (++visits > ev.nn) {  // a valid tree visits each node at most once
             atomicExch(err, FFSRL_ERR_STACK_OVERFLOW);
             return -1;
         }
-        if (node_hit(ro, rd, inv, ld3(ev.amin, node), ld3(ev.amax, node), tMin)) {
+        if (node_hit(ro, rd, rs, ld3(ev.amin, node), ld3(ev.amax, node), tMin)) {
             int left = ev.left[node];
             if (left == -1) {
                 int first = ev.first[node];

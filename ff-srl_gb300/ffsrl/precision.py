@@ -35,53 +35,70 @@ def det_f(x: np.ndarray, tets: np.ndarray, rest_signed: np.ndarray) -> np.ndarra
     return (s6 / 6.0) / rest_signed.astype(np.float64)
 
 
-def compare(make, steps: int, accumulations=ACCUMULATIONS) -> dict:
+def compare(make, steps: int, accumulations=ACCUMULATIONS, every: int = 0, on_row=None) -> dict:
     """Steps identical models ``make()`` in each float32 accumulation and in the float64
-    build, and reports every float32 run against the float64 run."""
+    build, and reports every float32 run against the float64 run.  With ``every`` > 0 the
+    runs advance in lock step and ``on_row`` receives the report at every ``every``-th
+    step (the last one is returned)."""
     import torch
     m64 = make()
     p64 = BatchPlan(m64, precision=64)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-    ev[0].record()
-    p64.step(steps)
-    ev[1].record()
-    torch.cuda.synchronize()
-    x64 = p64.state_f64()["vertex"]
-    scale = np.abs(x64).max()
-    tets = m64.host["tetrahedron"]
-    rest = m64.host["tetrahedronRestVolumeSigned"]
-    j64 = det_f(x64, tets, rest)
-    out = {"envs": int(m64.numEnvs), "steps": steps, "substeps": m64.simSubsteps, "iterations": m64.simConstraints,
-           "vertices": int(m64.numVertices), "tets": int(m64.numTetrahedrons), "ms_f64": ev[0].elapsed_time(ev[1]),
-           "volume_err_f64": {"max": float(np.abs(j64 - 1).max()), "mean": float(np.abs(j64 - 1).mean())},
-           "finite": bool(np.isfinite(x64).all())}
-    del p64
+    runs = {}
     for acc in accumulations:
         m = make()
-        p = BatchPlan(m, accumulation=acc)
+        runs[acc] = (m, BatchPlan(m, accumulation=acc))
+    tets = m64.host["tetrahedron"]
+    rest = m64.host["tetrahedronRestVolumeSigned"]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ms = {"f64": 0.0} | {acc: 0.0 for acc in accumulations}
+    done = 0
+    out = None
+    chunk = every if every > 0 else steps
+    while done < steps:
+        k = min(chunk, steps - done)
         ev[0].record()
-        p.step(steps)
+        p64.step(k)
         ev[1].record()
         torch.cuda.synchronize()
-        x = m.vertex.cpu().numpy().astype(np.float64)
-        d = np.linalg.norm(x - x64, axis=1)
-        j = det_f(x, tets, rest)
-        out[acc] = {"max_pos_err_rel": float(d.max() / scale), "rms_pos_err_rel": float(np.sqrt((d ** 2).mean()) / scale),
-                    "volume_err": {"max": float(np.abs(j - 1).max()), "mean": float(np.abs(j - 1).mean())},
-                    "ms": ev[0].elapsed_time(ev[1]), "status_nonzero": int((p.env_status() != 0).sum())}
-        out["finite"] = out["finite"] and bool(np.isfinite(x).all())
-        del p
+        ms["f64"] += ev[0].elapsed_time(ev[1])
+        for acc, (m, p) in runs.items():
+            ev[0].record()
+            p.step(k)
+            ev[1].record()
+            torch.cuda.synchronize()
+            ms[acc] += ev[0].elapsed_time(ev[1])
+        done += k
+        x64 = p64.state_f64()["vertex"]
+        scale = np.abs(x64).max()
+        j64 = det_f(x64, tets, rest)
+        out = {"envs": int(m64.numEnvs), "steps": done, "substeps": m64.simSubsteps, "iterations": m64.simConstraints,
+               "vertices": int(m64.numVertices), "tets": int(m64.numTetrahedrons), "ms_f64": ms["f64"],
+               "volume_err_f64": {"max": float(np.abs(j64 - 1).max()), "mean": float(np.abs(j64 - 1).mean())},
+               "finite": bool(np.isfinite(x64).all())}
+        for acc, (m, p) in runs.items():
+            x = m.vertex.cpu().numpy().astype(np.float64)
+            d = np.linalg.norm(x - x64, axis=1)
+            j = det_f(x, tets, rest)
+            out[acc] = {"max_pos_err_rel": float(d.max() / scale), "rms_pos_err_rel": float(np.sqrt((d ** 2).mean()) / scale),
+                        "volume_err": {"max": float(np.abs(j - 1).max()), "mean": float(np.abs(j - 1).mean())},
+                        "ms": ms[acc], "status_nonzero": int((p.env_status() != 0).sum())}
+            out["finite"] = out["finite"] and bool(np.isfinite(x).all())
+        if on_row is not None:
+            on_row(dict(out))
     return out
 
 
-def config3(envs: int = 4, steps: int = 300, device: str = "cuda:0", accumulations=ACCUMULATIONS) -> dict:
+def config3(envs: int = 4, steps: int = 300, device: str = "cuda:0", accumulations=ACCUMULATIONS, every: int = 0,
+            on_row=None) -> dict:
     """Config 3: the 12/8/6 cm ellipsoid at Poisson ratio 0.49, 16 substeps x 50 iterations,
     the liver constraint set without contact, ``envs`` identical envs."""
     from . import meshgen as mg
     mesh = mg.ellipsoid()
     make = lambda: sc.liver_model(device, envs, meshes=[mesh] * envs, nu=0.49, substeps=16, iterations=50,
                                   collide=False)[0]
-    return {"config": "3 ellipsoid, nu 0.49, 16 x 50"} | compare(make, steps, accumulations) | {"nu": 0.49}
+    tag = {"config": "3 ellipsoid, nu 0.49, 16 x 50"}
+    row = None if on_row is None else (lambda r: on_row(tag | r | {"nu": 0.49}))
+    return tag | compare(make, steps, accumulations, every=every, on_row=row) | {"nu": 0.49}
 
 
 def all_configs(device: str = "cuda:0", steps: int = 100, steps3: int = 300, envs3: int = 4, which=(0, 1, 2, 3)):
@@ -116,5 +133,9 @@ if __name__ == "__main__":
     import sys
     which = tuple(int(c) for c in sys.argv[1]) if len(sys.argv) > 1 else (0, 1, 2, 3)
     steps3 = int(sys.argv[2]) if len(sys.argv) > 2 else 300
-    for row in all_configs(which=which, steps3=steps3):
-        print(json.dumps(row), flush=True)
+    if which == (3,):
+        # config 3 alone: one env, every 25 steps a row, so a long run reports as it goes
+        config3(1, steps3, every=25, on_row=lambda r: print(json.dumps(r), flush=True))
+    else:
+        for row in all_configs(which=which, steps3=steps3):
+            print(json.dumps(row), flush=True)
